@@ -1,0 +1,276 @@
+"""perform_traj_simulation: the reference's keyword API over the C ABI.
+
+Mirrors src/TrajectorySimulation.jl:103-161 (keywords, defaults and
+checks).  The batch loop at :154-157 becomes one etraj_run call on the GPU;
+there is no CPU path.  Output: the reference writes JLD2/HDF5 files; here the
+result is returned as a dict with the same keys as that file
+(px, py[, pz], momentum_spec, ion_prob, ion_prob_uncollected,
+num_effective_traj, params_text) and, when output_path is given, saved as a
+NumPy .npz archive.
+"""
+import ctypes as C
+import math
+import warnings
+
+import numpy as np
+
+from . import abi
+from .lasers import Laser, MonochromaticLaser, BichromaticLaser
+from .targets import Target, SAEAtomBase
+
+_METHODS = {"ADK": abi.SAMPLER_ADK, "SPANE": abi.SAMPLER_SPANE, "SFAAE": abi.SAMPLER_SPANE,
+            "SPA": abi.SAMPLER_SPA, "SFA": abi.SAMPLER_SPA}
+_MOLECULAR = {"MOADK", "MOSPANE", "MOSFAAE", "MOSPA", "MOSFA", "WFAT"}
+_PHASES = {"CTMC": abi.PHASE_CTMC, "QTMC": abi.PHASE_QTMC, "SCTS": abi.PHASE_SCTS}
+_PREFIX_BITS = {"Pre": abi.PREFIX_PRE, "PreCC": abi.PREFIX_PRECC, "Jac": abi.PREFIX_JAC}
+_PRECISIONS = {"fp64": abi.PRECISION_FP64, "fp32_bulk": abi.PRECISION_FP32_BULK}
+
+
+def _sym(x):
+    return x[1:] if isinstance(x, str) and x.startswith(":") else x
+
+
+def rate_prefix_bits(rate_prefix):
+    """:Exp, :Full, :Pre, :PreCC, :Jac or a collection of them -> ETRAJ_PREFIX_* mask
+    (ADKSampler.jl:49-77)."""
+    if isinstance(rate_prefix, str):
+        p = _sym(rate_prefix)
+        if p == "Exp":
+            return 0
+        if p == "Full":
+            return abi.PREFIX_PRECC | abi.PREFIX_JAC
+        if p in _PREFIX_BITS:
+            return _PREFIX_BITS[p]
+        raise ValueError("[ADKSampler] Undefined tunneling rate prefix [%s]." % p)
+    items = [_sym(p) for p in rate_prefix]
+    if not all(p in _PREFIX_BITS for p in items):
+        raise ValueError("[ADKSampler] Undefined tunneling rate prefix [%s]." % (items,))
+    if "Pre" in items and "PreCC" in items:
+        raise ValueError("[ADKSampler] Rate prefixes [Pre] & [PreCC] conflict.")
+    bits = 0
+    for p in items:
+        bits |= _PREFIX_BITS[p]
+    return bits
+
+
+def make_job(*, init_cond_method, laser, target, dimension, sample_t_intv, sample_t_num,
+             traj_t_final, final_p_max, final_p_num, ss_kd_max=0.0, ss_kd_num=0, ss_kz_max=0.0,
+             ss_kz_num=0, mc_kt_num=0, mc_kd_max=0.0, mc_kz_max=0.0, traj_phase_method="CTMC",
+             traj_rtol=1e-6, sample_monte_carlo=False, sample_cutoff_limit=1e-16,
+             rate_prefix="Full", mol_orbit_ridx=0, precision="fp64", seed=0):
+    """Checks the keywords as TrajectorySimulationJob (TrajectorySimulation.jl:164-298) and
+    the sampler constructors do, and packs them into an etraj_job."""
+    method = _sym(init_cond_method)
+    if method in _MOLECULAR:
+        raise NotImplementedError("[ElectronSamplers] molecular method `%s` is not part of this "
+                                  "engine (molecular targets are not built)." % method)
+    if method not in _METHODS:
+        raise ValueError("[ElectronSamplers] Undefined initial condition method [%s]." % method)
+    if not isinstance(laser, Laser):
+        raise TypeError("`laser` must be a Laser.")
+    if not isinstance(target, SAEAtomBase):
+        raise NotImplementedError("only atomic targets (HydrogenLikeAtom, SAEAtom) are supported.")
+    phase = _sym(traj_phase_method)
+    if phase not in _PHASES:
+        raise ValueError("[ADKSampler] Undefined phase method [%s]." % phase)
+    assert sample_t_intv[0] < sample_t_intv[1], \
+        "[TrajectorySimulationJob] `sample_t_intv` must be a valid interval."
+    assert traj_t_final > sample_t_intv[1], \
+        "[TrajectorySimulationJob] `traj_t_final` must be greater than the last time point of `sample_t_intv`."
+    assert dimension in (2, 3), "[TrajectorySimulationJob] `dimension` must be either 2 or 3."
+    assert len(final_p_max) == len(final_p_num) == dimension, \
+        "[TrajectorySimulationJob] `length(final_p_max)` and `length(final_p_num)` should match `dimension`."
+    bits = rate_prefix_bits(rate_prefix)
+    if (bits & abi.PREFIX_PRECC) and isinstance(laser, BichromaticLaser):
+        warnings.warn("[ADKSampler] Laser is not monochromatic, Coulomb correction in rate prefix is unavailable.")
+    j = abi.Job()
+    j.init_cond_method = _METHODS[method]
+    j.dimension = dimension
+    j.sample_monte_carlo = 1 if sample_monte_carlo else 0
+    j.rate_prefix = bits
+    j.traj_phase_method = _PHASES[phase]
+    j.precision = _PRECISIONS[precision]
+    j.sample_t_intv[0], j.sample_t_intv[1] = float(sample_t_intv[0]), float(sample_t_intv[1])
+    j.sample_t_num = int(sample_t_num)
+    j.traj_t_final = float(traj_t_final)
+    j.traj_rtol = float(traj_rtol)
+    for d in range(3):
+        j.final_p_max[d] = float(final_p_max[d]) if d < dimension else 0.0
+        j.final_p_num[d] = int(final_p_num[d]) if d < dimension else 1
+    j.ss_kd_max, j.ss_kd_num = float(ss_kd_max), int(ss_kd_num)
+    j.ss_kz_max, j.ss_kz_num = float(ss_kz_max), int(ss_kz_num)
+    j.mc_kt_num, j.mc_kd_max, j.mc_kz_max = int(mc_kt_num), float(mc_kd_max), float(mc_kz_max)
+    j.sample_cutoff_limit = float(sample_cutoff_limit)
+    j.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+    j.laser = laser.to_c()
+    j.target = target.to_c()
+    return j
+
+
+class EtrajError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("etraj status %d: %s" % (status, message))
+        self.status = status
+
+
+class Engine:
+    """One etraj_ctx: a device, its buffers and its stream."""
+
+    def __init__(self, device=0, hbm_budget_bytes=0):
+        self.lib = abi.load_library()
+        self.ctx = C.c_void_p()
+        st = self.lib.etraj_create(C.byref(self.ctx), device, hbm_budget_bytes)
+        if st != abi.OK:
+            raise EtrajError(st, "etraj_create failed on device %d" % device)
+
+    def close(self):
+        if self.ctx:
+            self.lib.etraj_destroy(self.ctx)
+            self.ctx = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != abi.OK:
+            msg = self.lib.etraj_last_error(self.ctx)
+            raise EtrajError(st, msg.decode() if msg else "")
+
+    def set_stream(self, stream_handle):
+        self._check(self.lib.etraj_set_stream(self.ctx, C.c_void_p(stream_handle or 0)))
+
+    def run(self, job, want_spectrum=True, want_amplitude=False):
+        res = abi.Result()
+        spec = amp = None
+        if want_spectrum:
+            spec = np.zeros(job.grid_size, dtype=np.float64)
+            res.momentum_spec = abi.dptr(spec)
+        if want_amplitude and job.traj_phase_method != abi.PHASE_CTMC:
+            amp = np.zeros(2 * job.grid_size, dtype=np.float64)
+            res.amplitude = abi.dptr(amp)
+        self._check(self.lib.etraj_run(self.ctx, C.byref(job), C.byref(res)))
+        return res, spec, amp
+
+    def batch_info(self, job):
+        nb, mx = C.c_int64(), C.c_int64()
+        self._check(self.lib.etraj_batch_info(C.byref(job), C.byref(nb), C.byref(mx)))
+        return nb.value, mx.value
+
+    def sample_batch(self, job, batch_id):
+        """gen_electron_batch(sp, batch_id): (rows, count) matrix, or None when empty."""
+        _, mx = self.batch_info(job)
+        buf = np.zeros(job.rows * max(mx, 1), dtype=np.float64)
+        n = C.c_int64()
+        self._check(self.lib.etraj_sample_batch(self.ctx, C.byref(job), batch_id, abi.dptr(buf), mx,
+                                                C.byref(n)))
+        if n.value == 0:
+            return None
+        return buf[: job.rows * n.value].reshape(n.value, job.rows).T
+
+    def sample_all(self, job):
+        nb, mx = self.batch_info(job)
+        cap = nb * mx
+        buf = np.zeros(job.rows * max(cap, 1), dtype=np.float64)
+        n = C.c_int64()
+        self._check(self.lib.etraj_sample_all(self.ctx, C.byref(job), abi.dptr(buf), cap, C.byref(n)))
+        return buf[: job.rows * n.value].reshape(n.value, job.rows)
+
+    def integrate(self, job, init):
+        """init: (n, rows) float64 -> (final (n, state), status (n,), steps (n,))."""
+        init = np.ascontiguousarray(init, dtype=np.float64)
+        n = init.shape[0]
+        fin = np.zeros((n, job.state_size), dtype=np.float64)
+        status = np.zeros(n, dtype=np.int32)
+        steps = np.zeros(n, dtype=np.int32)
+        self._check(self.lib.etraj_integrate(self.ctx, C.byref(job), n, abi.dptr(init), abi.dptr(fin),
+                                             abi.i32ptr(status), abi.i32ptr(steps)))
+        return fin, status, steps
+
+    def submit(self, job):
+        t = C.c_uint64()
+        self._check(self.lib.etraj_submit(self.ctx, C.byref(job), C.byref(t)))
+        return t.value
+
+    def poll(self, ticket, res):
+        st = self.lib.etraj_poll(self.ctx, ticket, C.byref(res))
+        if st == abi.ERR_NOT_READY:
+            return False
+        self._check(st)
+        return True
+
+    def wait(self, ticket, res):
+        self._check(self.lib.etraj_wait(self.ctx, ticket, C.byref(res)))
+
+
+_default_engine = None
+
+
+def default_engine():
+    global _default_engine
+    if _default_engine is None:
+        _default_engine = Engine()
+    return _default_engine
+
+
+def _axis(pmax, num):
+    return np.linspace(-pmax, pmax, num) if num > 1 else np.array([0.0])
+
+
+def perform_traj_simulation(*, init_cond_method, laser, target, dimension, sample_t_intv,
+                            sample_t_num, traj_t_final, final_p_max, final_p_num,
+                            ss_kd_max=0.0, ss_kd_num=0, ss_kz_max=0.0, ss_kz_num=0,
+                            mc_kt_num=0, mc_kd_max=0.0, mc_kz_max=0.0,
+                            traj_phase_method="CTMC", traj_rtol=1e-6, output_fmt="npz",
+                            output_compress=True, output_path=None, sample_monte_carlo=False,
+                            sample_cutoff_limit=1e-16, rate_prefix="Full", mol_orbit_ridx=0,
+                            show_progress=False, precision="fp64", seed=0, engine=None):
+    """Performs a semiclassical trajectory simulation (TrajectorySimulation.jl:103-161) on the GPU.
+
+    Returns a dict with the keys of the reference's output file.  Extra keywords:
+    `precision` ("fp64" or "fp32_bulk"), `seed` (Monte-Carlo stream), `engine`."""
+    job = make_job(init_cond_method=init_cond_method, laser=laser, target=target,
+                   dimension=dimension, sample_t_intv=sample_t_intv, sample_t_num=sample_t_num,
+                   traj_t_final=traj_t_final, final_p_max=final_p_max, final_p_num=final_p_num,
+                   ss_kd_max=ss_kd_max, ss_kd_num=ss_kd_num, ss_kz_max=ss_kz_max,
+                   ss_kz_num=ss_kz_num, mc_kt_num=mc_kt_num, mc_kd_max=mc_kd_max,
+                   mc_kz_max=mc_kz_max, traj_phase_method=traj_phase_method, traj_rtol=traj_rtol,
+                   sample_monte_carlo=sample_monte_carlo, sample_cutoff_limit=sample_cutoff_limit,
+                   rate_prefix=rate_prefix, precision=precision, seed=seed)
+    eng = engine or default_engine()
+    res, spec, amp = eng.run(job, want_spectrum=True,
+                             want_amplitude=(_sym(traj_phase_method) != "CTMC"))
+    shape = tuple(int(x) for x in final_p_num)
+    out = {
+        "px": _axis(final_p_max[0], final_p_num[0]),
+        "py": _axis(final_p_max[1], final_p_num[1]),
+        "momentum_spec": spec.reshape(shape, order="F"),
+        "ion_prob": res.ion_prob,
+        "ion_prob_uncollected": res.ion_prob_uncollected,
+        "num_effective_traj": res.num_effective_traj,
+        "num_failed_traj": res.num_failed_traj,
+        "params_text": _params_text(locals()),
+    }
+    if dimension == 3:
+        out["pz"] = _axis(final_p_max[2], final_p_num[2])
+    if amp is not None:
+        out["amplitude"] = (amp[0::2] + 1j * amp[1::2]).reshape(shape, order="F")
+    if output_path:
+        path = output_path if output_path.endswith(".npz") else output_path + ".npz"
+        np.savez_compressed(path, **{k: v for k, v in out.items()}) if output_compress \
+            else np.savez(path, **out)
+        out["output_path"] = path
+    return out
+
+
+def _params_text(kw):
+    keys = ["init_cond_method", "sample_t_intv", "sample_t_num", "sample_monte_carlo",
+            "sample_cutoff_limit", "traj_phase_method", "traj_rtol", "traj_t_final",
+            "final_p_max", "final_p_num", "ss_kd_max", "ss_kd_num", "ss_kz_max", "ss_kz_num",
+            "mc_kt_num", "mc_kd_max", "mc_kz_max", "rate_prefix", "precision", "seed"]
+    lines = ["%s: %r" % (k, kw[k]) for k in keys if k in kw]
+    lines.append("laser: %r" % (kw.get("laser"),))
+    lines.append("target: %r" % (getattr(kw.get("target"), "__dict__", None),))
+    return "\n".join(lines)

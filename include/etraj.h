@@ -1,0 +1,215 @@
+/*
+ * etraj.h -- C ABI of the GB300 ensemble-trajectory engine.
+ *
+ * This library replaces the batch loop of eTraj.jl's trajectory simulation
+ * (src/TrajectorySimulation.jl:154-157, `@threads for i in 1:batch_num
+ * launch_and_collect!(job, i)`) with one call that runs every stage on one
+ * GPU: initial-condition sampling (gen_electron_batch in
+ * src/ElectronSamplers/ADKSampler.jl, SPANESampler.jl, SPASampler.jl), the adaptive Tsit5 ensemble solve
+ * (src/TrajectorySimulation.jl:334-342 / 429-437), the asymptotic Kepler
+ * step and SCTS phase correction (:356-374 / :451-469) and the spectrum
+ * collection (:375-393 / :470-493, reduced as in write_output! :521-543).
+ *
+ * Conventions
+ *  - All physical quantities are in atomic units, except the laser's peak
+ *    intensity (W/cm^2) and wavelength (nm), as in the reference's laser
+ *    constructors (src/Lasers/Cos4Laser.jl:44-74).
+ *  - Plain C types only; every array is caller-owned host memory unless an
+ *    entry point says otherwise.  No exceptions cross the ABI: every entry
+ *    point returns an etraj_status and etraj_last_error() explains it.
+ *  - Spectra are laid out in Julia column-major order (px fastest), so a
+ *    Julia caller can pass pointer(Array) under GC.@preserve.
+ *  - Sample matrices use the reference's `init` layout (ADKSampler.jl:299-303):
+ *    one column per electron, rows x,y[,z],kx,ky[,kz],t0,rate[,phase],
+ *    stored column-major (the rows of one electron are contiguous).
+ */
+#ifndef ETRAJ_H
+#define ETRAJ_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ETRAJ_ABI_VERSION 1
+
+typedef enum etraj_status {
+    ETRAJ_OK = 0,
+    ETRAJ_ERR_INVALID_ARGUMENT = 1, /* a check the reference makes with @assert / error() */
+    ETRAJ_ERR_UNSUPPORTED = 2,      /* valid in the reference, not built here */
+    ETRAJ_ERR_CUDA = 3,             /* a CUDA runtime call failed */
+    ETRAJ_ERR_OUT_OF_MEMORY = 4,    /* the job does not fit the context's HBM budget */
+    ETRAJ_ERR_TIMEOUT = 5,          /* a device work budget ran out */
+    ETRAJ_ERR_NOT_READY = 6,        /* etraj_poll: the job is still running */
+    ETRAJ_ERR_NOT_FOUND = 7         /* unknown ticket */
+} etraj_status;
+
+/* ---- lasers: src/Lasers/{Cos4,Cos2,Gaussian,Bichromatic}Laser.jl ---------- */
+typedef enum etraj_laser_kind {
+    ETRAJ_LASER_COS4 = 0,        /* Cos4Laser.jl:7 */
+    ETRAJ_LASER_COS2 = 1,        /* Cos2Laser.jl:7 */
+    ETRAJ_LASER_GAUSSIAN = 2,    /* GaussianLaser.jl:7 */
+    ETRAJ_LASER_BICHROMATIC = 3  /* BichromaticLaser.jl:7 */
+} etraj_laser_kind;
+
+typedef struct etraj_mono_laser {
+    int32_t kind;      /* ETRAJ_LASER_COS4, _COS2 or _GAUSSIAN */
+    int32_t reserved;
+    double peak_int;   /* W/cm^2 */
+    double wave_len;   /* nm */
+    double cyc_num;    /* Cos4/Cos2: number of cycles N; Gaussian: spread_cyc_num (sigma in cycles) */
+    double ellip;      /* -1 <= ellip <= 1 */
+    double azi;        /* azimuth of the principal axis, rad */
+    double cep;        /* carrier-envelope phase, rad */
+    double t_shift;    /* a.u. */
+} etraj_mono_laser;
+
+typedef struct etraj_laser {
+    int32_t kind;               /* monochromatic: mono[0]; BICHROMATIC: mono[0] + mono[1] */
+    int32_t reserved;
+    etraj_mono_laser mono[2];
+    double delay;               /* BICHROMATIC: delay of mono[1] (BichromaticLaser.jl:73-85) */
+} etraj_laser;
+
+/* ---- targets: src/Targets/{HydrogenLikeAtom,SAEAtom}.jl --------------------- */
+typedef enum etraj_target_kind {
+    ETRAJ_TARGET_HYDROGEN_LIKE = 0, /* HydrogenLikeAtom.jl:7 */
+    ETRAJ_TARGET_SAE = 1            /* SAEAtom.jl:7 */
+} etraj_target_kind;
+
+typedef struct etraj_target {
+    int32_t kind;
+    int32_t Z;              /* asymptotic nuclear charge (nucl_charge) */
+    int32_t l, m;
+    double Ip;              /* a.u. */
+    double asymp_coeff;     /* C_kl, already resolved (the :hartree default is SAEAtomBase_shared.jl:3-11) */
+    double quan_ax_theta;   /* rad */
+    double quan_ax_phi;     /* rad */
+    double a1, b1, a2, b2, a3, b3; /* SAE potential parameters; ignored for hydrogen-like targets */
+    double soft_core;
+} etraj_target;
+
+/* ---- job: the keyword arguments of perform_traj_simulation ---------------- */
+typedef enum etraj_sampler_kind {
+    ETRAJ_SAMPLER_ADK = 0,   /* :ADK   ADKSampler.jl */
+    ETRAJ_SAMPLER_SPANE = 1, /* :SPANE SPANESampler.jl */
+    ETRAJ_SAMPLER_SPA = 2    /* :SPA   SPASampler.jl */
+} etraj_sampler_kind;
+
+/* rate_prefix bit mask (ADKSampler.jl:49-77): :Exp = 0, :Full = PRECC|JAC */
+#define ETRAJ_PREFIX_PRE 1
+#define ETRAJ_PREFIX_PRECC 2
+#define ETRAJ_PREFIX_JAC 4
+
+typedef enum etraj_phase_method {
+    ETRAJ_PHASE_CTMC = 0,
+    ETRAJ_PHASE_QTMC = 1,
+    ETRAJ_PHASE_SCTS = 2
+} etraj_phase_method;
+
+typedef enum etraj_precision {
+    ETRAJ_PRECISION_FP64 = 0,      /* one thread per trajectory, FP64, bit-compatible with the oracle */
+    ETRAJ_PRECISION_FP32_BULK = 1  /* persistent work-stealing integrator, FP32 stages, compensated state */
+} etraj_precision;
+
+typedef struct etraj_job {
+    int32_t init_cond_method;    /* etraj_sampler_kind */
+    int32_t dimension;           /* 2 or 3 */
+    int32_t sample_monte_carlo;  /* 0: step sampling (ss_*), 1: Monte-Carlo (mc_*) */
+    int32_t rate_prefix;         /* ETRAJ_PREFIX_* mask */
+    int32_t traj_phase_method;   /* etraj_phase_method */
+    int32_t precision;           /* etraj_precision */
+    double sample_t_intv[2];     /* a.u. */
+    int64_t sample_t_num;
+    double traj_t_final;         /* a.u. */
+    double traj_rtol;            /* reference default 1e-6 */
+    double final_p_max[3];
+    int64_t final_p_num[3];      /* 2D jobs ignore index 2 */
+    double ss_kd_max;
+    int64_t ss_kd_num;
+    double ss_kz_max;
+    int64_t ss_kz_num;
+    int64_t mc_kt_num;
+    double mc_kd_max;
+    double mc_kz_max;
+    double sample_cutoff_limit;  /* reference default 1e-16 */
+    uint64_t seed;               /* Monte-Carlo stream; the reference draws from an unseeded global RNG */
+    etraj_laser laser;
+    etraj_target target;
+} etraj_job;
+
+typedef struct etraj_result {
+    /* caller-owned outputs; either pointer may be NULL to skip that copy */
+    double* momentum_spec;   /* prod(final_p_num) doubles, column-major; |amplitude|^2 for QTMC/SCTS */
+    double* amplitude;       /* QTMC/SCTS: 2*prod(final_p_num) doubles (re,im) before |.|^2 */
+    /* scalars written by the library (write_output!, TrajectorySimulation.jl:541-543) */
+    double ion_prob;
+    double ion_prob_uncollected;
+    int64_t num_effective_traj;  /* electrons that survived the cutoff, failed ODE solves included */
+    int64_t num_failed_traj;     /* ODE retcode != Success: skipped, as at :347-355 */
+    int64_t num_ionized_traj;    /* E_inf >= 0 */
+    int64_t num_steps;           /* Tsit5 step attempts over all trajectories */
+    int64_t num_kernel_launches; /* kernels this library launched for the job */
+    double elapsed_ms;           /* device time from the first to the last launch */
+} etraj_result;
+
+typedef struct etraj_ctx etraj_ctx;
+
+/* ---- library and context ---------------------------------------------------- */
+const char* etraj_version(void);
+
+/* Creates a context on `device`.  hbm_budget_bytes == 0 means "all free memory
+ * minus 1 GiB".  A context owns its device buffers and one CUDA stream. */
+int etraj_create(etraj_ctx** ctx, int device, size_t hbm_budget_bytes);
+void etraj_destroy(etraj_ctx* ctx);
+const char* etraj_last_error(const etraj_ctx* ctx);
+
+/* Runs subsequent work on a caller-provided cudaStream_t (NULL restores the
+ * context's own stream). */
+int etraj_set_stream(etraj_ctx* ctx, void* cuda_stream);
+
+/* Host-only validation with the reference's messages, e.g.
+ * TrajectorySimulation.jl:178-186, ADKSampler.jl:44-47,79-105. */
+int etraj_validate(const etraj_job* job, char* msg, size_t msg_len);
+
+/* Replaces the `@threads for i in 1:batch_num` loop: samples, integrates,
+ * collects and reduces the whole job on the device, then copies the spectrum
+ * into out->momentum_spec / out->amplitude (skipped when NULL). */
+int etraj_run(etraj_ctx* ctx, const etraj_job* job, etraj_result* out);
+
+/* ---- component entry points (parity tests and the Julia shim's debug path) --- */
+
+/* Number of batches (= time samples, ADKSampler.jl:153-155) and the largest
+ * batch (:158-164). */
+int etraj_batch_info(const etraj_job* job, int64_t* batch_num, int64_t* batch_max_size);
+
+/* gen_electron_batch(sp, batch_id) for one 1-based batch id: writes the
+ * surviving electrons' columns into `init` (capacity columns of `rows`
+ * doubles) and their count into *count (0 where the reference returns
+ * `nothing`).  rows = 6/7 (2D) or 8/9 (3D), CTMC/phase. */
+int etraj_sample_batch(etraj_ctx* ctx, const etraj_job* job, int64_t batch_id,
+                       double* init, int64_t capacity, int64_t* count);
+
+/* The sampling stage of the whole job, batches concatenated in order. */
+int etraj_sample_all(etraj_ctx* ctx, const etraj_job* job,
+                     double* init, int64_t capacity, int64_t* count);
+
+/* The ensemble ODE solve for n electrons given in reference `init` layout.
+ * final_state: n columns of the ODE state (x,y[,z],px,py[,pz][,phase]);
+ * status: 0 Success, 1 MaxIters, 2 DtLessThanMin, 3 Unstable; steps: step
+ * attempts.  Any output pointer may be NULL. */
+int etraj_integrate(etraj_ctx* ctx, const etraj_job* job, int64_t n, const double* init,
+                    double* final_state, int32_t* status, int32_t* steps);
+
+/* ---- asynchronous jobs (serving loop) ---------------------------------------- */
+int etraj_submit(etraj_ctx* ctx, const etraj_job* job, uint64_t* ticket);
+int etraj_poll(etraj_ctx* ctx, uint64_t ticket, etraj_result* out);
+int etraj_wait(etraj_ctx* ctx, uint64_t ticket, etraj_result* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ETRAJ_H */

@@ -1,0 +1,36 @@
+/* oracle_sampler.h -- sampler state of the CPU oracle (TEST INFRASTRUCTURE ONLY). */
+#ifndef ETRAJ_ORACLE_SAMPLER_H
+#define ETRAJ_ORACLE_SAMPLER_H
+
+#include "oracle_internal.h"
+
+typedef struct {
+    int method, dim, mc, prefix, phase, rows, mono;
+    double cutoff;
+    uint64_t seed;
+    o_laser laser;
+    double Ip, Z, kappa, n, c, cc_base, e_pre, C, q_theta, q_phi;
+    int l, m;
+    dm_cplx Plm[9];
+    int64_t n_t, n_kd, n_kz, n_cand;
+    double *t, *kd, *kz;
+    double mc_kd_max, mc_kz_max, dkdt;
+} o_sampler;
+
+typedef struct {
+    double tr, Fx, Fy, dFx, dFy, F, phi, sphi, cphi, gamma, c_cc, W;
+    double ny[3], nz[3];
+    dm_cplx D[9];
+} o_batch;
+
+void o_philox4x32(uint32_t c[4], uint64_t seed);
+double o_u53(uint32_t a, uint32_t b);
+double o_linrange(double a, double b, int64_t n, int64_t i);
+int o_sampler_init(const etraj_job* job, o_sampler* S);
+void o_sampler_free(o_sampler* S);
+void o_batch_prepare(const o_sampler* S, int64_t b, o_batch* B);
+int o_candidate(const o_sampler* S, const o_batch* B, double kd0, double kz0, double* row);
+void o_mc_point(const o_sampler* S, int64_t b, int64_t i, double* kd0, double* kz0);
+int64_t o_sample_batch(const o_sampler* S, int64_t b, double* init, int64_t capacity);
+
+#endif
