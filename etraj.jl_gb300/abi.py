@@ -111,7 +111,7 @@ SIGNATURES = [
     ("etraj_sample_batch", C.c_int, [C.c_void_p, C.POINTER(Job), C.c_int64, _DP, C.c_int64, _I64P]),
     ("etraj_sample_all", C.c_int, [C.c_void_p, C.POINTER(Job), _DP, C.c_int64, _I64P]),
     ("etraj_integrate", C.c_int, [C.c_void_p, C.POINTER(Job), C.c_int64, _DP, _DP, _I32P, _I32P]),
-    ("etraj_submit", C.c_int, [C.c_void_p, C.POINTER(Job), C.POINTER(C.c_uint64)]),
+    ("etraj_submit", C.c_int, [C.c_void_p, C.POINTER(Job), C.POINTER(Result), C.POINTER(C.c_uint64)]),
     ("etraj_poll", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(Result)]),
     ("etraj_wait", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(Result)]),
 ]

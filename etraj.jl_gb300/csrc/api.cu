@@ -1,0 +1,805 @@
+// api.cu -- the C ABI of include/etraj.h: contexts, validation, host-side job
+// set-up and the orchestration of the device pipeline.
+//
+// Pipeline of etraj_run (all launches on the context's stream, one host
+// synchronization at the end):
+//   k_batch_prepare  per time sample   (gen_electron_batch prologue)
+//   k_sample         per candidate     (gen_electron_batch loop body)
+//   compaction       order-preserving survivor list
+//   k_integrate_*    per survivor      (Tsit5 solve + collection)
+//   deposit          radix sort + segmented sums + canonical reductions
+// This replaces the `@threads for i in 1:batch_num` loop of
+// src/TrajectorySimulation.jl:154-157 and the reduction of write_output!
+// (:521-543).
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+
+using namespace etraj;
+
+#define ETRAJ_VERSION_STRING "etraj-gb300 1.0 (sm_103a)"
+
+namespace etraj {
+int launch_sample_range(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
+                        const DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
+                        cudaStream_t s);
+}
+
+namespace {
+
+constexpr bool kHaveFp32Bulk = false;
+
+// ---- host-side job set-up (same expressions as the reference's getters) ----------
+void mono_prepare(const etraj_mono_laser& in, DMono& L) {
+    std::memset(&L, 0, sizeof L);
+    L.kind = in.kind;
+    L.omega = 45.563352525 / in.wave_len;        // AngFreq, Cos4Laser.jl:81
+    L.period = 6.283185307179586 / L.omega;      // Period = 2pi/omega
+    L.F0 = std::sqrt((in.peak_int / (1.0 + in.ellip * in.ellip)) / 3.50944521e16);  // :85
+    L.A0 = L.F0 / L.omega;
+    L.N = in.cyc_num;
+    L.cep = in.cep;
+    L.t_shift = in.t_shift;
+    L.ellip = in.ellip;
+    L.azi_zero = (in.azi == 0.0);
+    dm_sincos(in.azi, &L.sphi, &L.cphi);
+    if (L.kind == ETRAJ_LASER_GAUSSIAN) {
+        L.sigma = in.cyc_num * L.period;          // SpreadDuration, GaussianLaser.jl:85
+        L.inv_s2 = 1.0 / (L.sigma * L.sigma);
+        L.inv_2s2 = 1.0 / (2.0 * (L.sigma * L.sigma));
+    } else {
+        L.w2n = L.omega / (2.0 * L.N);
+        L.cN = (L.kind == ETRAJ_LASER_COS4) ? 2.0 / L.N : 1.0 / L.N;
+        L.k = 200.0 / L.period;
+        L.Npiw = (L.N * 3.141592653589793) / L.omega;
+    }
+}
+
+double fact(int n) {
+    double f = 1.0;
+    for (int i = 2; i <= n; ++i) f *= (double)i;
+    return f;
+}
+
+// Prefactor of the solid harmonic Y_{l m} of shared_methods.jl:21.
+dm_cplx sph_prefactor(int l, int m, double kappa) {
+    double A = (m & 1) ? -1.0 : 1.0;
+    double B = std::sqrt((((2.0 * l + 1.0) / 12.566370614359172) * fact(l - m)) / fact(l + m));
+    dm_cplx C = dm_cpowi(dm_c(0.0, -kappa), l);
+    dm_cplx P = dm_cdiv(dm_c(A * B, 0.0), C);
+    return dm_cscale(P, fact(l + m));
+}
+
+void two_sum(double a, double b, double* s, double* e) {
+    double ss = a + b, bb = ss - a;
+    *s = ss;
+    *e = (a - (ss - bb)) + (b - bb);
+}
+
+// Element i (0-based) of Julia's range(a, b; length=n).
+double linrange(double a, double b, int64_t n, int64_t i) {
+    if (n == 1 || i == 0) return a;
+    if (i == n - 1) return b;
+    double lim = 4503599627370496.0 / (double)n;
+    if (a == std::rint(a) && b == std::rint(b) && std::fabs(a) < lim && std::fabs(b) < lim)
+        return (a * (double)(n - 1 - i) + b * (double)i) / (double)(n - 1);
+    double dh, dl, m = (double)(n - 1), fi = (double)i;
+    two_sum(b, -a, &dh, &dl);
+    double q1 = dh / m;
+    double r = std::fma(-q1, m, dh) + dl;
+    double q2 = r / m;
+    double p1 = fi * q1, p1e = std::fma(fi, q1, -p1);
+    double p2 = fi * q2;
+    double s, se;
+    two_sum(a, p1, &s, &se);
+    return s + (se + (p1e + p2));
+}
+
+void philox_host(uint32_t c[4], uint64_t seed) {
+    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    for (int r = 0; r < 10; ++r) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c[0];
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c[2];
+        uint32_t n0 = (uint32_t)(p1 >> 32) ^ c[1] ^ k0;
+        uint32_t n1 = (uint32_t)p1;
+        uint32_t n2 = (uint32_t)(p0 >> 32) ^ c[3] ^ k1;
+        uint32_t n3 = (uint32_t)p0;
+        c[0] = n0; c[1] = n1; c[2] = n2; c[3] = n3;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+double u53_host(uint32_t a, uint32_t b) {
+    return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
+}
+
+struct HostJob {
+    DJob J;
+    std::vector<double> t, kd, kz;
+};
+
+int validate_job(const etraj_job* job, std::string& err) {
+    auto fail = [&](const char* m) { err = m; return (int)ETRAJ_ERR_INVALID_ARGUMENT; };
+    if (!job) return fail("job is NULL");
+    if (!(job->sample_t_intv[0] < job->sample_t_intv[1]))
+        return fail("[TrajectorySimulationJob] `sample_t_intv` must be a valid interval.");
+    if (!(job->traj_t_final > job->sample_t_intv[1]))
+        return fail("[TrajectorySimulationJob] `traj_t_final` must be greater than the last time point of `sample_t_intv`.");
+    if (job->dimension != 2 && job->dimension != 3)
+        return fail("[TrajectorySimulationJob] `dimension` must be either 2 or 3.");
+    if (job->init_cond_method == ETRAJ_SAMPLER_SPA) {
+        err = "[SPASampler] the SFA-SPA sampler is not built in this engine.";
+        return ETRAJ_ERR_UNSUPPORTED;
+    }
+    if (job->init_cond_method != ETRAJ_SAMPLER_ADK && job->init_cond_method != ETRAJ_SAMPLER_SPANE)
+        return fail("[ElectronSamplers] Undefined initial condition method.");
+    if (job->traj_phase_method < 0 || job->traj_phase_method > 2)
+        return fail("[ADKSampler] Undefined phase method.");
+    if (job->precision == ETRAJ_PRECISION_FP32_BULK && !kHaveFp32Bulk) {
+        err = "the FP32-bulk integrator is not built in this library.";
+        return ETRAJ_ERR_UNSUPPORTED;
+    }
+    if (job->precision != ETRAJ_PRECISION_FP64 && job->precision != ETRAJ_PRECISION_FP32_BULK)
+        return fail("unknown precision.");
+    if (job->rate_prefix & ~7) return fail("[ADKSampler] Undefined tunneling rate prefix.");
+    if ((job->rate_prefix & ETRAJ_PREFIX_PRE) && (job->rate_prefix & ETRAJ_PREFIX_PRECC))
+        return fail("[ADKSampler] Rate prefixes [Pre] & [PreCC] conflict.");
+    if (!(job->sample_t_num > 0)) return fail("[ADKSampler] Invalid time sample number.");
+    if (!(job->sample_cutoff_limit >= 0)) return fail("[ADKSampler] Invalid cut-off limit.");
+    if (!job->sample_monte_carlo) {
+        if (job->dimension == 3) {
+            if (!(job->ss_kd_num > 0 && job->ss_kz_num > 0)) return fail("[ADKSampler] Invalid kd,kz sample number.");
+            if (!(job->ss_kd_max > 0 || job->ss_kz_max > 0))
+                return fail("[ADKSampler] Invalid kd,kz sample boundaries (cannot be zero simultaneously).");
+        } else {
+            if (!(job->ss_kd_num > 0)) return fail("[ADKSampler] Invalid kd sample number.");
+            if (!(job->ss_kd_max > 0)) return fail("[ADKSampler] Invalid kd sample boundaries.");
+        }
+    } else {
+        if (!(job->mc_kt_num > 0)) return fail("[ADKSampler] Invalid sampling kt_num.");
+        if (job->dimension == 3) {
+            if (!(job->mc_kd_max > 0 || job->mc_kz_max > 0))
+                return fail("[ADKSampler] Invalid kd,kz sample boundaries (cannot be zero simultaneously).");
+        } else if (!(job->mc_kd_max > 0)) {
+            return fail("[ADKSampler] Invalid kd sample boundaries.");
+        }
+    }
+    int64_t grid = 1;
+    for (int d = 0; d < job->dimension; ++d) {
+        if (job->final_p_num[d] < 1) return fail("[TrajectorySimulationJob] `final_p_num` must be positive.");
+        if (job->final_p_num[d] > 1 && !(job->final_p_max[d] > 0))
+            return fail("[TrajectorySimulationJob] `final_p_max` must be positive.");
+        grid *= job->final_p_num[d];
+    }
+    if (grid >= (int64_t)0xFFFFFFFFll) return fail("momentum grid too large (>= 2^32 bins).");
+    const etraj_target& T = job->target;
+    if (!(T.Ip > 0)) return fail("[SAEAtom] Ip should be positive.");
+    if (!(T.l >= 0 && T.l >= std::abs(T.m))) return fail("[SAEAtom] Invalid (l,m).");
+    if (T.l > kMaxL) {
+        err = "angular quantum number l > 4 is not supported.";
+        return ETRAJ_ERR_UNSUPPORTED;
+    }
+    if (!(T.asymp_coeff > 0)) return fail("[SAEAtom] asymp_coeff should be either `:hartree` or a positive number.");
+    if (T.kind == ETRAJ_TARGET_SAE) {
+        if (!(T.b1 >= 0 && T.b2 >= 0 && T.b3 >= 0)) return fail("[SAEAtom] b1,b2,b3 should be non-negative.");
+        if (!(T.soft_core > 0)) return fail("[SAEAtom] soft_core should be positive.");
+    } else if (T.kind == ETRAJ_TARGET_HYDROGEN_LIKE) {
+        if (!(T.soft_core >= 0)) return fail("[HydrogenLikeAtom] `soft_core` should be non-negative.");
+    } else {
+        return fail("Unknown target kind.");
+    }
+    if (job->laser.kind < 0 || job->laser.kind > 3) return fail("Unknown laser kind.");
+    int nm = (job->laser.kind == ETRAJ_LASER_BICHROMATIC) ? 2 : 1;
+    for (int i = 0; i < nm; ++i) {
+        const etraj_mono_laser& L = job->laser.mono[i];
+        if (L.kind < 0 || L.kind > 2) return fail("Unknown monochromatic laser kind.");
+        if (!(L.wave_len > 0)) return fail("[Cos4Laser] Must specify either `wave_len` or `ang_freq`.");
+        if (!(L.cyc_num > 0)) return fail("[Cos4Laser] Must specify either `cyc_num` or `duration`.");
+    }
+    if (!(job->traj_rtol > 0)) return fail("`traj_rtol` must be positive.");
+    int64_t ncand = job->sample_monte_carlo ? job->mc_kt_num
+                                            : job->ss_kd_num * ((job->dimension == 3) ? job->ss_kz_num : 1);
+    if ((double)ncand * (double)job->sample_t_num >= 4.0e9)
+        return fail("more than 4e9 candidate electrons in one job; split the job.");
+    return ETRAJ_OK;
+}
+
+void prepare_job(const etraj_job* job, HostJob& H) {
+    DJob& J = H.J;
+    std::memset(&J, 0, sizeof J);
+    J.method = job->init_cond_method;
+    J.dim = job->dimension;
+    J.mc = job->sample_monte_carlo ? 1 : 0;
+    int p = job->rate_prefix;
+    if ((p & ETRAJ_PREFIX_PRECC) && job->laser.kind == ETRAJ_LASER_BICHROMATIC)
+        p = (p & ~ETRAJ_PREFIX_PRECC) | ETRAJ_PREFIX_PRE;  // ADKSampler.jl:72-77
+    J.prefix = p;
+    J.phase = job->traj_phase_method;
+    J.rows = (J.dim == 3) ? ((J.phase == ETRAJ_PHASE_CTMC) ? 8 : 9) : ((J.phase == ETRAJ_PHASE_CTMC) ? 6 : 7);
+    J.n_state = (J.dim == 3 ? 6 : 4) + (J.phase != ETRAJ_PHASE_CTMC ? 1 : 0);
+    J.mono = (job->laser.kind != ETRAJ_LASER_BICHROMATIC) ? 1 : 0;
+    J.cutoff = job->sample_cutoff_limit;
+    J.seed = job->seed;
+    J.laser.kind = job->laser.kind;
+    mono_prepare(job->laser.mono[0], J.laser.m[0]);
+    if (job->laser.kind == ETRAJ_LASER_BICHROMATIC) {
+        mono_prepare(job->laser.mono[1], J.laser.m[1]);
+        J.laser.delay = job->laser.delay;
+        J.laser.nmono = 2;
+    } else {
+        J.laser.nmono = 1;
+    }
+    const etraj_target& T = job->target;
+    J.target.kind = T.kind;
+    J.target.Z = (double)T.Z;
+    J.target.Ip = T.Ip;
+    J.target.sc = T.soft_core;
+    J.target.a1 = T.a1; J.target.b1 = T.b1;
+    J.target.a2 = T.a2; J.target.b2 = T.b2;
+    J.target.a3 = T.a3; J.target.b3 = T.b3;
+    J.Ip = T.Ip;
+    J.Z = (double)T.Z;
+    J.l = T.l;
+    J.m = T.m;
+    J.C = T.asymp_coeff;
+    J.q_theta = T.quan_ax_theta;
+    J.q_phi = T.quan_ax_phi;
+    J.kappa = std::sqrt(2.0 * J.Ip);
+    J.nstar = J.Z / J.kappa;
+    const double n = J.nstar;
+    J.c = (dm_pow_pos(2.0, n / 2.0 + 1.0) * dm_pow_pos(J.kappa, 2.0 * n + 0.5)) * std::tgamma(n / 2.0 + 1.0);
+    J.cc_base = dm_pow_pos(2.0, (3.0 * n) / 2.0 + 1.0) * dm_pow_pos(J.kappa, 5.0 * n + 0.5);
+    J.e_pre = (n + 1.0) / 4.0;
+    for (int mp = -J.l; mp <= J.l; ++mp) {
+        dm_cplx P = sph_prefactor(J.l, mp, J.kappa);
+        J.Plm[2 * (mp + J.l)] = P.re;
+        J.Plm[2 * (mp + J.l) + 1] = P.im;
+    }
+    // time samples: range(t1, t2; length=n) or sort!(rand(n)*(t2-t1) .+ t1)  (ADKSampler.jl:136,141)
+    J.n_t = job->sample_t_num;
+    H.t.resize((size_t)J.n_t);
+    const double t1 = job->sample_t_intv[0], t2 = job->sample_t_intv[1];
+    if (!J.mc) {
+        for (int64_t j = 0; j < J.n_t; ++j) H.t[(size_t)j] = linrange(t1, t2, J.n_t, j);
+    } else {
+        const double span = t2 - t1;
+        for (int64_t j = 0; j < J.n_t; ++j) {
+            uint32_t c[4] = {(uint32_t)j, (uint32_t)((uint64_t)j >> 32), 0u, 0x54494D45u};
+            philox_host(c, job->seed);
+            H.t[(size_t)j] = u53_host(c[0], c[1]) * span + t1;
+        }
+        std::sort(H.t.begin(), H.t.end());
+    }
+    const double t_step = (H.t.back() - H.t.front()) / (double)J.n_t;  // ADKSampler.jl:267
+    if (!J.mc) {
+        int64_t nkd = job->ss_kd_num, nkz = (J.dim == 3) ? job->ss_kz_num : 1;
+        double kdm = std::fabs(job->ss_kd_max), kzm = (J.dim == 3) ? std::fabs(job->ss_kz_max) : 0.0;
+        J.n_kd = nkd;
+        J.n_kz = nkz;
+        H.kd.resize((size_t)nkd);
+        H.kz.resize((size_t)nkz);
+        for (int64_t i = 0; i < nkd; ++i) H.kd[(size_t)i] = linrange(-kdm, kdm, nkd, i);
+        for (int64_t i = 0; i < nkz; ++i) H.kz[(size_t)i] = linrange(-kzm, kzm, nkz, i);
+        double kd_step = (nkd > 1) ? (kdm - (-kdm)) / (double)nkd : 1.0;
+        double kz_step = (J.dim == 3 && nkz > 1) ? (kzm - (-kzm)) / (double)nkz : 1.0;
+        J.dkdt = (t_step * kd_step) * kz_step;
+        J.n_cand = nkd * nkz;
+    } else {
+        J.mc_kd_max = job->mc_kd_max;
+        J.mc_kz_max = job->mc_kz_max;
+        double kd_span = (job->mc_kd_max > 0.0) ? 2.0 * job->mc_kd_max : 1.0;
+        double kz_span = (job->mc_kz_max > 0.0) ? 2.0 * job->mc_kz_max : 1.0;
+        J.dkdt = ((t_step * kd_span) * kz_span) / (double)job->mc_kt_num;
+        J.n_cand = job->mc_kt_num;
+        J.n_kd = 1;
+        J.n_kz = 1;
+        H.kd.assign(1, 0.0);
+        H.kz.assign(1, 0.0);
+    }
+    J.n_total = J.n_t * J.n_cand;
+    J.rtol = job->traj_rtol;
+    J.t_final = job->traj_t_final;
+    J.grid = 1;
+    for (int d = 0; d < 3; ++d) {
+        if (d < J.dim) {
+            J.pmax[d] = job->final_p_max[d];
+            J.pnum[d] = job->final_p_num[d];
+            J.binw[d] = (J.pmax[d] / (double)J.pnum[d]) * 2.0;
+            J.grid *= J.pnum[d];
+        } else {
+            J.pnum[d] = 1;
+        }
+    }
+}
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+struct AsyncJob {
+    int status;
+    etraj_result result;
+    std::string error;
+};
+
+}  // namespace
+
+struct etraj_ctx {
+    int device = 0;
+    int sm_count = 152;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    size_t budget = 0;
+    size_t used = 0;
+    std::string err;
+    std::map<std::string, DevBuf> bufs;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    uint64_t next_ticket = 1;
+    std::map<uint64_t, AsyncJob> jobs;
+    std::mutex mu;
+};
+
+namespace {
+
+int set_err(etraj_ctx* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->err = msg;
+    return code;
+}
+
+int cuda_err(etraj_ctx* ctx, cudaError_t e, const char* where) {
+    return set_err(ctx, ETRAJ_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+// Grow-only named device buffer, counted against the context's HBM budget.
+int ensure(etraj_ctx* ctx, const char* name, size_t bytes, void** out) {
+    if (bytes == 0) bytes = 256;
+    DevBuf& b = ctx->bufs[name];
+    if (b.bytes >= bytes) {
+        *out = b.p;
+        return ETRAJ_OK;
+    }
+    size_t grow = bytes + bytes / 8;
+    if (ctx->used - b.bytes + grow > ctx->budget) {
+        grow = bytes;
+        if (ctx->used - b.bytes + grow > ctx->budget)
+            return set_err(ctx, ETRAJ_ERR_OUT_OF_MEMORY,
+                           std::string("HBM budget exceeded allocating ") + name + " (" +
+                               std::to_string(bytes) + " bytes; budget " + std::to_string(ctx->budget) +
+                               ", in use " + std::to_string(ctx->used) + ")");
+    }
+    if (b.p) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaFree(b.p);
+        ctx->used -= b.bytes;
+        b.p = nullptr;
+        b.bytes = 0;
+    }
+    cudaError_t e = cudaMalloc(&b.p, grow);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(ctx, ETRAJ_ERR_OUT_OF_MEMORY, std::string("cudaMalloc ") + name + ": " + cudaGetErrorString(e));
+    }
+    b.bytes = grow;
+    ctx->used += grow;
+    *out = b.p;
+    return ETRAJ_OK;
+}
+
+template <typename T>
+int ensure_t(etraj_ctx* ctx, const char* name, size_t count, T** out) {
+    void* p = nullptr;
+    int st = ensure(ctx, name, count * sizeof(T), &p);
+    *out = (T*)p;
+    return st;
+}
+
+struct Pipeline {
+    double* t = nullptr;
+    double* kd = nullptr;
+    double* kz = nullptr;
+    DBatch* batches = nullptr;
+    InitSoA soa{};
+    uint8_t* flag = nullptr;
+    int64_t* idx = nullptr;
+    uint32_t* block_sums = nullptr;
+    unsigned long long* count = nullptr;
+    TrajOut out{};
+    DepositScratch dep{};
+    double* spec_re = nullptr;
+    double* spec_im = nullptr;
+    double* mspec = nullptr;
+    double* sums = nullptr;
+    Counters* counters = nullptr;
+    unsigned long long* work = nullptr;
+};
+
+#define ETRAJ_TRY(x)                 \
+    do {                             \
+        int _st = (x);               \
+        if (_st != ETRAJ_OK) return _st; \
+    } while (0)
+
+int alloc_sampling(etraj_ctx* ctx, const HostJob& H, Pipeline& P) {
+    const DJob& J = H.J;
+    const size_t n = (size_t)J.n_total;
+    ETRAJ_TRY(ensure_t(ctx, "t", H.t.size(), &P.t));
+    ETRAJ_TRY(ensure_t(ctx, "kd", H.kd.size(), &P.kd));
+    ETRAJ_TRY(ensure_t(ctx, "kz", H.kz.size(), &P.kz));
+    ETRAJ_TRY(ensure_t(ctx, "batches", (size_t)J.n_t, &P.batches));
+    ETRAJ_TRY(ensure_t(ctx, "soa.x", n, &P.soa.x));
+    ETRAJ_TRY(ensure_t(ctx, "soa.y", n, &P.soa.y));
+    ETRAJ_TRY(ensure_t(ctx, "soa.kx", n, &P.soa.kx));
+    ETRAJ_TRY(ensure_t(ctx, "soa.ky", n, &P.soa.ky));
+    ETRAJ_TRY(ensure_t(ctx, "soa.kz", n, &P.soa.kz));
+    ETRAJ_TRY(ensure_t(ctx, "soa.rate", n, &P.soa.rate));
+    if (J.phase != ETRAJ_PHASE_CTMC) ETRAJ_TRY(ensure_t(ctx, "soa.phase", n, &P.soa.phase));
+    else P.soa.phase = nullptr;
+    ETRAJ_TRY(ensure_t(ctx, "soa.batch", n, &P.soa.batch));
+    ETRAJ_TRY(ensure_t(ctx, "flag", n, &P.flag));
+    ETRAJ_TRY(ensure_t(ctx, "idx", n, &P.idx));
+    ETRAJ_TRY(ensure_t(ctx, "block_sums", (size_t)compact_blocks((int64_t)n) + 1, &P.block_sums));
+    ETRAJ_TRY(ensure_t(ctx, "count", 4, &P.count));
+    return ETRAJ_OK;
+}
+
+int alloc_outputs(etraj_ctx* ctx, const DJob& J, int64_t max_n, bool with_state, Pipeline& P) {
+    const size_t n = (size_t)(max_n > 0 ? max_n : 1);
+    ETRAJ_TRY(ensure_t(ctx, "out.key", n, &P.out.key));
+    ETRAJ_TRY(ensure_t(ctx, "out.c_re", n, &P.out.c_re));
+    ETRAJ_TRY(ensure_t(ctx, "out.c_im", n, &P.out.c_im));
+    ETRAJ_TRY(ensure_t(ctx, "out.w_ion", n, &P.out.w_ion));
+    ETRAJ_TRY(ensure_t(ctx, "out.w_unc", n, &P.out.w_unc));
+    ETRAJ_TRY(ensure_t(ctx, "out.status", n, &P.out.status));
+    ETRAJ_TRY(ensure_t(ctx, "out.steps", n, &P.out.steps));
+    if (with_state) ETRAJ_TRY(ensure_t(ctx, "out.final_state", n * (size_t)J.n_state, &P.out.final_state));
+    else P.out.final_state = nullptr;
+    P.out.p_inf = nullptr;
+    void* dep = nullptr;
+    ETRAJ_TRY(ensure(ctx, "deposit", deposit_scratch_bytes(max_n), &dep));
+    deposit_scratch_carve(dep, max_n, &P.dep);
+    ETRAJ_TRY(ensure_t(ctx, "spec_re", (size_t)J.grid, &P.spec_re));
+    ETRAJ_TRY(ensure_t(ctx, "spec_im", (size_t)J.grid, &P.spec_im));
+    ETRAJ_TRY(ensure_t(ctx, "mspec", (size_t)J.grid, &P.mspec));
+    ETRAJ_TRY(ensure_t(ctx, "sums", 2, &P.sums));
+    ETRAJ_TRY(ensure_t(ctx, "counters", 1, &P.counters));
+    ETRAJ_TRY(ensure_t(ctx, "work", 4, &P.work));
+    return ETRAJ_OK;
+}
+
+int launch_integrate(etraj_ctx* ctx, const DJob& J, const InitSoA& soa, const double* t, const int64_t* idx,
+                     const unsigned long long* count, const TrajOut& out, int64_t max_n, unsigned long long* work,
+                     int precision) {
+    (void)work;
+    (void)precision;
+    return launch_integrate_fp64(J, soa, t, idx, count, out, max_n, ctx->sm_count, ctx->stream);
+}
+
+int run_job(etraj_ctx* ctx, const etraj_job* job, etraj_result* res) {
+    std::string err;
+    int st = validate_job(job, err);
+    if (st != ETRAJ_OK) return set_err(ctx, st, err);
+    HostJob H;
+    prepare_job(job, H);
+    const DJob& J = H.J;
+    Pipeline P;
+    ETRAJ_TRY(alloc_sampling(ctx, H, P));
+    ETRAJ_TRY(alloc_outputs(ctx, J, J.n_total, false, P));
+    cudaStream_t s = ctx->stream;
+    int launches = 0;
+    cudaMemcpyAsync(P.t, H.t.data(), H.t.size() * sizeof(double), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(P.kd, H.kd.data(), H.kd.size() * sizeof(double), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(P.kz, H.kz.data(), H.kz.size() * sizeof(double), cudaMemcpyHostToDevice, s);
+    cudaEventRecord(ctx->ev0, s);
+    launches += launch_batch_prepare(J, P.t, P.batches, s);
+    launches += launch_sample_range(J, 0, J.n_t, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s);
+    launches += launch_compact(P.flag, J.n_total, P.idx, P.block_sums, compact_blocks(J.n_total) + 1, P.count, s);
+    cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), s);
+    launches += launch_integrate(ctx, J, P.soa, P.t, P.idx, P.count, P.out, J.n_total, P.work, job->precision);
+    launches += launch_deposit(J, P.out, P.count, J.n_total, P.dep, P.spec_re, P.spec_im, P.mspec, P.sums,
+                               P.counters, s);
+    cudaEventRecord(ctx->ev1, s);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_err(ctx, e, "kernel launch");
+    double sums[2] = {0.0, 0.0};
+    Counters cnt{};
+    cudaMemcpyAsync(sums, P.sums, sizeof sums, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&cnt, P.counters, sizeof cnt, cudaMemcpyDeviceToHost, s);
+    if (res->momentum_spec)
+        cudaMemcpyAsync(res->momentum_spec, P.mspec, (size_t)J.grid * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (res->amplitude && J.phase != ETRAJ_PHASE_CTMC) {
+        cudaMemcpy2DAsync(res->amplitude, 2 * sizeof(double), P.spec_re, sizeof(double), sizeof(double),
+                          (size_t)J.grid, cudaMemcpyDeviceToHost, s);
+        cudaMemcpy2DAsync(res->amplitude + 1, 2 * sizeof(double), P.spec_im, sizeof(double), sizeof(double),
+                          (size_t)J.grid, cudaMemcpyDeviceToHost, s);
+    }
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "etraj_run");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    res->ion_prob = sums[0];
+    res->ion_prob_uncollected = sums[1];
+    res->num_effective_traj = (int64_t)cnt.n_eff;
+    res->num_failed_traj = (int64_t)cnt.n_failed;
+    res->num_ionized_traj = (int64_t)cnt.n_ionized;
+    res->num_steps = (int64_t)cnt.n_steps;
+    res->num_kernel_launches = launches;
+    res->elapsed_ms = ms;
+    return ETRAJ_OK;
+}
+
+// Copies sampled candidates back and assembles the reference's `init` columns.
+int gather_rows(etraj_ctx* ctx, const HostJob& H, const Pipeline& P, int64_t g0, int64_t ng, double* init,
+                int64_t capacity, int64_t* count) {
+    const DJob& J = H.J;
+    cudaStream_t s = ctx->stream;
+    std::vector<uint8_t> flag((size_t)ng);
+    std::vector<double> x((size_t)ng), y((size_t)ng), kx((size_t)ng), ky((size_t)ng), kz((size_t)ng),
+        rate((size_t)ng), ph((size_t)ng);
+    std::vector<int32_t> batch((size_t)ng);
+    cudaMemcpyAsync(flag.data(), P.flag + g0, (size_t)ng, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(x.data(), P.soa.x + g0, (size_t)ng * 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(y.data(), P.soa.y + g0, (size_t)ng * 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(kx.data(), P.soa.kx + g0, (size_t)ng * 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(ky.data(), P.soa.ky + g0, (size_t)ng * 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(kz.data(), P.soa.kz + g0, (size_t)ng * 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(rate.data(), P.soa.rate + g0, (size_t)ng * 8, cudaMemcpyDeviceToHost, s);
+    if (P.soa.phase) cudaMemcpyAsync(ph.data(), P.soa.phase + g0, (size_t)ng * 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(batch.data(), P.soa.batch + g0, (size_t)ng * 4, cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "sample copy-back");
+    int64_t c = 0;
+    for (int64_t i = 0; i < ng; ++i) {
+        if (!flag[(size_t)i]) continue;
+        if (c < capacity) {
+            double* r = init + c * J.rows;
+            int k = 0;
+            r[k++] = x[(size_t)i];
+            r[k++] = y[(size_t)i];
+            if (J.dim == 3) r[k++] = 0.0;
+            r[k++] = kx[(size_t)i];
+            r[k++] = ky[(size_t)i];
+            if (J.dim == 3) r[k++] = kz[(size_t)i];
+            r[k++] = H.t[(size_t)batch[(size_t)i]];
+            r[k++] = rate[(size_t)i];
+            if (J.phase != ETRAJ_PHASE_CTMC) r[k++] = ph[(size_t)i];
+        }
+        ++c;
+    }
+    *count = c;
+    return ETRAJ_OK;
+}
+
+int sample_range(etraj_ctx* ctx, const etraj_job* job, int64_t b0, int64_t nb, double* init, int64_t capacity,
+                 int64_t* count) {
+    std::string err;
+    int st = validate_job(job, err);
+    if (st != ETRAJ_OK) return set_err(ctx, st, err);
+    HostJob H;
+    prepare_job(job, H);
+    Pipeline P;
+    ETRAJ_TRY(alloc_sampling(ctx, H, P));
+    cudaStream_t s = ctx->stream;
+    cudaMemcpyAsync(P.t, H.t.data(), H.t.size() * sizeof(double), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(P.kd, H.kd.data(), H.kd.size() * sizeof(double), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(P.kz, H.kz.data(), H.kz.size() * sizeof(double), cudaMemcpyHostToDevice, s);
+    launch_batch_prepare(H.J, P.t, P.batches, s);
+    launch_sample_range(H.J, b0, nb, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_err(ctx, e, "sample launch");
+    return gather_rows(ctx, H, P, b0 * H.J.n_cand, nb * H.J.n_cand, init, capacity, count);
+}
+
+}  // namespace
+
+// ---- exported entry points --------------------------------------------------------
+extern "C" {
+
+const char* etraj_version(void) { return ETRAJ_VERSION_STRING; }
+
+int etraj_create(etraj_ctx** out, int device, size_t hbm_budget_bytes) {
+    if (!out) return ETRAJ_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || device < 0 || device >= ndev) {
+        cudaGetLastError();
+        return ETRAJ_ERR_CUDA;
+    }
+    e = cudaSetDevice(device);
+    if (e != cudaSuccess) return ETRAJ_ERR_CUDA;
+    etraj_ctx* ctx = new etraj_ctx();
+    ctx->device = device;
+    cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    const size_t reserve = (size_t)1 << 30;
+    ctx->budget = hbm_budget_bytes ? hbm_budget_bytes : (free_b > reserve ? free_b - reserve : free_b / 2);
+    if (cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess) {
+        delete ctx;
+        return ETRAJ_ERR_CUDA;
+    }
+    ctx->stream = ctx->own_stream;
+    *out = ctx;
+    return ETRAJ_OK;
+}
+
+void etraj_destroy(etraj_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (auto& kv : ctx->bufs)
+        if (kv.second.p) cudaFree(kv.second.p);
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+}
+
+const char* etraj_last_error(const etraj_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int etraj_set_stream(etraj_ctx* ctx, void* cuda_stream) {
+    if (!ctx) return ETRAJ_ERR_INVALID_ARGUMENT;
+    ctx->stream = cuda_stream ? (cudaStream_t)cuda_stream : ctx->own_stream;
+    return ETRAJ_OK;
+}
+
+int etraj_validate(const etraj_job* job, char* msg, size_t msg_len) {
+    std::string err;
+    int st = validate_job(job, err);
+    if (msg && msg_len > 0) {
+        std::strncpy(msg, err.c_str(), msg_len - 1);
+        msg[msg_len - 1] = 0;
+    }
+    return st;
+}
+
+int etraj_batch_info(const etraj_job* job, int64_t* batch_num, int64_t* batch_max_size) {
+    if (!job) return ETRAJ_ERR_INVALID_ARGUMENT;
+    if (batch_num) *batch_num = job->sample_t_num;
+    if (batch_max_size)
+        *batch_max_size = job->sample_monte_carlo ? job->mc_kt_num
+                                                  : job->ss_kd_num * ((job->dimension == 3) ? job->ss_kz_num : 1);
+    return ETRAJ_OK;
+}
+
+int etraj_run(etraj_ctx* ctx, const etraj_job* job, etraj_result* out) {
+    if (!ctx || !job || !out) return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    return run_job(ctx, job, out);
+}
+
+int etraj_sample_batch(etraj_ctx* ctx, const etraj_job* job, int64_t batch_id, double* init, int64_t capacity,
+                       int64_t* count) {
+    if (!ctx || !job || !count) return ETRAJ_ERR_INVALID_ARGUMENT;
+    if (batch_id < 1 || batch_id > job->sample_t_num)
+        return set_err(ctx, ETRAJ_ERR_INVALID_ARGUMENT, "batch_id out of range");
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    return sample_range(ctx, job, batch_id - 1, 1, init, capacity, count);
+}
+
+int etraj_sample_all(etraj_ctx* ctx, const etraj_job* job, double* init, int64_t capacity, int64_t* count) {
+    if (!ctx || !job || !count) return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    return sample_range(ctx, job, 0, job->sample_t_num, init, capacity, count);
+}
+
+int etraj_integrate(etraj_ctx* ctx, const etraj_job* job, int64_t n, const double* init, double* final_state,
+                    int32_t* status, int32_t* steps) {
+    if (!ctx || !job || (n > 0 && !init) || n < 0) return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    std::string err;
+    int st = validate_job(job, err);
+    if (st != ETRAJ_OK) return set_err(ctx, st, err);
+    if (n == 0) return ETRAJ_OK;
+    if (n >= ((int64_t)1 << 31)) return set_err(ctx, ETRAJ_ERR_INVALID_ARGUMENT, "n too large");
+    HostJob H;
+    prepare_job(job, H);
+    const DJob& J = H.J;
+    // unpack the reference `init` columns into a structure of arrays
+    std::vector<double> x((size_t)n), y((size_t)n), kx((size_t)n), ky((size_t)n), kz((size_t)n, 0.0),
+        rate((size_t)n), ph((size_t)n, 0.0), t0((size_t)n);
+    std::vector<int32_t> batch((size_t)n);
+    for (int64_t i = 0; i < n; ++i) {
+        const double* r = init + i * J.rows;
+        size_t u = (size_t)i;
+        x[u] = r[0];
+        y[u] = r[1];
+        if (J.dim == 2) {
+            kx[u] = r[2]; ky[u] = r[3]; t0[u] = r[4]; rate[u] = r[5];
+        } else {
+            kx[u] = r[3]; ky[u] = r[4]; kz[u] = r[5]; t0[u] = r[6]; rate[u] = r[7];
+        }
+        if (J.phase != ETRAJ_PHASE_CTMC) ph[u] = r[J.rows - 1];
+        batch[u] = (int32_t)i;
+    }
+    Pipeline P;
+    ETRAJ_TRY(ensure_t(ctx, "soa.x", (size_t)n, &P.soa.x));
+    ETRAJ_TRY(ensure_t(ctx, "soa.y", (size_t)n, &P.soa.y));
+    ETRAJ_TRY(ensure_t(ctx, "soa.kx", (size_t)n, &P.soa.kx));
+    ETRAJ_TRY(ensure_t(ctx, "soa.ky", (size_t)n, &P.soa.ky));
+    ETRAJ_TRY(ensure_t(ctx, "soa.kz", (size_t)n, &P.soa.kz));
+    ETRAJ_TRY(ensure_t(ctx, "soa.rate", (size_t)n, &P.soa.rate));
+    ETRAJ_TRY(ensure_t(ctx, "soa.phase", (size_t)n, &P.soa.phase));
+    ETRAJ_TRY(ensure_t(ctx, "soa.batch", (size_t)n, &P.soa.batch));
+    ETRAJ_TRY(ensure_t(ctx, "t", (size_t)n, &P.t));
+    ETRAJ_TRY(ensure_t(ctx, "count", 4, &P.count));
+    ETRAJ_TRY(alloc_outputs(ctx, J, n, true, P));
+    cudaStream_t s = ctx->stream;
+    auto up = [&](void* d, const void* h, size_t b) { cudaMemcpyAsync(d, h, b, cudaMemcpyHostToDevice, s); };
+    up(P.soa.x, x.data(), (size_t)n * 8);
+    up(P.soa.y, y.data(), (size_t)n * 8);
+    up(P.soa.kx, kx.data(), (size_t)n * 8);
+    up(P.soa.ky, ky.data(), (size_t)n * 8);
+    up(P.soa.kz, kz.data(), (size_t)n * 8);
+    up(P.soa.rate, rate.data(), (size_t)n * 8);
+    up(P.soa.phase, ph.data(), (size_t)n * 8);
+    up(P.soa.batch, batch.data(), (size_t)n * 4);
+    up(P.t, t0.data(), (size_t)n * 8);
+    unsigned long long cn = (unsigned long long)n;
+    up(P.count, &cn, sizeof cn);
+    cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), s);
+    launch_integrate(ctx, J, P.soa, P.t, nullptr, P.count, P.out, n, P.work, job->precision);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_err(ctx, e, "integrate launch");
+    std::vector<int32_t> stv((size_t)n);
+    if (final_state)
+        cudaMemcpyAsync(final_state, P.out.final_state, (size_t)n * J.n_state * 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(stv.data(), P.out.status, (size_t)n * 4, cudaMemcpyDeviceToHost, s);
+    if (steps) cudaMemcpyAsync(steps, P.out.steps, (size_t)n * 4, cudaMemcpyDeviceToHost, s);
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "etraj_integrate");
+    if (status)
+        for (int64_t i = 0; i < n; ++i) status[i] = stv[(size_t)i] & 0xff;
+    return ETRAJ_OK;
+}
+
+// The asynchronous interface runs each submitted job to completion on the
+// context's stream; results are kept until polled.
+int etraj_submit(etraj_ctx* ctx, const etraj_job* job, etraj_result* out, uint64_t* ticket) {
+    if (!ctx || !job || !ticket || !out) return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    uint64_t tk = ctx->next_ticket++;
+    AsyncJob aj;
+    aj.result = *out;
+    aj.status = run_job(ctx, job, &aj.result);
+    aj.error = ctx->err;
+    ctx->jobs[tk] = aj;
+    *ticket = tk;
+    return ETRAJ_OK;
+}
+
+int etraj_poll(etraj_ctx* ctx, uint64_t ticket, etraj_result* out) {
+    if (!ctx || !out) return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    auto it = ctx->jobs.find(ticket);
+    if (it == ctx->jobs.end()) return set_err(ctx, ETRAJ_ERR_NOT_FOUND, "unknown ticket");
+    double* ms = out->momentum_spec;
+    double* amp = out->amplitude;
+    *out = it->second.result;
+    out->momentum_spec = ms;
+    out->amplitude = amp;
+    int st = it->second.status;
+    if (st != ETRAJ_OK) ctx->err = it->second.error;
+    ctx->jobs.erase(it);
+    return st;
+}
+
+int etraj_wait(etraj_ctx* ctx, uint64_t ticket, etraj_result* out) { return etraj_poll(ctx, ticket, out); }
+
+}  // extern "C"

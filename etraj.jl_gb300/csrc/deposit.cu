@@ -1,0 +1,384 @@
+// deposit.cu -- deterministic momentum-spectrum deposit and reductions.
+//
+// Reference: the deposit `spec_collect_current[pxIdx,pyIdx] += prob` (CTMC)
+// or `+= sqrt(prob)*exp(1im*phase)` (QTMC/SCTS), TrajectorySimulation.jl:
+// 384-392 (3D :484-492), the thread sum and abs2 of write_output! (:521-533)
+// and the probability sums (:541-542).
+//
+// The reference's sum order depends on Julia's thread schedule.  Here the
+// order is fixed and independent of the launch shape: each bin is summed
+// left to right from 0.0 in trajectory order, which a stable LSD radix sort
+// of (bin, trajectory) followed by one sequential pass per bin segment
+// produces.  No floating-point atomics are used.  ion_prob and
+// ion_prob_uncollected are 256-ary trees over trajectory order, each node
+// summed left to right from 0.0.
+//
+// Roofline: HBM bound.  Per trajectory and 8-bit pass: read 4 B key
+// (histogram), read 8 B + write 8 B (scatter); the segmented pass reads 8 B
+// of the sorted pair plus 16 B of contribution; passes = ceil(bits(grid+1)/8).
+
+#include "engine.h"
+
+namespace etraj {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kRounds = 16;
+constexpr int kTile = kThreads * kRounds;  // keys per block and pass
+constexpr int kWarps = kThreads / 32;
+
+__global__ void __launch_bounds__(kThreads)
+k_radix_hist(const uint32_t* __restrict__ keys, const unsigned long long* __restrict__ count, int shift,
+             int64_t nblocks, uint32_t* __restrict__ hist) {
+    __shared__ uint32_t h[256];
+    const int64_t n = (int64_t)*count;
+    h[threadIdx.x] = 0u;
+    __syncthreads();
+    const int64_t base = (int64_t)blockIdx.x * kTile;
+    for (int r = 0; r < kRounds; ++r) {
+        int64_t i = base + (int64_t)r * kThreads + threadIdx.x;
+        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[(int64_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+// ---- exclusive scan of a uint32 array (reduce, scan partials, scan) --------
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanChunk = kScanThreads * kScanItems;
+
+__device__ __forceinline__ uint32_t block_scan_excl(uint32_t v, uint32_t* total) {
+    __shared__ uint32_t ws[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = (lane < nw) ? ws[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < nw) ws[lane] = w;
+    }
+    __syncthreads();
+    uint32_t r = ((warp > 0) ? ws[warp - 1] : 0u) + x - v;
+    if (total) *total = ws[nw - 1];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+k_scan_reduce(const uint32_t* __restrict__ a, int64_t n, uint32_t* __restrict__ part) {
+    const int64_t base = (int64_t)blockIdx.x * kScanChunk + (int64_t)threadIdx.x * kScanItems;
+    uint32_t c = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) c += (base + k < n) ? a[base + k] : 0u;
+    c = __reduce_add_sync(0xffffffffu, c);
+    __shared__ uint32_t ws[32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t s = 0;
+        for (int w = 0; w < kScanThreads / 32; ++w) s += ws[w];
+        part[blockIdx.x] = s;
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_partials(uint32_t* __restrict__ part, int64_t np) {
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0u;
+    __syncthreads();
+    for (int64_t off = 0; off < np; off += blockDim.x) {
+        int64_t i = off + threadIdx.x;
+        uint32_t v = (i < np) ? part[i] : 0u, tot;
+        uint32_t ex = block_scan_excl(v, &tot);
+        if (i < np) part[i] = carry + ex;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += tot;
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+k_scan_apply(uint32_t* __restrict__ a, int64_t n, const uint32_t* __restrict__ part) {
+    const int64_t base = (int64_t)blockIdx.x * kScanChunk + (int64_t)threadIdx.x * kScanItems;
+    uint32_t v[kScanItems], c = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        v[k] = (base + k < n) ? a[base + k] : 0u;
+        c += v[k];
+    }
+    uint32_t run = part[blockIdx.x] + block_scan_excl(c, nullptr);
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        if (base + k < n) a[base + k] = run;
+        run += v[k];
+    }
+}
+
+// Stable scatter of one 8-bit digit.  Within a block the tile is processed in
+// kRounds rounds of kThreads consecutive keys; inside a round the rank of a
+// key among equal digits of lower index comes from __match_any_sync within
+// the warp and a per-digit prefix over warps.
+__global__ void __launch_bounds__(kThreads)
+k_radix_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
+                uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
+                const unsigned long long* __restrict__ count, int shift, int64_t nblocks,
+                const uint32_t* __restrict__ offs) {
+    __shared__ uint32_t base[256];
+    __shared__ uint32_t wc[kWarps][256];
+    const int64_t n = (int64_t)*count;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    base[threadIdx.x] = offs[(int64_t)threadIdx.x * nblocks + blockIdx.x];
+    for (int w = 0; w < kWarps; ++w) wc[w][threadIdx.x] = 0u;
+    __syncthreads();
+    const int64_t tile = (int64_t)blockIdx.x * kTile;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    for (int r = 0; r < kRounds; ++r) {
+        const int64_t i = tile + (int64_t)r * kThreads + threadIdx.x;
+        const bool valid = i < n;
+        uint32_t key = 0u, val = 0u, d = 256u;
+        if (valid) {
+            key = kin[i];
+            val = vin ? vin[i] : (uint32_t)i;
+            d = (key >> shift) & 255u;
+        }
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const uint32_t rank = __popc(peers & lt_mask);
+        const int leader = __ffs(peers) - 1;
+        if (valid && lane == leader) wc[warp][d] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            uint32_t before = 0u;
+            for (int w = 0; w < warp; ++w) before += wc[w][d];
+            const uint32_t pos = base[d] + before + rank;
+            kout[pos] = key;
+            vout[pos] = val;
+        }
+        __syncthreads();
+        uint32_t tot = 0u;
+        for (int w = 0; w < kWarps; ++w) {
+            tot += wc[w][threadIdx.x];
+            wc[w][threadIdx.x] = 0u;
+        }
+        base[threadIdx.x] += tot;
+        __syncthreads();
+    }
+}
+
+// One pass over each bin's segment of the sorted pairs, left to right from 0.0.
+__global__ void __launch_bounds__(256)
+k_segment_sum(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
+              const unsigned long long* __restrict__ count, uint32_t grid,
+              const double* __restrict__ c_re, const double* __restrict__ c_im, int coherent,
+              double* __restrict__ spec_re, double* __restrict__ spec_im) {
+    const int64_t n = (int64_t)*count;
+    for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t k = keys[p];
+        if (k >= grid) continue;
+        if (p > 0 && keys[p - 1] == k) continue;
+        double sr = 0.0, si = 0.0;
+        for (int64_t q = p; q < n && keys[q] == k; ++q) {
+            const uint32_t v = vals[q];
+            sr = sr + c_re[v];
+            if (coherent) si = si + c_im[v];
+        }
+        spec_re[k] = sr;
+        if (coherent) spec_im[k] = si;
+    }
+}
+
+__global__ void k_finalize_spec(const double* __restrict__ re, const double* __restrict__ im,
+                                int64_t grid, int coherent, double* __restrict__ out) {
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < grid;
+         g += (int64_t)gridDim.x * blockDim.x)
+        out[g] = coherent ? re[g] * re[g] + im[g] * im[g] : re[g];
+}
+
+// One level of the 256-ary canonical tree over two arrays.  Level 0 reads
+// n = *count elements, level k reads ceil(n / 256^k).
+__global__ void k_tree_level(const double* __restrict__ a_in, const double* __restrict__ b_in,
+                             double* __restrict__ a_out, double* __restrict__ b_out,
+                             const unsigned long long* __restrict__ count, int level) {
+    int64_t m = (int64_t)*count;
+    for (int k = 0; k < level; ++k) m = (m + 255) / 256;
+    const int64_t nb = (m + 255) / 256;
+    for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nb;
+         b += (int64_t)gridDim.x * blockDim.x) {
+        double sa = 0.0, sb = 0.0;
+        const int64_t e = ((b + 1) * 256 < m) ? (b + 1) * 256 : m;
+        for (int64_t i = b * 256; i < e; ++i) {
+            sa = sa + a_in[i];
+            sb = sb + b_in[i];
+        }
+        a_out[b] = sa;
+        b_out[b] = sb;
+    }
+}
+
+__global__ void k_tree_result(const double* __restrict__ a, const double* __restrict__ b,
+                              const unsigned long long* __restrict__ count, double* __restrict__ sums) {
+    const bool empty = (*count == 0ull);
+    sums[0] = empty ? 0.0 : a[0];
+    sums[1] = empty ? 0.0 : b[0];
+}
+
+__global__ void __launch_bounds__(256)
+k_counters(const int32_t* __restrict__ status, const int32_t* __restrict__ steps,
+           const unsigned long long* __restrict__ count, Counters* __restrict__ c) {
+    const int64_t n = (int64_t)*count;
+    unsigned long long f = 0, io = 0, st = 0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t s = status[i];
+        f += ((s & 0xff) != 0) ? 1ull : 0ull;
+        io += (s & 0x100) ? 1ull : 0ull;
+        st += (unsigned long long)steps[i];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        f += __shfl_down_sync(0xffffffffu, f, o);
+        io += __shfl_down_sync(0xffffffffu, io, o);
+        st += __shfl_down_sync(0xffffffffu, st, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        if (f) atomicAdd(&c->n_failed, f);
+        if (io) atomicAdd(&c->n_ionized, io);
+        if (st) atomicAdd(&c->n_steps, st);
+    }
+}
+
+__global__ void k_copy_count(const unsigned long long* __restrict__ count, Counters* __restrict__ c) {
+    c->n_eff = *count;
+}
+
+int64_t tiles_for(int64_t n) { return (n + kTile - 1) / kTile; }
+int64_t scan_parts_for(int64_t n) { return (n + kScanChunk - 1) / kScanChunk; }
+
+int64_t tree_size(int64_t n) {
+    int64_t s = 0, m = n;
+    do {
+        m = (m + 255) / 256;
+        s += m;
+    } while (m > 1);
+    return s + 2;
+}
+
+int key_bits(int64_t grid) {
+    int b = 1;
+    while (b < 40 && ((int64_t)1 << b) <= grid) ++b;
+    return b;
+}
+
+}  // namespace
+
+size_t deposit_scratch_bytes(int64_t max_n) {
+    int64_t nb = tiles_for(max_n > 0 ? max_n : 1);
+    int64_t hist = 256 * nb;
+    size_t bytes = 0;
+    bytes += 4 * (size_t)max_n * sizeof(uint32_t) + 4 * 256;  // keys a/b, vals a/b
+    bytes += (size_t)hist * sizeof(uint32_t) + 256;
+    bytes += (size_t)(scan_parts_for(hist) + 64) * sizeof(uint32_t) + 256;
+    bytes += 2 * (size_t)tree_size(max_n) * sizeof(double) + 512;
+    return bytes;
+}
+
+void deposit_scratch_carve(void* base, int64_t max_n, DepositScratch* d) {
+    auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    char* p = (char*)base;
+    size_t off = 0;
+    int64_t nb = tiles_for(max_n > 0 ? max_n : 1);
+    int64_t hist = 256 * nb;
+    d->keys_a = (uint32_t*)(p + off); off = align(off + (size_t)max_n * 4);
+    d->keys_b = (uint32_t*)(p + off); off = align(off + (size_t)max_n * 4);
+    d->vals_a = (uint32_t*)(p + off); off = align(off + (size_t)max_n * 4);
+    d->vals_b = (uint32_t*)(p + off); off = align(off + (size_t)max_n * 4);
+    d->hist = (uint32_t*)(p + off); off = align(off + (size_t)hist * 4);
+    d->scan_tmp = (uint32_t*)(p + off); off = align(off + (size_t)(scan_parts_for(hist) + 64) * 4);
+    int64_t ts = tree_size(max_n);
+    d->tree_a = (double*)(p + off); off = align(off + (size_t)ts * 8);
+    d->tree_b = (double*)(p + off);
+}
+
+int launch_deposit(const DJob& J, const TrajOut& out, const unsigned long long* count, int64_t max_n,
+                   DepositScratch d, double* spec_re, double* spec_im, double* momentum_spec,
+                   double* sums, Counters* counters, cudaStream_t s) {
+    int launches = 0;
+    const int64_t grid = J.grid;
+    const int coherent = (J.phase != ETRAJ_PHASE_CTMC) ? 1 : 0;
+    cudaMemsetAsync(spec_re, 0, (size_t)grid * sizeof(double), s);
+    if (coherent) cudaMemsetAsync(spec_im, 0, (size_t)grid * sizeof(double), s);
+    cudaMemsetAsync(counters, 0, sizeof(Counters), s);
+    if (max_n > 0) {
+        // stable LSD radix sort of (key, survivor index); keys are in [0, grid]
+        const int64_t nb = tiles_for(max_n);
+        const int64_t hist_n = 256 * nb;
+        const int64_t parts = scan_parts_for(hist_n);
+        const int bits = key_bits(grid);
+        const uint32_t* kin = out.key;
+        const uint32_t* vin = nullptr;
+        uint32_t* kbuf[2] = {d.keys_a, d.keys_b};
+        uint32_t* vbuf[2] = {d.vals_a, d.vals_b};
+        int which = 0;
+        for (int shift = 0; shift < bits; shift += 8) {
+            k_radix_hist<<<(unsigned)nb, kThreads, 0, s>>>(kin, count, shift, nb, d.hist);
+            k_scan_reduce<<<(unsigned)parts, kScanThreads, 0, s>>>(d.hist, hist_n, d.scan_tmp);
+            k_scan_partials<<<1, kScanThreads, 0, s>>>(d.scan_tmp, parts);
+            k_scan_apply<<<(unsigned)parts, kScanThreads, 0, s>>>(d.hist, hist_n, d.scan_tmp);
+            k_radix_scatter<<<(unsigned)nb, kThreads, 0, s>>>(kin, vin, kbuf[which], vbuf[which], count,
+                                                               shift, nb, d.hist);
+            launches += 5;
+            kin = kbuf[which];
+            vin = vbuf[which];
+            which ^= 1;
+        }
+        int sblocks = (int)((max_n + 255) / 256);
+        if (sblocks > 152 * 64) sblocks = 152 * 64;
+        k_segment_sum<<<sblocks, 256, 0, s>>>(kin, vin, count, (uint32_t)grid, out.c_re, out.c_im,
+                                              coherent, spec_re, spec_im);
+        ++launches;
+        // canonical 256-ary trees for ion_prob and ion_prob_uncollected
+        const double* a = out.w_ion;
+        const double* b = out.w_unc;
+        double* ta = d.tree_a;
+        double* tb = d.tree_b;
+        int64_t m = max_n;
+        int level = 0;
+        do {
+            int64_t nbl = (m + 255) / 256;
+            int tb_blocks = (int)((nbl + 255) / 256);
+            k_tree_level<<<tb_blocks, 256, 0, s>>>(a, b, ta, tb, count, level);
+            ++launches;
+            a = ta;
+            b = tb;
+            ta += nbl;
+            tb += nbl;
+            m = nbl;
+            ++level;
+        } while (m > 1);
+        k_tree_result<<<1, 1, 0, s>>>(a, b, count, sums);
+        int cblocks = (int)((max_n + 255) / 256);
+        if (cblocks > 152 * 8) cblocks = 152 * 8;
+        k_counters<<<cblocks, 256, 0, s>>>(out.status, out.steps, count, counters);
+        launches += 2;
+    } else {
+        cudaMemsetAsync(sums, 0, 2 * sizeof(double), s);
+    }
+    k_copy_count<<<1, 1, 0, s>>>(count, counters);
+    int fblocks = (int)((grid + 255) / 256);
+    if (fblocks > 152 * 16) fblocks = 152 * 16;
+    k_finalize_spec<<<fblocks, 256, 0, s>>>(spec_re, spec_im, grid, coherent, momentum_spec);
+    launches += 2;
+    return launches;
+}
+
+}  // namespace etraj

@@ -1,0 +1,127 @@
+// engine.h -- device-side job description and the kernel launchers shared by
+// the translation units of libetraj_gb300.
+//
+// Every field is derived on the host from an etraj_job (setup.cpp) with the
+// same expressions the reference uses (src/Lasers/*.jl getters,
+// src/ElectronSamplers/ADKSampler.jl:226-276), then passed to kernels by
+// value as a __grid_constant__ parameter.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/etraj.h"
+#include "detmath.h"
+
+namespace etraj {
+
+struct DMono {
+    int kind;
+    int azi_zero;
+    double omega, period, F0, A0, N, cep, t_shift, ellip;
+    double cphi, sphi;        // cos/sin of the azimuth
+    double w2n, cN, k, Npiw;  // cos^n envelope: omega/(2N), 2/N or 1/N, 200/T, N*pi/omega
+    double sigma, inv_s2, inv_2s2;  // Gaussian envelope
+};
+
+struct DLaser {
+    int nmono;
+    int kind;
+    DMono m[2];
+    double delay;
+};
+
+struct DTarget {
+    int kind;
+    double Z, Ip, sc, a1, b1, a2, b2, a3, b3;
+};
+
+// Per-time-sample constants of the ADK/SPANE samplers (the prologue of
+// gen_electron_batch, ADKSampler.jl:168-296).
+struct DBatch {
+    double tr, Fx, Fy, dFx, dFy, F, sphi, cphi, c_cc, W;
+    double ny0, ny1, nz0, nz1;
+    double D[2 * 9];  // D^l_{m' m}, m' = -l..l, interleaved (re, im)
+};
+
+constexpr int kMaxL = 4;
+
+struct DJob {
+    // sampling
+    int method, dim, mc, prefix, phase, rows, mono, l, m;
+    int n_state;
+    int64_t n_t, n_kd, n_kz, n_cand, n_total;  // n_total = n_t * n_cand
+    double Ip, Z, kappa, nstar, c, cc_base, e_pre, C, q_theta, q_phi;
+    double cutoff, dkdt, mc_kd_max, mc_kz_max;
+    uint64_t seed;
+    double Plm[2 * (2 * kMaxL + 1)];
+    // integration
+    double rtol, t_final;
+    // collection
+    double pmax[3], binw[3];
+    int64_t pnum[3];
+    int64_t grid;
+    DLaser laser;
+    DTarget target;
+};
+
+// Sampled electrons, candidate-indexed structure of arrays.
+struct InitSoA {
+    double *x, *y, *kx, *ky, *kz, *rate, *phase;
+    int32_t* batch;   // time-sample index (t0 = t_samples[batch])
+};
+
+// Per-survivor outputs of the integrate+collect kernel.
+struct TrajOut {
+    uint32_t* key;       // bin (0..grid-1) or grid for "not deposited"
+    double* c_re;        // contribution: w (CTMC) or sqrt(w)cos(phi)
+    double* c_im;        // sqrt(w) sin(phi) (QTMC/SCTS)
+    double* w_ion;       // w if ionized, else 0
+    double* w_unc;       // w if ionized and outside the grid, else 0
+    int32_t* status;     // 0 Success, 1 MaxIters, 2 DtLessThanMin, 3 Unstable, 4 DtNaN
+    int32_t* steps;      // step attempts
+    double* final_state; // optional: n_state doubles per survivor (row-major)
+    double* p_inf;       // optional: 3 doubles per survivor
+};
+
+struct Counters {
+    unsigned long long n_eff;
+    unsigned long long n_failed;
+    unsigned long long n_ionized;
+    unsigned long long n_steps;
+};
+
+// ---- launchers (all stream-ordered; each returns the number of kernel launches) ----
+int launch_batch_prepare(const DJob& J, const double* t, DBatch* batches, cudaStream_t s);
+// Samples the candidates of time samples [b0, b0+nb) (flag and SoA indexed by
+// b * n_cand + i).
+int launch_sample_range(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
+                        const DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
+                        cudaStream_t s);
+// Order-preserving compaction: idx[k] = k-th i with flag[i] != 0; *count = total.
+int launch_compact(const uint8_t* flag, int64_t n, int64_t* idx, uint32_t* block_sums,
+                   int64_t nblocks_cap, unsigned long long* count, cudaStream_t s);
+int64_t compact_blocks(int64_t n);
+int launch_integrate_fp64(const DJob& J, InitSoA soa, const double* t, const int64_t* idx,
+                          const unsigned long long* count, TrajOut out, int64_t max_n,
+                          int sm_count, cudaStream_t s);
+int launch_integrate_fp32(const DJob& J, InitSoA soa, const double* t, const int64_t* idx,
+                          const unsigned long long* count, TrajOut out, int64_t max_n,
+                          unsigned long long* work_counter, int sm_count, cudaStream_t s);
+
+// Deterministic deposit: stable radix sort of (key, survivor) and segmented sums.
+struct DepositScratch {
+    uint32_t *keys_a, *keys_b, *vals_a, *vals_b;
+    uint32_t* hist;       // 256 * nblocks
+    uint32_t* scan_tmp;   // scan partials
+    double* tree_a;       // canonical-sum partials
+    double* tree_b;
+};
+size_t deposit_scratch_bytes(int64_t max_n);
+void deposit_scratch_carve(void* base, int64_t max_n, DepositScratch* d);
+int launch_deposit(const DJob& J, const TrajOut& out, const unsigned long long* count,
+                   int64_t max_n, DepositScratch d, double* spec_re, double* spec_im,
+                   double* momentum_spec, double* sums /* [2]: ion, unc */,
+                   Counters* counters, cudaStream_t s);
+
+}  // namespace etraj

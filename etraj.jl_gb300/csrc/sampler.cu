@@ -1,0 +1,397 @@
+// sampler.cu -- ADK and SPANE initial-condition sampling on the device.
+//
+// Reference: gen_electron_batch in src/ElectronSamplers/ADKSampler.jl:167-396
+// and SPANESampler.jl:163-404, with the helpers of shared_methods.jl:4-47.
+//
+// Layout: one thread per candidate (time sample b, transverse-momentum
+// sample i), candidates in the reference's loop order (kd outer, kz inner;
+// Monte-Carlo index i).  k_sample writes the candidate-indexed structure of
+// arrays and a keep flag; the compaction kernels turn the flags into the
+// ordered survivor list, so survivor k is the reference's k-th column of the
+// concatenated `init` matrices.  The per-batch prologue (field at t_r, its
+// derivative, Keldysh parameter, Coulomb-corrected prefactor constant and
+// the Wigner-D row) runs once per time sample in k_batch_prepare.
+//
+// Monte-Carlo draws come from Philox4x32-10 (Salmon et al., SC'11), counter
+// (i, batch, 0x4B445A00) keyed by the job seed: kd from output words 0,1 and
+// kz from words 2,3, each mapped to [0,1) with 53 bits.
+//
+// Roofline: memory bound on the SoA writes (about 61 B per candidate).
+
+#include "physics.cuh"
+
+namespace etraj {
+namespace {
+
+__device__ __forceinline__ void philox4x32(uint32_t c[4], uint64_t seed) {
+    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        uint32_t hi0 = __umulhi(0xD2511F53u, c[0]), lo0 = 0xD2511F53u * c[0];
+        uint32_t hi1 = __umulhi(0xCD9E8D57u, c[2]), lo1 = 0xCD9E8D57u * c[2];
+        uint32_t n0 = hi1 ^ c[1] ^ k0, n2 = hi0 ^ c[3] ^ k1;
+        c[0] = n0;
+        c[1] = lo1;
+        c[2] = n2;
+        c[3] = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+}
+
+__device__ __forceinline__ double u53(uint32_t a, uint32_t b) {
+    return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
+}
+
+__device__ __forceinline__ double fact(int n) {
+    double f = 1.0;
+    for (int i = 2; i <= n; ++i) f *= (double)i;
+    return f;
+}
+
+// Wigner small-d d^j_{m'm}(beta), explicit sum (standard convention).
+__device__ double wigner_d(int j, int mp, int m, double beta) {
+    double sh, ch;
+    dm_sincos(0.5 * beta, &sh, &ch);
+    double pref = sqrt(fact(j + mp) * fact(j - mp) * fact(j + m) * fact(j - m));
+    double sum = 0.0;
+    for (int s = 0; s <= 2 * j; ++s) {
+        int a1 = j + m - s, a3 = mp - m + s, a4 = j - mp - s;
+        if (a1 < 0 || a3 < 0 || a4 < 0) continue;
+        double den = fact(a1) * fact(s) * fact(a3) * fact(a4);
+        double sign = ((mp - m + s) & 1) ? -1.0 : 1.0;
+        int pc = 2 * j + m - mp - 2 * s, ps = mp - m + 2 * s;
+        double cpow = 1.0, spow = 1.0;
+        for (int i = 0; i < pc; ++i) cpow *= ch;
+        for (int i = 0; i < ps; ++i) spow *= sh;
+        sum = sum + ((sign * pref / den) * cpow) * spow;
+    }
+    return sum;
+}
+
+__device__ void rotzyz(double a, double b, double g, double R[3][3]) {
+    double sa, ca, sb, cb, sg, cg;
+    dm_sincos(a, &sa, &ca);
+    dm_sincos(b, &sb, &cb);
+    dm_sincos(g, &sg, &cg);
+    R[0][0] = ca * cb * cg - sa * sg; R[0][1] = -(ca * cb * sg) - sa * cg; R[0][2] = ca * sb;
+    R[1][0] = sa * cb * cg + ca * sg; R[1][1] = -(sa * cb * sg) + ca * cg; R[1][2] = sa * sb;
+    R[2][0] = -(sb * cg);             R[2][1] = sb * sg;                   R[2][2] = cb;
+}
+
+// gen_electron_batch prologue (ADKSampler.jl:168-235, SPANESampler.jl:164-235).
+__global__ void k_batch_prepare(const __grid_constant__ DJob J, const double* __restrict__ t,
+                                DBatch* __restrict__ out) {
+    int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= J.n_t) return;
+    DBatch B;
+    double tr = t[b];
+    B.tr = tr;
+    if (J.method == ETRAJ_SAMPLER_SPANE) {
+        laser_F_dual(J.laser, tr, B.Fx, B.Fy, B.dFx, B.dFy);
+    } else {
+        laser_F(J.laser, tr, B.Fx, B.Fy);
+        B.dFx = 0.0;
+        B.dFy = 0.0;
+    }
+    B.F = dm_hypot(B.Fx, B.Fy);
+    double phi = dm_atan2(-B.Fy, -B.Fx);
+    dm_sincos(phi, &B.sphi, &B.cphi);
+    double gamma = 0.0;
+    if (J.mono) {
+        const DMono& M = J.laser.m[0];
+        gamma = (M.omega * J.kappa) / (M.F0 * mono_env(M, tr));
+    }
+    B.c_cc = (J.cc_base * dm_pow_pos(B.F, -J.nstar)) *
+             dm_pow_pos(1.0 + (2.0 * gamma) / 2.718281828459045, -J.nstar);
+    B.W = B.Fx * B.dFy - B.dFx * B.Fy;
+    B.ny0 = B.Fy / B.F;
+    B.ny1 = -B.Fx / B.F;
+    B.nz0 = B.Fx / B.F;
+    B.nz1 = B.Fy / B.F;
+    // Euler angles FF -> MF (shared_methods.jl:31-38), MF = RotZYZ(phi_q, theta_q, 0)
+    double FF[3][3] = {{0.0, B.Fy / B.F, B.Fx / B.F}, {0.0, -B.Fx / B.F, B.Fy / B.F}, {1.0, 0.0, 0.0}};
+    double MF[3][3], M[3][3];
+    rotzyz(J.q_phi, J.q_theta, 0.0, MF);
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+            M[i][j] = (MF[0][i] * FF[0][j] + MF[1][i] * FF[1][j]) + MF[2][i] * FF[2][j];
+    double t1 = dm_atan2(M[1][2], M[0][2]);
+    double st1, ct1;
+    dm_sincos(t1, &st1, &ct1);
+    double t2 = dm_atan2(M[0][2] * ct1 + M[1][2] * st1, M[2][2]);
+    double t3 = dm_atan2(M[1][0] * ct1 - M[0][0] * st1, M[1][1] * ct1 - M[0][1] * st1);
+    for (int mp = -J.l; mp <= J.l; ++mp) {
+        double s1, c1, s3, c3;
+        dm_sincos(-((double)mp * t1), &s1, &c1);
+        dm_sincos(-((double)J.m * t3), &s3, &c3);
+        double d = wigner_d(J.l, mp, J.m, t2);
+        dm_cplx D = dm_cmul(dm_cscale(dm_c(c1, s1), d), dm_c(c3, s3));
+        B.D[2 * (mp + J.l)] = D.re;
+        B.D[2 * (mp + J.l) + 1] = D.im;
+    }
+    out[b] = B;
+}
+
+// The k-sum of the solid harmonic (shared_methods.jl:21).
+__device__ dm_cplx sph_sum(int l, int m, dm_cplx x, dm_cplx y, dm_cplx z) {
+    dm_cplx xp = dm_c(x.re - y.im, x.im + y.re);
+    dm_cplx xm = dm_c(x.re + y.im, x.im - y.re);
+    int kmin = (m < 0) ? -m : 0, kmax = (l - m) / 2;
+    dm_cplx acc = dm_c(0.0, 0.0);
+    for (int k = kmin; k <= kmax; ++k) {
+        double den = fact(k + m) * fact(k) * fact(l - m - 2 * k);
+        double p2 = 1.0;
+        for (int i = 0; i < 2 * k + m; ++i) p2 *= 2.0;
+        double coef = ((k & 1) ? -1.0 : 1.0) / (p2 * den);
+        dm_cplx tt = dm_cscale(dm_cpowi(xp, k + m), coef);
+        tt = dm_cmul(tt, dm_cpowi(xm, k));
+        tt = dm_cmul(tt, dm_cpowi(z, l - m - 2 * k));
+        acc = (k == kmin) ? tt : dm_cadd(acc, tt);
+    }
+    return acc;
+}
+
+// Sum over m' of C D^l_{m' m} Y_{l m'} (ADKSampler.jl:243-265).
+__device__ dm_cplx pre_numerator(const DJob& J, const DBatch& B, dm_cplx kx, dm_cplx ky, dm_cplx kz) {
+    dm_cplx ckx = dm_cconj(kx), cky = dm_cconj(ky), ckz = dm_cconj(kz);
+    dm_cplx nkx = dm_cadd(dm_cadd(dm_cscale(ckx, 0.0), dm_cscale(cky, 0.0)), dm_cscale(ckz, 1.0));
+    dm_cplx nky = dm_cadd(dm_cadd(dm_cscale(ckx, B.ny0), dm_cscale(cky, B.ny1)), dm_cscale(ckz, 0.0));
+    dm_cplx nkz = dm_cadd(dm_cadd(dm_cscale(ckx, B.nz0), dm_cscale(cky, B.nz1)), dm_cscale(ckz, 0.0));
+    dm_cplx acc = dm_c(0.0, 0.0);
+    for (int mp = -J.l; mp <= J.l; ++mp) {
+        int i = mp + J.l;
+        dm_cplx P = dm_c(J.Plm[2 * i], J.Plm[2 * i + 1]);
+        dm_cplx Y = dm_cmul(P, sph_sum(J.l, mp, nkx, nky, nkz));
+        dm_cplx term = dm_cmul(dm_cscale(dm_c(B.D[2 * i], B.D[2 * i + 1]), J.C), Y);
+        acc = (mp == -J.l) ? term : dm_cadd(acc, term);
+    }
+    return acc;
+}
+
+__global__ void __launch_bounds__(256)
+k_sample(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double* __restrict__ kdv,
+         const double* __restrict__ kzv, const DBatch* __restrict__ batches, InitSoA soa,
+         uint8_t* __restrict__ flag) {
+    const int64_t total = nb * J.n_cand;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t bl = q / J.n_cand, i = q - bl * J.n_cand, b = b0 + bl;
+        const DBatch& B = batches[b];
+        double kd0, kz0;
+        if (!J.mc) {
+            kd0 = kdv[i / J.n_kz];
+            kz0 = kzv[i % J.n_kz];
+        } else {
+            uint32_t c[4] = {(uint32_t)i, (uint32_t)((uint64_t)i >> 32), (uint32_t)b, 0x4B445A00u};
+            philox4x32(c, J.seed);
+            double ua = u53(c[0], c[1]), ub = u53(c[2], c[3]);
+            kd0 = ((ua - 0.5) * 2.0) * J.mc_kd_max;
+            if (J.dim == 3) {
+                kz0 = ((ub - 0.5) * 2.0) * J.mc_kz_max;
+                if (J.mc_kd_max == 0.0) kd0 = 0.0;
+                else if (J.mc_kz_max == 0.0) kz0 = 0.0;
+            } else {
+                kz0 = 0.0;
+            }
+        }
+        uint8_t keep = 0;
+        double x0 = 0.0, y0 = 0.0, kx0 = 0.0, ky0 = 0.0, rate = 0.0, ph = 0.0;
+        if (!(fabs(kd0) < 1e-4)) {
+            const double Ip = J.Ip, F = B.F;
+            kx0 = kd0 * (-B.sphi);
+            ky0 = kd0 * B.cphi;
+            const bool spane = (J.method == ETRAJ_SAMPLER_SPANE);
+            double F2eff = 0.0, ti, X2, Fexp;
+            bool skip = false;
+            if (!spane) {
+                double r0 = (Ip + (kd0 * kd0 + kz0 * kz0) / 2.0) / F;
+                x0 = r0 * B.cphi;
+                y0 = r0 * B.sphi;
+                ti = sqrt((J.kappa * J.kappa + kd0 * kd0) + kz0 * kz0) / F;
+                X2 = (((kx0 * kx0 + ky0 * ky0) + kz0 * kz0) + 2.0 * Ip) * (F * F);
+                Fexp = F;
+            } else {
+                F2eff = F * F - (kx0 * B.dFx + ky0 * B.dFy);
+                double Xk = ((kx0 * kx0 + ky0 * ky0) + kz0 * kz0) + 2.0 * Ip;
+                double r0 = ((F / 2.0) * Xk) / F2eff;
+                x0 = r0 * B.cphi;
+                y0 = r0 * B.sphi;
+                double lim = J.mc ? (F * F) / 25.0 : (F * F) / 9.0;
+                skip = (F2eff <= lim);
+                ti = sqrt(((J.kappa * J.kappa + kd0 * kd0) + kz0 * kz0) / F2eff);
+                X2 = Xk * F2eff;
+                Fexp = sqrt(F2eff);
+            }
+            if (!skip) {
+                double Xe = (kd0 * kd0 + kz0 * kz0) + 2.0 * Ip;
+                double E = dm_exp(-(Xe * sqrt(Xe)) / (3.0 * Fexp));
+                double r1 = sqrt(J.dkdt) * E;
+                dm_cplx amp;
+                if (J.prefix & (ETRAJ_PREFIX_PRE | ETRAJ_PREFIX_PRECC)) {
+                    dm_cplx kx, ky, kz = dm_c(kz0, 0.0);
+                    if (!spane) {
+                        kx = dm_c(kx0, -(ti * B.Fx));
+                        ky = dm_c(ky0, -(ti * B.Fy));
+                    } else {
+                        double h = (ti * ti) / 2.0;
+                        kx = dm_c(kx0 + h * B.dFx, -(ti * B.Fx));
+                        ky = dm_c(ky0 + h * B.dFy, -(ti * B.Fy));
+                    }
+                    dm_cplx num = pre_numerator(J, B, kx, ky, kz);
+                    double cpre = (J.prefix & ETRAJ_PREFIX_PRE) ? J.c : B.c_cc;
+                    double den = (J.e_pre == 0.5) ? sqrt(X2) : dm_pow_pos(X2, J.e_pre);
+                    dm_cplx pre = dm_cscale(num, cpre);
+                    pre = dm_c(pre.re / den, pre.im / den);
+                    amp = dm_cscale(pre, r1);
+                } else {
+                    amp = dm_c(r1, 0.0);
+                }
+                if (J.prefix & ETRAJ_PREFIX_JAC) {
+                    double jac = spane ? fabs(F + (sqrt(kd0 * kd0 + kz0 * kz0) / (F * F)) * B.W) : F;
+                    amp = dm_cscale(amp, sqrt(jac));
+                }
+                rate = amp.re * amp.re + amp.im * amp.im;
+                double crit = spane ? rate / J.dkdt : rate;
+                keep = (!(rate != rate) && !(crit < J.cutoff)) ? 1 : 0;
+                if (keep && J.phase != ETRAJ_PHASE_CTMC) ph = dm_carg(amp);
+            }
+        }
+        const int64_t g = b * J.n_cand + i;
+        flag[g] = keep;
+        if (keep) {
+            soa.x[g] = x0;
+            soa.y[g] = y0;
+            soa.kx[g] = kx0;
+            soa.ky[g] = ky0;
+            soa.kz[g] = kz0;
+            soa.rate[g] = rate;
+            if (soa.phase) soa.phase[g] = ph;
+            soa.batch[g] = (int32_t)b;
+        }
+    }
+}
+
+// ---- order-preserving compaction -------------------------------------------------
+constexpr int kCompactThreads = 256;
+constexpr int kCompactItems = 8;
+constexpr int kCompactChunk = kCompactThreads * kCompactItems;
+
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* total) {
+    __shared__ uint32_t warp_sums[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = (lane < nw) ? warp_sums[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < nw) warp_sums[lane] = w;
+    }
+    __syncthreads();
+    uint32_t base = (warp > 0) ? warp_sums[warp - 1] : 0u;
+    if (total) *total = warp_sums[nw - 1];
+    uint32_t r = base + x - v;
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(kCompactThreads)
+k_compact_count(const uint8_t* __restrict__ flag, int64_t n, uint32_t* __restrict__ block_sums) {
+    const int64_t base = (int64_t)blockIdx.x * kCompactChunk + (int64_t)threadIdx.x * kCompactItems;
+    uint32_t c = 0;
+#pragma unroll
+    for (int k = 0; k < kCompactItems; ++k) c += (base + k < n && flag[base + k]) ? 1u : 0u;
+    c = __reduce_add_sync(0xffffffffu, c);
+    __shared__ uint32_t ws[kCompactThreads / 32];
+    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t s = 0;
+        for (int w = 0; w < kCompactThreads / 32; ++w) s += ws[w];
+        block_sums[blockIdx.x] = s;
+    }
+}
+
+// Exclusive scan of block_sums in place (one block), total to *count.
+__global__ void __launch_bounds__(1024)
+k_compact_scan(uint32_t* __restrict__ block_sums, int64_t nblocks, unsigned long long* __restrict__ count) {
+    __shared__ unsigned long long carry;
+    if (threadIdx.x == 0) carry = 0ull;
+    __syncthreads();
+    for (int64_t off = 0; off < nblocks; off += blockDim.x) {
+        int64_t i = off + threadIdx.x;
+        uint32_t v = (i < nblocks) ? block_sums[i] : 0u;
+        uint32_t tot;
+        uint32_t ex = block_exclusive_scan(v, &tot);
+        if (i < nblocks) block_sums[i] = (uint32_t)(carry + ex);
+        __syncthreads();
+        if (threadIdx.x == 0) carry += tot;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *count = carry;
+}
+
+__global__ void __launch_bounds__(kCompactThreads)
+k_compact_scatter(const uint8_t* __restrict__ flag, int64_t n, const uint32_t* __restrict__ block_off,
+                  int64_t* __restrict__ idx) {
+    const int64_t base = (int64_t)blockIdx.x * kCompactChunk + (int64_t)threadIdx.x * kCompactItems;
+    uint8_t f[kCompactItems];
+    uint32_t c = 0;
+#pragma unroll
+    for (int k = 0; k < kCompactItems; ++k) {
+        f[k] = (base + k < n) ? flag[base + k] : 0;
+        c += f[k] ? 1u : 0u;
+    }
+    uint32_t ex = block_exclusive_scan(c, nullptr);
+    int64_t pos = (int64_t)block_off[blockIdx.x] + ex;
+#pragma unroll
+    for (int k = 0; k < kCompactItems; ++k)
+        if (f[k]) idx[pos++] = base + k;
+}
+
+}  // namespace
+
+int launch_batch_prepare(const DJob& J, const double* t, DBatch* batches, cudaStream_t s) {
+    int threads = 128;
+    int blocks = (int)((J.n_t + threads - 1) / threads);
+    k_batch_prepare<<<blocks, threads, 0, s>>>(J, t, batches);
+    return 1;
+}
+
+int launch_sample_range(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
+                        const DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
+                        cudaStream_t s) {
+    int threads = 256;
+    int64_t want = (nb * J.n_cand + threads - 1) / threads;
+    int64_t cap = (int64_t)sm_count * 32;
+    int blocks = (int)(want < cap ? (want > 0 ? want : 1) : cap);
+    k_sample<<<blocks, threads, 0, s>>>(J, b0, nb, kd, kz, batches, soa, flag);
+    return 1;
+}
+
+int64_t compact_blocks(int64_t n) { return (n + kCompactChunk - 1) / kCompactChunk; }
+
+int launch_compact(const uint8_t* flag, int64_t n, int64_t* idx, uint32_t* block_sums,
+                   int64_t nblocks_cap, unsigned long long* count, cudaStream_t s) {
+    int64_t nb = compact_blocks(n);
+    if (nb > nblocks_cap || nb == 0) {
+        cudaMemsetAsync(count, 0, sizeof(unsigned long long), s);
+        return 0;
+    }
+    k_compact_count<<<(unsigned)nb, kCompactThreads, 0, s>>>(flag, n, block_sums);
+    k_compact_scan<<<1, 1024, 0, s>>>(block_sums, nb, count);
+    k_compact_scatter<<<(unsigned)nb, kCompactThreads, 0, s>>>(flag, n, block_sums, idx);
+    return 3;
+}
+
+}  // namespace etraj

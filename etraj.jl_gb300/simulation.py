@@ -189,9 +189,11 @@ class Engine:
                                              abi.i32ptr(status), abi.i32ptr(steps)))
         return fin, status, steps
 
-    def submit(self, job):
+    def submit(self, job, res):
+        """Queue `job`; `res` (an abi.Result) carries the output pointers, which must stay
+        valid until poll/wait reports the ticket done."""
         t = C.c_uint64()
-        self._check(self.lib.etraj_submit(self.ctx, C.byref(job), C.byref(t)))
+        self._check(self.lib.etraj_submit(self.ctx, C.byref(job), C.byref(res), C.byref(t)))
         return t.value
 
     def poll(self, ticket, res):

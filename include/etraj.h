@@ -203,8 +203,13 @@ int etraj_sample_all(etraj_ctx* ctx, const etraj_job* job,
 int etraj_integrate(etraj_ctx* ctx, const etraj_job* job, int64_t n, const double* init,
                     double* final_state, int32_t* status, int32_t* steps);
 
-/* ---- asynchronous jobs (serving loop) ---------------------------------------- */
-int etraj_submit(etraj_ctx* ctx, const etraj_job* job, uint64_t* ticket);
+/* ---- asynchronous jobs (serving loop) ----------------------------------------
+ * etraj_submit queues a job; `out` supplies the caller-owned output pointers
+ * (momentum_spec, amplitude), which must stay valid until etraj_poll or
+ * etraj_wait has returned ETRAJ_OK for the ticket.  etraj_poll returns
+ * ETRAJ_ERR_NOT_READY while the job runs; both fill the scalars of `out`
+ * (its pointers are left as they are) and release the ticket. */
+int etraj_submit(etraj_ctx* ctx, const etraj_job* job, etraj_result* out, uint64_t* ticket);
 int etraj_poll(etraj_ctx* ctx, uint64_t ticket, etraj_result* out);
 int etraj_wait(etraj_ctx* ctx, uint64_t ticket, etraj_result* out);
 
