@@ -114,6 +114,7 @@ SIGNATURES = [
     ("etraj_submit", C.c_int, [C.c_void_p, C.POINTER(Job), C.POINTER(Result), C.POINTER(C.c_uint64)]),
     ("etraj_poll", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(Result)]),
     ("etraj_wait", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(Result)]),
+    ("etraj_stage_times", C.c_int, [C.c_void_p, _DP, C.c_int]),
 ]
 
 _lib = None

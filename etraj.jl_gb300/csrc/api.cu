@@ -35,7 +35,7 @@ int launch_sample_range(const DJob& J, int64_t b0, int64_t nb, const double* kd,
 
 namespace {
 
-constexpr bool kHaveFp32Bulk = false;
+constexpr bool kHaveFp32Bulk = true;
 
 // ---- host-side job set-up (same expressions as the reference's getters) ----------
 void mono_prepare(const etraj_mono_laser& in, DMono& L) {
@@ -344,6 +344,11 @@ struct etraj_ctx {
     std::string err;
     std::map<std::string, DevBuf> bufs;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // stage boundaries of the last etraj_run: sample | compact | field table |
+    // integrate | collect | deposit
+    static constexpr int kStages = 6;
+    cudaEvent_t stage_ev[kStages + 1] = {};
+    bool stage_valid = false;
     uint64_t next_ticket = 1;
     std::map<uint64_t, AsyncJob> jobs;
     std::mutex mu;
@@ -476,12 +481,64 @@ int alloc_outputs(etraj_ctx* ctx, const DJob& J, int64_t max_n, bool with_state,
     return ETRAJ_OK;
 }
 
+// Bulk-integrator parameters: field table spanning [tmin, t_final] with
+// spacing T_min/128 (T_min the shortest laser period).
+void prepare_bulk(const DJob& J, double tmin, BulkParams& B) {
+    std::memset(&B, 0, sizeof B);
+    B.dim = J.dim;
+    B.phase = J.phase;
+    B.tgt = J.target.kind;
+    double T = J.laser.m[0].period;
+    if (J.laser.nmono == 2) T = std::min(T, J.laser.m[1].period);
+    const double h = T / 128.0;
+    B.T0 = tmin - h;
+    B.n_int = (int)std::ceil((J.t_final - B.T0) / h) + 2;
+    B.inv_h_d = 1.0 / h;
+    B.h = (float)h;
+    B.inv_h = (float)(1.0 / h);
+    B.t_final = J.t_final;
+    const double q = (J.t_final - B.T0) / h;
+    const double fl = std::floor(q);
+    B.nf = (int)fl;
+    B.ff = (float)(q - fl);
+    B.rtol = (float)J.rtol;
+    B.table_in_smem = ((size_t)B.n_int * 2 * sizeof(float4) <= (size_t)96 * 1024) ? 1 : 0;
+    B.threads = 256;
+    B.blocks_per_sm = 2;
+    B.refill_min = 4;
+    const DTarget& T_ = J.target;
+    B.Z = (float)T_.Z;
+    B.Ip = (float)T_.Ip;
+    B.sc = (float)T_.sc;
+    B.a1 = (float)T_.a1; B.b1 = (float)T_.b1;
+    B.a2 = (float)T_.a2; B.b2 = (float)T_.b2;
+    B.a3 = (float)T_.a3; B.b3 = (float)T_.b3;
+    B.a2b2 = (float)(T_.a2 * T_.b2);
+}
+
 int launch_integrate(etraj_ctx* ctx, const DJob& J, const InitSoA& soa, const double* t, const int64_t* idx,
                      const unsigned long long* count, const TrajOut& out, int64_t max_n, unsigned long long* work,
-                     int precision) {
-    (void)work;
-    (void)precision;
-    return launch_integrate_fp64(J, soa, t, idx, count, out, max_n, ctx->sm_count, ctx->stream);
+                     int precision, double tmin, int* launches, cudaEvent_t* ev = nullptr) {
+    // ev (optional): events recorded after the field table [0] and the integrator [1]
+    cudaStream_t s = ctx->stream;
+    if (precision != ETRAJ_PRECISION_FP32_BULK) {
+        if (ev) cudaEventRecord(ev[0], s);
+        *launches += launch_integrate_fp64(J, soa, t, idx, count, out, max_n, ctx->sm_count, s);
+        if (ev) cudaEventRecord(ev[1], s);
+        return ETRAJ_OK;
+    }
+    BulkParams B;
+    prepare_bulk(J, tmin, B);
+    float4* tab = nullptr;
+    ETRAJ_TRY(ensure_t(ctx, "field_table", (size_t)B.n_int * 2, &tab));
+    B.table = tab;
+    *launches += launch_field_table(J, B.T0, (double)1.0 / B.inv_h_d, B.n_int, tab, s);
+    cudaMemsetAsync(work, 0, sizeof(unsigned long long), s);
+    if (ev) cudaEventRecord(ev[0], s);
+    *launches += launch_integrate_bulk(B, soa, t, idx, count, work, out, ctx->sm_count, s);
+    if (ev) cudaEventRecord(ev[1], s);
+    *launches += launch_collect_fp64(J, soa, t, idx, count, out, max_n, ctx->sm_count, s);
+    return ETRAJ_OK;
 }
 
 int run_job(etraj_ctx* ctx, const etraj_job* job, etraj_result* res) {
@@ -493,21 +550,27 @@ int run_job(etraj_ctx* ctx, const etraj_job* job, etraj_result* res) {
     const DJob& J = H.J;
     Pipeline P;
     ETRAJ_TRY(alloc_sampling(ctx, H, P));
-    ETRAJ_TRY(alloc_outputs(ctx, J, J.n_total, false, P));
+    ETRAJ_TRY(alloc_outputs(ctx, J, J.n_total, job->precision == ETRAJ_PRECISION_FP32_BULK, P));
     cudaStream_t s = ctx->stream;
     int launches = 0;
     cudaMemcpyAsync(P.t, H.t.data(), H.t.size() * sizeof(double), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(P.kd, H.kd.data(), H.kd.size() * sizeof(double), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(P.kz, H.kz.data(), H.kz.size() * sizeof(double), cudaMemcpyHostToDevice, s);
     cudaEventRecord(ctx->ev0, s);
+    cudaEventRecord(ctx->stage_ev[0], s);
     launches += launch_batch_prepare(J, P.t, P.batches, s);
     launches += launch_sample_range(J, 0, J.n_t, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s);
+    cudaEventRecord(ctx->stage_ev[1], s);
     launches += launch_compact(P.flag, J.n_total, P.idx, P.block_sums, compact_blocks(J.n_total) + 1, P.count, s);
-    cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), s);
-    launches += launch_integrate(ctx, J, P.soa, P.t, P.idx, P.count, P.out, J.n_total, P.work, job->precision);
+    cudaEventRecord(ctx->stage_ev[2], s);
+    ETRAJ_TRY(launch_integrate(ctx, J, P.soa, P.t, P.idx, P.count, P.out, J.n_total, P.work, job->precision,
+                               H.t.front(), &launches, ctx->stage_ev + 3));
+    cudaEventRecord(ctx->stage_ev[5], s);
     launches += launch_deposit(J, P.out, P.count, J.n_total, P.dep, P.spec_re, P.spec_im, P.mspec, P.sums,
                                P.counters, s);
+    cudaEventRecord(ctx->stage_ev[6], s);
     cudaEventRecord(ctx->ev1, s);
+    ctx->stage_valid = true;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_err(ctx, e, "kernel launch");
     double sums[2] = {0.0, 0.0};
@@ -629,6 +692,11 @@ int etraj_create(etraj_ctx** out, int device, size_t hbm_budget_bytes) {
         delete ctx;
         return ETRAJ_ERR_CUDA;
     }
+    for (int i = 0; i <= etraj_ctx::kStages; ++i) {
+        if (cudaEventCreate(&ctx->stage_ev[i]) == cudaSuccess) continue;
+        delete ctx;
+        return ETRAJ_ERR_CUDA;
+    }
     ctx->stream = ctx->own_stream;
     *out = ctx;
     return ETRAJ_OK;
@@ -642,6 +710,8 @@ void etraj_destroy(etraj_ctx* ctx) {
         if (kv.second.p) cudaFree(kv.second.p);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    for (int i = 0; i <= etraj_ctx::kStages; ++i)
+        if (ctx->stage_ev[i]) cudaEventDestroy(ctx->stage_ev[i]);
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
 }
@@ -752,8 +822,9 @@ int etraj_integrate(etraj_ctx* ctx, const etraj_job* job, int64_t n, const doubl
     up(P.t, t0.data(), (size_t)n * 8);
     unsigned long long cn = (unsigned long long)n;
     up(P.count, &cn, sizeof cn);
-    cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), s);
-    launch_integrate(ctx, J, P.soa, P.t, nullptr, P.count, P.out, n, P.work, job->precision);
+    int nl = 0;
+    ETRAJ_TRY(launch_integrate(ctx, J, P.soa, P.t, nullptr, P.count, P.out, n, P.work, job->precision,
+                               *std::min_element(t0.begin(), t0.end()), &nl));
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_err(ctx, e, "integrate launch");
     std::vector<int32_t> stv((size_t)n);
@@ -801,5 +872,19 @@ int etraj_poll(etraj_ctx* ctx, uint64_t ticket, etraj_result* out) {
 }
 
 int etraj_wait(etraj_ctx* ctx, uint64_t ticket, etraj_result* out) { return etraj_poll(ctx, ticket, out); }
+
+int etraj_stage_times(etraj_ctx* ctx, double* ms, int n) {
+    if (!ctx || !ms) return 0;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    if (!ctx->stage_valid) return 0;
+    if (cudaEventSynchronize(ctx->stage_ev[etraj_ctx::kStages]) != cudaSuccess) return 0;
+    int k = 0;
+    for (; k < etraj_ctx::kStages && k < n; ++k) {
+        float f = 0.f;
+        cudaEventElapsedTime(&f, ctx->stage_ev[k], ctx->stage_ev[k + 1]);
+        ms[k] = f;
+    }
+    return k;
+}
 
 }  // extern "C"

@@ -27,6 +27,7 @@ UNITS = {
     "sampler.cu": ["--fmad=false"],
     "integrate_fp64.cu": ["--fmad=false"],
     "deposit.cu": ["--fmad=false"],
+    "integrate_fp32.cu": ["--fmad=true"],
 }
 HEADERS = ["engine.h", "physics.cuh", "detmath.h"]
 

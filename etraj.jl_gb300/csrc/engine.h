@@ -105,9 +105,29 @@ int64_t compact_blocks(int64_t n);
 int launch_integrate_fp64(const DJob& J, InitSoA soa, const double* t, const int64_t* idx,
                           const unsigned long long* count, TrajOut out, int64_t max_n,
                           int sm_count, cudaStream_t s);
-int launch_integrate_fp32(const DJob& J, InitSoA soa, const double* t, const int64_t* idx,
-                          const unsigned long long* count, TrajOut out, int64_t max_n,
-                          unsigned long long* work_counter, int sm_count, cudaStream_t s);
+// FP64 collection of final states written by the bulk integrator (same code as
+// the epilogue of the plain kernel).
+int launch_collect_fp64(const DJob& J, InitSoA soa, const double* t, const int64_t* idx,
+                        const unsigned long long* count, TrajOut out, int64_t max_n, int sm_count,
+                        cudaStream_t s);
+
+// Parameters of the FP32 bulk integrator (integrate_fp32.cu).
+struct BulkParams {
+    int dim, phase, tgt;
+    int n_int;          // field-table intervals
+    int table_in_smem;  // 1: stage the table in shared memory
+    int threads, blocks_per_sm, refill_min;
+    const float4* table;
+    double T0, inv_h_d, t_final;
+    float h, inv_h, rtol;
+    int nf;             // t_final = T0 + h (nf + ff)
+    float ff;
+    float Z, Ip, sc, a1, b1, a2, b2, a3, b3, a2b2;
+};
+int launch_field_table(const DJob& J, double T0, double h, int n_int, float4* tab, cudaStream_t s);
+int launch_integrate_bulk(const BulkParams& P, InitSoA soa, const double* t, const int64_t* idx,
+                          const unsigned long long* count, unsigned long long* queue, TrajOut out,
+                          int sm_count, cudaStream_t s);
 
 // Deterministic deposit: stable radix sort of (key, survivor) and segmented sums.
 struct DepositScratch {

@@ -353,6 +353,26 @@ k_integrate_fp64(const __grid_constant__ DJob J, InitSoA soa, const double* __re
     }
 }
 
+// Collection of final states computed elsewhere (the FP32 bulk integrator).
+template <int DIM, int PHASE>
+__global__ void __launch_bounds__(128)
+k_collect_fp64(const __grid_constant__ DJob J, InitSoA soa, const double* __restrict__ tsamp,
+               const int64_t* __restrict__ idx, const unsigned long long* __restrict__ count,
+               TrajOut out) {
+    constexpr int N = (DIM == 3 ? 6 : 4) + (PHASE != ETRAJ_PHASE_CTMC ? 1 : 0);
+    const int64_t n = (int64_t)(*count);
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t g = idx ? idx[s] : s;
+        double f[N];
+#pragma unroll
+        for (int j = 0; j < N; ++j) f[j] = out.final_state[s * N + j];
+        const int st = out.status[s] & 0xff;
+        const bool ion = collect<DIM, PHASE, N>(J, st, f, tsamp[soa.batch[g]], soa.rate[g], out, s);
+        out.status[s] = st | (ion ? 0x100 : 0);
+    }
+}
+
 template <int DIM, int PHASE, int TGT>
 int launch_t(const DJob& J, InitSoA soa, const double* t, const int64_t* idx,
              const unsigned long long* count, TrajOut out, int64_t max_n, int sm_count,
@@ -385,6 +405,27 @@ int launch_integrate_fp64(const DJob& J, InitSoA soa, const double* t, const int
         ETRAJ_DISPATCH_TGT(3, ETRAJ_PHASE_SCTS)
     }
 #undef ETRAJ_DISPATCH_TGT
+}
+
+int launch_collect_fp64(const DJob& J, InitSoA soa, const double* t, const int64_t* idx,
+                        const unsigned long long* count, TrajOut out, int64_t max_n, int sm_count,
+                        cudaStream_t s) {
+    const int threads = 128;
+    int64_t want = (max_n + threads - 1) / threads;
+    int64_t cap = (int64_t)sm_count * 16;
+    int blocks = (int)(want < cap ? (want > 0 ? want : 1) : cap);
+#define ETRAJ_COLLECT(D, P) k_collect_fp64<D, P><<<blocks, threads, 0, s>>>(J, soa, t, idx, count, out)
+    if (J.dim == 2) {
+        if (J.phase == ETRAJ_PHASE_CTMC) ETRAJ_COLLECT(2, ETRAJ_PHASE_CTMC);
+        else if (J.phase == ETRAJ_PHASE_QTMC) ETRAJ_COLLECT(2, ETRAJ_PHASE_QTMC);
+        else ETRAJ_COLLECT(2, ETRAJ_PHASE_SCTS);
+    } else {
+        if (J.phase == ETRAJ_PHASE_CTMC) ETRAJ_COLLECT(3, ETRAJ_PHASE_CTMC);
+        else if (J.phase == ETRAJ_PHASE_QTMC) ETRAJ_COLLECT(3, ETRAJ_PHASE_QTMC);
+        else ETRAJ_COLLECT(3, ETRAJ_PHASE_SCTS);
+    }
+#undef ETRAJ_COLLECT
+    return 1;
 }
 
 }  // namespace etraj

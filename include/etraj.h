@@ -209,6 +209,13 @@ int etraj_integrate(etraj_ctx* ctx, const etraj_job* job, int64_t n, const doubl
  * etraj_wait has returned ETRAJ_OK for the ticket.  etraj_poll returns
  * ETRAJ_ERR_NOT_READY while the job runs; both fill the scalars of `out`
  * (its pointers are left as they are) and release the ticket. */
+/* ---- diagnostics ----------------------------------------------------------------
+ * Device time (ms) of the stages of the last etraj_run on this context: sampling,
+ * compaction, field table, integrator, collection, deposit.  Writes up to n
+ * values and returns how many were written (0 before the first run).  No
+ * counterpart in the reference, which has no stage timers. */
+int etraj_stage_times(etraj_ctx* ctx, double* ms, int n);
+
 int etraj_submit(etraj_ctx* ctx, const etraj_job* job, etraj_result* out, uint64_t* ticket);
 int etraj_poll(etraj_ctx* ctx, uint64_t ticket, etraj_result* out);
 int etraj_wait(etraj_ctx* ctx, uint64_t ticket, etraj_result* out);

@@ -255,7 +255,8 @@ def test_gpu_config1_full_size(eng):
                       ss_kz_num=21, traj_phase_method="CTMC")
     res, spec, _ = eng.run(job)
     rspec, _, rsc = O.run(job)
-    assert res.num_effective_traj == int(rsc["num_effective"]) > 500000
+    # 2000 x 441 candidates; about 1.1e5 survive the default 1e-16 rate cutoff
+    assert res.num_effective_traj == int(rsc["num_effective"]) > 100000
     assert rel_l2(spec, rspec) <= 1e-10
     assert same_bits(spec, rspec)
     assert res.ion_prob == rsc["ion_prob"]
