@@ -482,7 +482,7 @@ int alloc_outputs(etraj_ctx* ctx, const DJob& J, int64_t max_n, bool with_state,
 }
 
 // Bulk-integrator parameters: field table spanning [tmin, t_final] with
-// spacing T_min/128 (T_min the shortest laser period).
+// spacing T_min/512 (T_min the shortest laser period).
 void prepare_bulk(const DJob& J, double tmin, BulkParams& B) {
     std::memset(&B, 0, sizeof B);
     B.dim = J.dim;
@@ -490,7 +490,7 @@ void prepare_bulk(const DJob& J, double tmin, BulkParams& B) {
     B.tgt = J.target.kind;
     double T = J.laser.m[0].period;
     if (J.laser.nmono == 2) T = std::min(T, J.laser.m[1].period);
-    const double h = T / 128.0;
+    const double h = T / 512.0;
     B.T0 = tmin - h;
     B.n_int = (int)std::ceil((J.t_final - B.T0) / h) + 2;
     B.inv_h_d = 1.0 / h;
