@@ -115,6 +115,8 @@ SIGNATURES = [
     ("etraj_poll", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(Result)]),
     ("etraj_wait", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(Result)]),
     ("etraj_stage_times", C.c_int, [C.c_void_p, _DP, C.c_int]),
+    ("etraj_deposit_noalloc", C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
+                                        C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
 ]
 
 _lib = None

@@ -382,3 +382,121 @@ int launch_deposit(const DJob& J, const TrajOut& out, const unsigned long long* 
 }
 
 }  // namespace etraj
+
+// ---- deposit without allocation ------------------------------------------------------
+//
+// Some callers cannot allocate device memory while they call into this library:
+// a host that lets only its own memory pool own device memory (for example a
+// Julia program whose CUDA.jl arrays are the only allocations it permits), a
+// caller that reserves all of its memory before a latency-critical run, or code
+// that must not synchronize the device, as cudaMalloc and cudaFree may.  For
+// them etraj_deposit_noalloc runs the deterministic deposit (stable radix sort
+// of (bin, electron), per-bin sums in electron order, |A|^2) on caller-owned
+// inputs and outputs, with its sort scratch in one fixed device array declared
+// below.  The array's size is fixed at build time (kNoallocMaxN contributions,
+// about 8 MiB) and every GPU that loads this library holds it until the
+// process exits.
+
+#include <mutex>
+
+namespace etraj {
+namespace {
+
+constexpr int64_t kNoallocMaxN = (int64_t)1 << 19;
+constexpr int64_t kNoallocTiles = (kNoallocMaxN + kTile - 1) / kTile;
+constexpr int64_t kNoallocHist = 256 * kNoallocTiles;
+constexpr int64_t kNoallocParts = (kNoallocHist + kScanChunk - 1) / kScanChunk;
+// layout: keys_a | keys_b | vals_a | vals_b | hist | scan partials | count
+constexpr size_t kNoallocOffHist = (size_t)4 * kNoallocMaxN * sizeof(uint32_t);
+constexpr size_t kNoallocOffParts = kNoallocOffHist + (size_t)kNoallocHist * sizeof(uint32_t);
+constexpr size_t kNoallocOffCount = (kNoallocOffParts + (size_t)(kNoallocParts + 64) * sizeof(uint32_t) + 255) & ~(size_t)255;
+constexpr size_t kNoallocBytes = kNoallocOffCount + 256;
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kMaxDevices] = {};
+
+__global__ void k_set_count(unsigned long long* c, unsigned long long n) { *c = n; }
+
+}  // namespace
+}  // namespace etraj
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[etraj::kNoallocBytes];
+
+namespace etraj {
+namespace {
+
+// Device address of g_noalloc_scratch on the current device.  The symbol's
+// host-side name is only a stand-in, so the address is looked up once per
+// device with that device current (cudaGetSymbolAddress) and cached.
+int noalloc_scratch(void** out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return ETRAJ_ERR_CUDA;
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            cudaGetLastError();
+            return ETRAJ_ERR_CUDA;
+        }
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return ETRAJ_OK;
+}
+
+}  // namespace
+}  // namespace etraj
+
+extern "C" int etraj_deposit_noalloc(int64_t n, const uint32_t* key, const double* c_re,
+                                     const double* c_im, int64_t grid, int coherent, double* spec_re,
+                                     double* spec_im, double* momentum_spec, void* cuda_stream) {
+    using namespace etraj;
+    if (n < 0 || n > kNoallocMaxN) return ETRAJ_ERR_INVALID_ARGUMENT;
+    if (grid < 1 || grid >= (int64_t)0xFFFFFFFFll) return ETRAJ_ERR_INVALID_ARGUMENT;
+    if (!spec_re || !momentum_spec || (coherent && !spec_im)) return ETRAJ_ERR_INVALID_ARGUMENT;
+    if (n > 0 && (!key || !c_re || (coherent && !c_im))) return ETRAJ_ERR_INVALID_ARGUMENT;
+    void* base = nullptr;
+    int st = noalloc_scratch(&base);
+    if (st != ETRAJ_OK) return st;
+    cudaStream_t s = (cudaStream_t)cuda_stream;
+    unsigned char* p = (unsigned char*)base;
+    uint32_t* kbuf[2] = {(uint32_t*)p, (uint32_t*)p + kNoallocMaxN};
+    uint32_t* vbuf[2] = {(uint32_t*)p + 2 * kNoallocMaxN, (uint32_t*)p + 3 * kNoallocMaxN};
+    uint32_t* hist = (uint32_t*)(p + kNoallocOffHist);
+    uint32_t* parts = (uint32_t*)(p + kNoallocOffParts);
+    unsigned long long* count = (unsigned long long*)(p + kNoallocOffCount);
+    // the outputs start at zero; the scratch keeps the previous call's contents and
+    // every part of it that is read is written first (count, histograms, sorted pairs)
+    cudaMemsetAsync(spec_re, 0, (size_t)grid * sizeof(double), s);
+    if (coherent) cudaMemsetAsync(spec_im, 0, (size_t)grid * sizeof(double), s);
+    k_set_count<<<1, 1, 0, s>>>(count, (unsigned long long)n);
+    if (n > 0) {
+        const int64_t nb = tiles_for(n);
+        const int64_t hist_n = 256 * nb;
+        const int64_t np = scan_parts_for(hist_n);
+        const int bits = key_bits(grid);
+        const uint32_t* kin = key;
+        const uint32_t* vin = nullptr;
+        int which = 0;
+        for (int shift = 0; shift < bits; shift += 8) {
+            k_radix_hist<<<(unsigned)nb, kThreads, 0, s>>>(kin, count, shift, nb, hist);
+            k_scan_reduce<<<(unsigned)np, kScanThreads, 0, s>>>(hist, hist_n, parts);
+            k_scan_partials<<<1, kScanThreads, 0, s>>>(parts, np);
+            k_scan_apply<<<(unsigned)np, kScanThreads, 0, s>>>(hist, hist_n, parts);
+            k_radix_scatter<<<(unsigned)nb, kThreads, 0, s>>>(kin, vin, kbuf[which], vbuf[which], count,
+                                                               shift, nb, hist);
+            kin = kbuf[which];
+            vin = vbuf[which];
+            which ^= 1;
+        }
+        int sblocks = (int)((n + 255) / 256);
+        k_segment_sum<<<sblocks, 256, 0, s>>>(kin, vin, count, (uint32_t)grid, c_re, c_im, coherent,
+                                              spec_re, spec_im);
+    }
+    int fblocks = (int)((grid + 255) / 256);
+    if (fblocks > 152 * 16) fblocks = 152 * 16;
+    k_finalize_spec<<<fblocks, 256, 0, s>>>(spec_re, spec_im, grid, coherent, momentum_spec);
+    return (cudaGetLastError() == cudaSuccess) ? ETRAJ_OK : ETRAJ_ERR_CUDA;
+}

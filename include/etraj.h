@@ -216,6 +216,31 @@ int etraj_integrate(etraj_ctx* ctx, const etraj_job* job, int64_t n, const doubl
  * counterpart in the reference, which has no stage timers. */
 int etraj_stage_times(etraj_ctx* ctx, double* ms, int n);
 
+/* ---- deposit without allocation ---------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory while they call this library (their own memory pool owns the device,
+ * or they reserve everything before a run): the deterministic deposit of n
+ * per-electron contributions into a momentum grid, with no cudaMalloc, no
+ * cudaFree and no context.  All pointers are device pointers owned by the
+ * caller:
+ *   key[i]        bin of electron i in [0, grid], grid meaning "not deposited"
+ *                 (larger values are not allowed)
+ *   c_re, c_im    its contribution (c_im read only when coherent != 0)
+ *   spec_re/im    outputs: per-bin sums in electron order (spec_im when coherent)
+ *   momentum_spec output: spec_re (CTMC) or spec_re^2 + spec_im^2 (coherent)
+ * Work is queued on cuda_stream (NULL = legacy default stream); the call
+ * returns without synchronizing.  The sort scratch is one fixed device array
+ * of the library, sized for at most 524288 (2^19) contributions per call
+ * (about 8 MiB, held by every GPU that loads the library until the process
+ * exits); larger n returns ETRAJ_ERR_INVALID_ARGUMENT.  The array is shared
+ * by all calls: calls whose work overlaps on the GPU (different streams,
+ * different host threads) race, so serialize them.  The first call on a
+ * device looks up the array's device address; make that first call before
+ * any stream capture on that device. */
+int etraj_deposit_noalloc(int64_t n, const uint32_t* key, const double* c_re, const double* c_im,
+                          int64_t grid, int coherent, double* spec_re, double* spec_im,
+                          double* momentum_spec, void* cuda_stream);
+
 int etraj_submit(etraj_ctx* ctx, const etraj_job* job, etraj_result* out, uint64_t* ticket);
 int etraj_poll(etraj_ctx* ctx, uint64_t ticket, etraj_result* out);
 int etraj_wait(etraj_ctx* ctx, uint64_t ticket, etraj_result* out);

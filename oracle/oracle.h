@@ -49,6 +49,8 @@ int oracle_collect(const etraj_job* job, int64_t n, const double* init, const do
                    const int32_t* status, const int32_t* steps, double* spec, double* amp,
                    double* scalars, double* p_inf, int32_t* bin);
 int oracle_run(const etraj_job* job, double* spec, double* amp, double* scalars, int nthreads);
+int oracle_contributions(const etraj_job* job, int64_t n, const double* init, const double* final_state,
+                         const int32_t* status, uint32_t* key, double* c_re, double* c_im);
 
 /* physics probes used by the known-answer tests */
 void oracle_laser_eval(const etraj_laser* laser, int64_t n, const double* t, double* Fx,

@@ -370,6 +370,31 @@ static void o_collect_one(const etraj_job* job, const o_sys* S, const double* r,
     }
 }
 
+/* Per-electron deposit inputs: bin key (grid when not deposited) and the
+ * contribution w or sqrt(w) e^{i phi}, as the deposit consumes them. */
+int oracle_contributions(const etraj_job* job, int64_t n, const double* init, const double* final_state,
+                         const int32_t* status, uint32_t* key, double* c_re, double* c_im) {
+    o_sys S;
+    o_sys_prepare(job, &S);
+    int rows = (S.dim == 3) ? ((S.phase == ETRAJ_PHASE_CTMC) ? 8 : 9) : ((S.phase == ETRAJ_PHASE_CTMC) ? 6 : 7);
+    int64_t G = 1;
+    for (int d = 0; d < job->dimension; ++d) G *= job->final_p_num[d];
+    for (int64_t i = 0; i < n; ++i) {
+        o_coll C;
+        key[i] = (uint32_t)G;
+        c_re[i] = 0.0;
+        c_im[i] = 0.0;
+        if (status && status[i] != 0) continue;
+        o_collect_one(job, &S, init + i * rows, final_state + i * S.n, &C);
+        if (C.ionized && C.in_grid) {
+            key[i] = (uint32_t)C.bin;
+            c_re[i] = C.are;
+            c_im[i] = C.aim;
+        }
+    }
+    return 0;
+}
+
 /* 256-ary tree sum over v[0..n), each node summed left to right from 0.0 */
 static double o_canon_sum(const double* v, int64_t n) {
     if (n == 0) return 0.0;

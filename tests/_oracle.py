@@ -41,6 +41,7 @@ def lib():
             "oracle_integrate": (C.c_int, [_JP, C.c_int64, _DP, _DP, _I32P, _I32P, C.c_int]),
             "oracle_collect": (C.c_int, [_JP, C.c_int64, _DP, _DP, _I32P, _I32P, _DP, _DP, _DP, _DP, _I32P]),
             "oracle_run": (C.c_int, [_JP, _DP, _DP, _DP, C.c_int]),
+            "oracle_contributions": (C.c_int, [_JP, C.c_int64, _DP, _DP, _I32P, C.c_void_p, _DP, _DP]),
             "oracle_laser_eval": (None, [C.POINTER(abi.Laser), C.c_int64, _DP, _DP, _DP, _DP, _DP, _DP, _DP, _DP]),
             "oracle_laser_eval_complex": (None, [C.POINTER(abi.Laser), C.c_int64, _DP, _DP, _DP, _DP, _DP, _DP]),
             "oracle_target_eval": (None, [C.POINTER(abi.Target), C.c_int64, _DP, _DP, _DP]),
@@ -129,6 +130,17 @@ def collect(job, init, fin, status, steps=None):
                          st.ctypes.data_as(_I32P), None if sp is None else sp.ctypes.data_as(_I32P),
                          _p(spec), _p(amp), _p(sc), _p(pinf), binv.ctypes.data_as(_I32P))
     return spec, amp, dict(zip(SCALARS, sc)), pinf, binv
+
+
+def contributions(job, init, fin, status):
+    n = init.shape[0]
+    key = np.zeros(n, dtype=np.uint32)
+    cre = np.zeros(n)
+    cim = np.zeros(n)
+    st = np.ascontiguousarray(status, dtype=np.int32)
+    lib().oracle_contributions(C.byref(job), n, _p(np.ascontiguousarray(init)), _p(np.ascontiguousarray(fin)),
+                               st.ctypes.data_as(_I32P), key.ctypes.data, _p(cre), _p(cim))
+    return key, cre, cim
 
 
 def run(job):
