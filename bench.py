@@ -85,7 +85,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -190,11 +190,16 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--t-num", type=int, default=10000)
+    ap.add_argument("--t-num", type=int, default=10000,
+                    help="time samples (x 1000 kd candidates); 10000 is the full workload")
+    ap.add_argument("--precision", default="fp32_bulk", choices=["fp32_bulk", "fp64"],
+                    help="path timed as `value` (fp64 profiles the plain kernel)")
+    ap.add_argument("--no-fp64-compare", action="store_true",
+                    help="skip the FP64 run used for the speed ratio and PMD error (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -211,15 +216,12 @@ def main():
     stream = torch.cuda.Stream(device=dev)
     eng.set_stream(stream.cuda_stream)
 
-    job = make_job("fp32_bulk", seed=rank, t_num=args.t_num)
+    job = make_job(args.precision, seed=rank, t_num=args.t_num)
     job64 = make_job("fp64", seed=rank, t_num=args.t_num)
     grid = job.grid_size
 
     # accuracy: FP32-bulk against the FP64 plain path on the same sampled electrons
-    res64, spec64, _ = eng.run(job64, want_spectrum=True)
-    res32, spec32, _ = eng.run(job, want_spectrum=True)
-    pmd_l2 = float(np.linalg.norm(spec32 - spec64) / np.linalg.norm(spec64))
-    t64 = res64.elapsed_ms
+    acc = accuracy_report(eng, job, job64) if not args.no_fp64_compare else None
 
     def sync_all():
         torch.cuda.synchronize(dev)
@@ -285,11 +287,11 @@ def main():
             "config": {"workload": WORKLOAD, "effective_trajectories_per_step": statistics.mean(effs),
                        "candidates_per_step": args.t_num * 1000, "l2_flush": "outputs 1e7 x 64 B > L2",
                        "parallelism": "weak: one Monte-Carlo shard per GPU (seed = rank)"},
-            "fp64_plain": {"value": res64.num_effective_traj / (t64 / 1e3), "unit": UNIT,
-                           "ms_per_step": t64},
-            "speedup_fp32_bulk_vs_fp64": (res64.num_effective_traj / (t64 / 1e3)) and
-            value / world / (res64.num_effective_traj / (t64 / 1e3)),
-            "pmd_rel_l2_vs_fp64": pmd_l2,
+            "precision": args.precision,
+            "fp64_plain": acc and acc["fp64_plain"],
+            "speedup_fp32_bulk_vs_fp64": acc and value / world / acc["fp64_plain"]["value"],
+            "pmd_rel_l2_vs_fp64": acc and acc["pmd_rel_l2_vs_fp64"],
+            "accuracy": acc,
             "latency_ms": {"p50": float(np.percentile(ms, 50)), "p99": float(np.percentile(ms, 99))},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * (args.t_num + 2),
                     "d2h_bytes_per_step": 8 * grid + 64},
@@ -311,6 +313,34 @@ def main():
     if world > 1:
         dist.destroy_process_group()
     return 0
+
+
+def accuracy_report(eng, job, job64):
+    """PMD error of the timed path against the FP64 plain path on the same electrons,
+    next to the FP64 path's own sensitivity to its tolerance (rtol 1e-6 vs 1e-7), at
+    the full 1000 x 1000 resolution and after rebinning to 100 x 100 and 20 x 20."""
+    res64, spec64, _ = eng.run(job64, want_spectrum=True)
+    res, spec, _ = eng.run(job, want_spectrum=True)
+    j7 = job64.copy()
+    j7.traj_rtol = 1e-7
+    _, spec64b, _ = eng.run(j7, want_spectrum=True)
+
+    def l2(a, b):
+        return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+    def rebin(P, f):
+        n = int(round(math.sqrt(P.size)))
+        return P.reshape(n, n).reshape(n // f, f, n // f, f).sum(axis=(1, 3))
+
+    out = {"fp64_plain": {"value": res64.num_effective_traj / (res64.elapsed_ms / 1e3), "unit": UNIT,
+                          "ms_per_step": res64.elapsed_ms},
+           "pmd_rel_l2_vs_fp64": l2(spec, spec64),
+           "fp64_rtol1e-7_vs_rtol1e-6_pmd_rel_l2": l2(spec64b, spec64),
+           "ion_prob_rel_diff": abs(res.ion_prob - res64.ion_prob) / res64.ion_prob}
+    for f in (10, 50):
+        out["pmd_rel_l2_vs_fp64_rebin%d" % f] = l2(rebin(spec, f), rebin(spec64, f))
+        out["fp64_rtol1e-7_vs_rtol1e-6_rebin%d" % f] = l2(rebin(spec64b, f), rebin(spec64, f))
+    return out
 
 
 def integrator_kernel_ms(eng, job, stream):

@@ -210,6 +210,17 @@ int validate_job(const etraj_job* job, std::string& err) {
                                             : job->ss_kd_num * ((job->dimension == 3) ? job->ss_kz_num : 1);
     if ((double)ncand * (double)job->sample_t_num >= 4.0e9)
         return fail("more than 4e9 candidate electrons in one job; split the job.");
+    if (job->precision == ETRAJ_PRECISION_FP32_BULK) {
+        // the bulk integrator's clock counts field-table intervals of T/512 in FP32
+        double T = 6.283185307179586 * job->laser.mono[0].wave_len / 45.563352525;
+        if (nm == 2) T = std::min(T, 6.283185307179586 * job->laser.mono[1].wave_len / 45.563352525);
+        const double span = (job->traj_t_final - job->sample_t_intv[0]) / (T / 512.0);
+        if (!(span < (double)(1 << 21) - 8.0)) {
+            err = "the FP32-bulk integrator covers at most 4096 laser periods from the first time sample "
+                  "to traj_t_final; use FP64 precision.";
+            return ETRAJ_ERR_UNSUPPORTED;
+        }
+    }
     return ETRAJ_OK;
 }
 
@@ -246,6 +257,10 @@ void prepare_job(const etraj_job* job, HostJob& H) {
     J.target.a1 = T.a1; J.target.b1 = T.b1;
     J.target.a2 = T.a2; J.target.b2 = T.b2;
     J.target.a3 = T.a3; J.target.b3 = T.b3;
+    {
+        const double a[3] = {T.a1, T.a2, T.a3}, b[3] = {T.b1, T.b2, T.b3};
+        J.target.skip_ok = etraj_sae_skip_exact((double)T.Z, a, b, T.soft_core);
+    }
     J.Ip = T.Ip;
     J.Z = (double)T.Z;
     J.l = T.l;
@@ -263,6 +278,8 @@ void prepare_job(const etraj_job* job, HostJob& H) {
         dm_cplx P = sph_prefactor(J.l, mp, J.kappa);
         J.Plm[2 * (mp + J.l)] = P.re;
         J.Plm[2 * (mp + J.l) + 1] = P.im;
+        J.fPlm[2 * (mp + J.l)] = (float)P.re;
+        J.fPlm[2 * (mp + J.l) + 1] = (float)P.im;
     }
     // time samples: range(t1, t2; length=n) or sort!(rand(n)*(t2-t1) .+ t1)  (ADKSampler.jl:136,141)
     J.n_t = job->sample_t_num;
@@ -537,7 +554,7 @@ int launch_integrate(etraj_ctx* ctx, const DJob& J, const InitSoA& soa, const do
     if (ev) cudaEventRecord(ev[0], s);
     *launches += launch_integrate_bulk(B, soa, t, idx, count, work, out, ctx->sm_count, s);
     if (ev) cudaEventRecord(ev[1], s);
-    *launches += launch_collect_fp64(J, soa, t, idx, count, out, max_n, ctx->sm_count, s);
+    *launches += launch_collect_bulk(J, soa, t, idx, count, out, max_n, ctx->sm_count, s);
     return ETRAJ_OK;
 }
 
@@ -559,7 +576,10 @@ int run_job(etraj_ctx* ctx, const etraj_job* job, etraj_result* res) {
     cudaEventRecord(ctx->ev0, s);
     cudaEventRecord(ctx->stage_ev[0], s);
     launches += launch_batch_prepare(J, P.t, P.batches, s);
-    launches += launch_sample_range(J, 0, J.n_t, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s);
+    if (job->precision == ETRAJ_PRECISION_FP32_BULK && J.cutoff >= kSample32MinCutoff)
+        launches += launch_sample32_range(J, 0, J.n_t, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s);
+    else
+        launches += launch_sample_range(J, 0, J.n_t, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s);
     cudaEventRecord(ctx->stage_ev[1], s);
     launches += launch_compact(P.flag, J.n_total, P.idx, P.block_sums, compact_blocks(J.n_total) + 1, P.count, s);
     cudaEventRecord(ctx->stage_ev[2], s);

@@ -28,6 +28,7 @@ UNITS = {
     "integrate_fp64.cu": ["--fmad=false"],
     "deposit.cu": ["--fmad=false"],
     "integrate_fp32.cu": ["--fmad=true"],
+    "sampler_fp32.cu": ["--fmad=true"],
 }
 HEADERS = ["engine.h", "physics.cuh", "detmath.h"]
 

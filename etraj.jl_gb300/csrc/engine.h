@@ -12,6 +12,7 @@
 
 #include "../../include/etraj.h"
 #include "detmath.h"
+#include "sae_skip.h"
 
 namespace etraj {
 
@@ -33,15 +34,24 @@ struct DLaser {
 
 struct DTarget {
     int kind;
+    int skip_ok;  // exp(-b r) with b r > 60 may be dropped exactly (sae_exp in physics.cuh)
     double Z, Ip, sc, a1, b1, a2, b2, a3, b3;
 };
 
 // Per-time-sample constants of the ADK/SPANE samplers (the prologue of
 // gen_electron_batch, ADKSampler.jl:168-296).
+// FP32 copies read by the bulk path's sampler (CD = C * D).
+struct FBatch {
+    float Fx, Fy, dFx, dFy, F, sphi, cphi, c_cc, W;
+    float ny0, ny1, nz0, nz1;
+    float CD[2 * 9];
+};
+
 struct DBatch {
     double tr, Fx, Fy, dFx, dFy, F, sphi, cphi, c_cc, W;
     double ny0, ny1, nz0, nz1;
     double D[2 * 9];  // D^l_{m' m}, m' = -l..l, interleaved (re, im)
+    FBatch f;
 };
 
 constexpr int kMaxL = 4;
@@ -55,6 +65,7 @@ struct DJob {
     double cutoff, dkdt, mc_kd_max, mc_kz_max;
     uint64_t seed;
     double Plm[2 * (2 * kMaxL + 1)];
+    float fPlm[2 * (2 * kMaxL + 1)];  // FP32 copy for the bulk path's sampler
     // integration
     double rtol, t_final;
     // collection
@@ -98,6 +109,12 @@ int launch_batch_prepare(const DJob& J, const double* t, DBatch* batches, cudaSt
 int launch_sample_range(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
                         const DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
                         cudaStream_t s);
+// FP32 variant of the same kernel for the bulk path (sampler_fp32.cu); used
+// when the rate cutoff keeps every kept rate in FP32's normal range.
+int launch_sample32_range(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
+                          const DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
+                          cudaStream_t s);
+constexpr double kSample32MinCutoff = 1e-30;
 // Order-preserving compaction: idx[k] = k-th i with flag[i] != 0; *count = total.
 int launch_compact(const uint8_t* flag, int64_t n, int64_t* idx, uint32_t* block_sums,
                    int64_t nblocks_cap, unsigned long long* count, cudaStream_t s);
@@ -125,6 +142,10 @@ struct BulkParams {
     float Z, Ip, sc, a1, b1, a2, b2, a3, b3, a2b2;
 };
 int launch_field_table(const DJob& J, double T0, double h, int n_int, float4* tab, cudaStream_t s);
+// FP32 collection of the bulk integrator's final states.
+int launch_collect_bulk(const DJob& J, InitSoA soa, const double* t, const int64_t* idx,
+                        const unsigned long long* count, TrajOut out, int64_t max_n, int sm_count,
+                        cudaStream_t s);
 int launch_integrate_bulk(const BulkParams& P, InitSoA soa, const double* t, const int64_t* idx,
                           const unsigned long long* count, unsigned long long* queue, TrajOut out,
                           int sm_count, cudaStream_t s);

@@ -20,6 +20,13 @@
 //    momentum derivatives: algebraically the same Tsit5 step, but the
 //    position error estimate dt^2 (b~ A) . K no longer cancels large stage
 //    momenta, which in FP32 put a noise floor of ~3e-5 under EEst.
+//  * Noise-aware error estimate.  Each FP32 stage value carries ~1 ulp of
+//    the magnitude of the terms summed into it; the error sums cancel those
+//    values to ~dt^5, so the estimate is taken less a bound on that noise
+//    (2 ulp x the sum of |weights|).  Without it, EEst would not fall below
+//    ~1e-5 and a trajectory starting with a tiny step would grow it by ~2x per
+//    step instead of 10x: 15-20% more steps than the FP64 path for the same
+//    tolerance.  Near EEst ~ 1 the bound is ~1e-5 of the tolerance.
 //  * Compensated state.  Positions, momenta and the QTMC/SCTS phase are
 //    double-float pairs (hi + lo, Knuth's TwoSum), so 1e3 steps add no
 //    rounding drift; stage values and the error estimate are plain FP32.
@@ -28,9 +35,9 @@
 //    step counts that differ 100x between trajectories do not idle the warp.
 //    `refill_min` lanes must be free before a warp refills (autotuned).
 //
-// The kernel writes the final state in FP64 (hi + lo); the Kepler asymptote,
-// SCTS correction and deposit contribution are then computed in FP64 by the
-// collection kernel of integrate_fp64.cu, exactly as on the plain path.
+// The kernel writes the final state in FP64 (hi + lo); k_collect_bulk then
+// computes the Kepler asymptote, SCTS correction and deposit contribution of
+// every electron in FP32 (the phase sum and its reduction in FP64).
 //
 // Roofline: FP32 issue bound, MUFU for rsqrt/exp2/log2; no tensor cores.
 
@@ -63,6 +70,20 @@ constexpr double bta(int l) {
     for (int i = 0; i < 7; ++i) s += kBT[i] * kA[i][l];
     return s;
 }
+constexpr double cabs_(double x) { return x < 0 ? -x : x; }
+constexpr double sum_abs_bt() {
+    double s = 0.0;
+    for (int l = 0; l < 7; ++l) s += cabs_(kBT[l]);
+    return s;
+}
+constexpr double sum_abs_bta() {
+    double s = 0.0;
+    for (int l = 0; l < 7; ++l) s += cabs_(bta(l));
+    return s;
+}
+// Rounding-noise bound of one FP32 stage value of magnitude M: 2 M 2^-24.
+constexpr float kNoiseUlp = 1.1920928955078125e-7f;
+constexpr float kSumAbsBT = (float)sum_abs_bt(), kSumAbsBTA = (float)sum_abs_bta();
 
 #define ETRAJ_ROW(f, i) {(float)f(i, 0), (float)f(i, 1), (float)f(i, 2), (float)f(i, 3), (float)f(i, 4), (float)f(i, 5), (float)f(i, 6)}
 #define ETRAJ_A(i, l) kA[i][l]
@@ -78,7 +99,7 @@ __constant__ float cBT[7] = {(float)kBT[0], (float)kBT[1], (float)kBT[2], (float
 __constant__ float cBTA[7] = {(float)bta(0), (float)bta(1), (float)bta(2), (float)bta(3), (float)bta(4), (float)bta(5), (float)bta(6)};
 
 constexpr float ABSTOL = 1e-6f, BETA1 = 0.14f, BETA2 = 0.08f, QMIN_INV = 5.0f, QMAX_INV = 0.1f,
-                GAMMA = 0.9f, QOLDINIT = 1e-4f;
+                INV_GAMMA = 1.0f / 0.9f, LOG2_QOLDINIT = -13.287712379549449f;  // log2(1e-4)
 constexpr int MAXITERS = 1000000;
 constexpr float kDthMin = 2.4e-7f;  // smallest step (in table intervals) the FP32 clock resolves
 
@@ -112,9 +133,13 @@ __device__ __forceinline__ void field(const float4* __restrict__ tab, int n_int,
 
 // Momentum derivatives K = F_target(X) - F_laser(t) and the phase rate
 // (HydrogenLikeAtom.jl:78-159, SAEAtom.jl:278-366); x . F_target = coef r^2.
+// mK and mph are the magnitudes of the terms summed into K and the phase rate
+// (for the rounding-noise bound of the error estimate; unused outputs of the
+// inlined call are removed by the compiler).
 template <int DIM, int PHASE, int TGT>
 __device__ __forceinline__ void accel(const BulkParams& P, const float4* __restrict__ tab, int ni, float fi,
-                                      const float* X, const float* Pm, float* K, float& kph) {
+                                      const float* X, const float* Pm, float* K, float& kph, float& mK,
+                                      float& mph) {
     float Fx, Fy;
     field(tab, P.n_int, ni, fi, Fx, Fy);
     const float r2 = (DIM == 3) ? fmaf(X[0], X[0], fmaf(X[1], X[1], X[2] * X[2])) : fmaf(X[0], X[0], X[1] * X[1]);
@@ -138,20 +163,33 @@ __device__ __forceinline__ void accel(const BulkParams& P, const float4* __restr
     K[0] = fmaf(coef, X[0], -Fx);
     K[1] = fmaf(coef, X[1], -Fy);
     if (DIM == 3) K[2] = coef * X[2];
+    const float ax = fmaxf(fabsf(X[0]), fabsf(X[1]));
+    mK = fmaf(fabsf(coef), (DIM == 3) ? fmaxf(ax, fabsf(X[2])) : ax, fmaxf(fabsf(Fx), fabsf(Fy)));
     if (PHASE != ETRAJ_PHASE_CTMC) {
         const float KE = 0.5f * ((DIM == 3) ? fmaf(Pm[0], Pm[0], fmaf(Pm[1], Pm[1], Pm[2] * Pm[2]))
                                             : fmaf(Pm[0], Pm[0], Pm[1] * Pm[1]));
         kph = (PHASE == ETRAJ_PHASE_QTMC) ? -((P.Ip + KE) - V) : -((KE - V) + coef * r2);
+        mph = (P.Ip + KE) + fabsf(V) + ((PHASE == ETRAJ_PHASE_SCTS) ? fabsf(coef * r2) : 0.0f);
     } else {
         kph = 0.0f;
+        mph = 0.0f;
     }
 }
 
+// Fixed-point clock: t = T0 + h (n + f), 0 <= f < 1.  Adding kMagic = 1.5 * 2^23
+// with round-down leaves floor(g) in the low mantissa bits for 0 <= g < 2^22
+// (the host keeps every job below 2^21 intervals), so the split costs two FP32
+// adds and an integer subtract instead of floor and float-int conversions.
+constexpr float kMagic = 12582912.0f;
 __device__ __forceinline__ void advance(int n, float f, float dth, int& no, float& fo) {
-    float g = f + dth;
-    float fl = floorf(g);
-    no = n + (int)fl;
-    fo = g - fl;
+    const float g = f + dth;
+    const float r = __fadd_rd(g, kMagic);
+    no = n + (__float_as_int(r) - __float_as_int(kMagic));
+    fo = g - (r - kMagic);  // exact: g and floor(g) are within a factor of 2, or floor(g) = 0
+}
+// (float)k for 0 <= k < 2^22, without a conversion instruction
+__device__ __forceinline__ float small_int_to_float(int k) {
+    return __int_as_float(__float_as_int(kMagic) + k) - kMagic;
 }
 
 template <int DIM, int PHASE, int TGT>
@@ -176,8 +214,9 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
     // state (hi, lo): x[DIM], p[DIM], phase
     float xh[DIM], xl[DIM], ph[DIM], pl[DIM], fh = 0.0f, flo = 0.0f;
     float K1[DIM], kph1 = 0.0f;  // FSAL derivatives
+    float mK1 = 0.0f, mph1 = 0.0f;  // and their term magnitudes
     int tn = 0, iter = 0, attempts = 0;
-    float tfr = 0.0f, dth = 0.0f, dthp = 0.0f, dthmax = 0.0f, qold = QOLDINIT, q11 = 1.0f;
+    float tfr = 0.0f, dth = 0.0f, dthp = 0.0f, dthmax = 0.0f, lqold = LOG2_QOLDINIT, q11 = 1.0f;
     bool accept = false, active = false, need = true;
     unsigned long long s = 0;
 
@@ -221,7 +260,7 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
                     tn = (int)fl;
                     tfr = (float)(q0 - fl);
                     dthmax = (float)((P.t_final - t0) * P.inv_h_d);
-                    accel<DIM, PHASE, TGT>(P, tab, tn, tfr, xh, ph, K1, kph1);
+                    accel<DIM, PHASE, TGT>(P, tab, tn, tfr, xh, ph, K1, kph1, mK1, mph1);
                     // d0 = |u0/sk|, d1 = |f0/sk| (f0 = (p, K, phase rate))
                     float skx[DIM], skp[DIM], skf = 0.0f, a0 = 0.0f, a1 = 0.0f;
 #pragma unroll
@@ -253,7 +292,8 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
                     int n1;
                     float f1r;
                     advance(tn, tfr, dt0 * P.inv_h, n1, f1r);
-                    accel<DIM, PHASE, TGT>(P, tab, n1, f1r, X1, P1, K1b, kph1b);
+                    float unused_m, unused_p;
+                    accel<DIM, PHASE, TGT>(P, tab, n1, f1r, X1, P1, K1b, kph1b, unused_m, unused_p);
                     float a2 = 0.0f;
 #pragma unroll
                     for (int d = 0; d < DIM; ++d) {
@@ -270,7 +310,7 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
                                                      : exp2f(-(2.0f + log10f(md)) * (3.321928094887362f / 5.0f));
                     dth = fminf(fminf(100.0f * dt0, dt1), dthmax * P.h) * P.inv_h;
                     dthp = dth;
-                    qold = QOLDINIT;
+                    lqold = LOG2_QOLDINIT;
                     q11 = 1.0f;
                     accept = false;
                     iter = 0;
@@ -284,12 +324,12 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
             // ---- one Tsit5 step attempt (lanes without work idle; every lane returns to
             //      the ballots above, so the *_sync calls always see the full warp) -----------
             if (iter > 0) {
-                if (!accept) dth = dth / fminf(QMIN_INV, q11 / GAMMA);
+                if (!accept) dth = __fdividef(dth, fminf(QMIN_INV, q11 * INV_GAMMA));
                 else dth = dthp;
             }
             ++iter;
             dth = fminf(dth, dthmax);
-            const float remaining = (float)(P.nf - tn) + (P.ff - tfr);
+            const float remaining = small_int_to_float(P.nf - tn) + (P.ff - tfr);
             const bool last = dth >= remaining;
             if (last) dth = remaining;
             int status = 0;
@@ -298,7 +338,7 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
             else if (dth < kDthMin && !last) status = 2;
             if (status == 0) {
                 const float dt = dth * P.h, dt2 = dt * dt;
-                float K[7][DIM], kph[7], X[DIM], Pm[DIM];
+                float K[7][DIM], kph[7], X[DIM], Pm[DIM], mK7 = 0.0f, mph7 = 0.0f;
                 int n1 = 0;
                 float f1 = 0.0f;
                 if (last) {
@@ -326,7 +366,7 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
                     int ni = n1;
                     float fi = f1;
                     if (st < 5) advance(tn, tfr, cC[st] * dth, ni, fi);
-                    accel<DIM, PHASE, TGT>(P, tab, ni, fi, X, Pm, K[st], kph[st]);
+                    accel<DIM, PHASE, TGT>(P, tab, ni, fi, X, Pm, K[st], kph[st], mK7, mph7);
                 }
                 // X, Pm now hold the new position and momentum (stage 7 = solution)
                 float incf = 0.0f, phnew = 0.0f;
@@ -337,6 +377,13 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
                     incf = dt * a;
                     phnew = fh + incf;
                 }
+                // Error estimate less its own FP32 rounding noise: the weighted sums
+                // below cancel to ~dt^5 while each stage value carries ~1 ulp of the
+                // magnitude of its terms, which would otherwise put a floor of
+                // ~1e-5 under EEst and hold the step growth of well-resolved
+                // trajectories to ~2x per step instead of the controller's 10x.
+                const float mk = fmaxf(mK1, mK7) * kNoiseUlp;
+                const float nx = dt2 * kSumAbsBTA * mk, np = dt * kSumAbsBT * mk;
                 float acc = 0.0f;
 #pragma unroll
                 for (int d = 0; d < DIM; ++d) {
@@ -348,7 +395,8 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
                     }
                     const float scx = fmaf(fmaxf(fabsf(xh[d]), fabsf(X[d])), P.rtol, ABSTOL);
                     const float scp = fmaf(fmaxf(fabsf(ph[d]), fabsf(Pm[d])), P.rtol, ABSTOL);
-                    const float rx = (dt2 * ex) / scx, rp = (dt * ep) / scp;
+                    const float rx = __fdividef(fmaxf(fabsf(dt2 * ex) - nx, 0.0f), scx);
+                    const float rp = __fdividef(fmaxf(fabsf(dt * ep) - np, 0.0f), scp);
                     acc = fmaf(rx, rx, fmaf(rp, rp, acc));
                 }
                 if (HASPH) {
@@ -356,24 +404,27 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
 #pragma unroll
                     for (int l = 0; l < 7; ++l) ef = fmaf(cBT[l], kph[l], ef);
                     const float scf = fmaf(fmaxf(fabsf(fh), fabsf(phnew)), P.rtol, ABSTOL);
-                    const float rf = (dt * ef) / scf;
+                    const float nf = dt * kSumAbsBT * (fmaxf(mph1, mph7) * kNoiseUlp);
+                    const float rf = __fdividef(fmaxf(fabsf(dt * ef) - nf, 0.0f), scf);
                     acc = fmaf(rf, rf, acc);
                 }
-                const float EEst = sqrtf(acc * (1.0f / N));
+                // EEst^2 and half its log2: the controller needs only powers of EEst
+                const float ms = acc * (1.0f / N);
+                const float lh = 0.5f * __log2f(ms);  // log2 EEst
                 ++attempts;
                 float q;
-                if (EEst == 0.0f) {
+                if (ms == 0.0f) {
                     q = QMAX_INV;
                 } else {
-                    q11 = exp2f(BETA1 * __log2f(EEst));
-                    q = q11 * exp2f(-BETA2 * __log2f(qold));
-                    q = fmaxf(QMAX_INV, fminf(QMIN_INV, q / GAMMA));
+                    q11 = exp2f(BETA1 * lh);
+                    q = q11 * exp2f(-BETA2 * lqold);
+                    q = fmaxf(QMAX_INV, fminf(QMIN_INV, q * INV_GAMMA));
                 }
-                accept = (EEst <= 1.0f);
-                if (!(EEst == EEst)) status = 4;
+                accept = (ms <= 1.0f);
+                if (!(ms == ms)) status = 4;
                 if (accept && status == 0) {
-                    qold = fmaxf(EEst, QOLDINIT);
-                    dthp = fminf(dthmax, dth / q);
+                    lqold = fmaxf(lh, LOG2_QOLDINIT);
+                    dthp = fminf(dthmax, __fdividef(dth, q));
 #pragma unroll
                     for (int d = 0; d < DIM; ++d) {
                         float a = 0.0f, b = 0.0f;
@@ -388,6 +439,8 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
                     }
                     if (HASPH) df_add(fh, flo, incf);
                     kph1 = kph[6];
+                    mK1 = mK7;
+                    mph1 = mph7;
                     tn = n1;
                     tfr = f1;
                     if (last) {
@@ -416,6 +469,128 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
                 need = true;
             }
         }  // active
+    }
+}
+
+// FP32 collection of the bulk path's final states (TrajectorySimulation.jl:356-393,
+// 3D :451-493): the same Kepler asymptote, SCTS phase correction, binning and
+// contributions as collect() in integrate_fp64.cu, in FP32 except for the phase
+// sum and its reduction mod 2 pi (FP64, a few operations per electron), so the
+// absolute phase error stays ~1e-6 rad for phases of 1e3 rad.  A separate
+// kernel rather than an epilogue of k_integrate_bulk: there, each finishing
+// lane would stall its warp for the whole collection.
+template <int DIM, int PHASE>
+__global__ void __launch_bounds__(256)
+k_collect_bulk(const __grid_constant__ DJob J, InitSoA soa, const double* __restrict__ tsamp,
+               const int64_t* __restrict__ idx, const unsigned long long* __restrict__ count,
+               TrajOut out) {
+    constexpr int N = 2 * DIM + (PHASE != ETRAJ_PHASE_CTMC ? 1 : 0);
+    const int64_t n = (int64_t)(*count);
+    const float Z = (float)J.target.Z, sc = (float)J.target.sc;
+    for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        const int st = out.status[s] & 0xff;
+        const int64_t g = idx ? idx[s] : s;
+        const double prob = soa.rate[g];
+        uint32_t key = (uint32_t)J.grid;
+        double cre = 0.0, cim = 0.0, wion = 0.0, wunc = 0.0;
+        float pin[3] = {0.0f, 0.0f, 0.0f};
+        bool ionized = false;
+        if (st == 0) {
+            const double* f = out.final_state + s * N;
+            float rv[3], pv[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                rv[d] = (d < DIM) ? (float)f[d] : 0.0f;
+                pv[d] = (d < DIM) ? (float)f[DIM + d] : 0.0f;
+            }
+            const float r2 = fmaf(rv[0], rv[0], fmaf(rv[1], rv[1], rv[2] * rv[2]));
+            const float K = 0.5f * fmaf(pv[0], pv[0], fmaf(pv[1], pv[1], pv[2] * pv[2]));
+            float V;
+            if (J.target.kind == ETRAJ_TARGET_HYDROGEN_LIKE) {
+                V = -Z * rsqrt_nr(r2 + sc);
+            } else {
+                const DTarget& T = J.target;
+                const float r = sqrtf(r2);
+                const float num = fmaf((float)T.a3, __expf(-(float)T.b3 * r),
+                                       fmaf((float)T.a2 * r, __expf(-(float)T.b2 * r),
+                                            fmaf((float)T.a1, __expf(-(float)T.b1 * r), Z)));
+                V = -num * rsqrt_nr(r2 + sc);
+            }
+            const float E = K + V;
+            const float L[3] = {rv[1] * pv[2] - rv[2] * pv[1], rv[2] * pv[0] - rv[0] * pv[2],
+                                rv[0] * pv[1] - rv[1] * pv[0]};
+            const float L2 = fmaf(L[0], L[0], fmaf(L[1], L[1], L[2] * L[2]));
+            double phase = 0.0;
+            if (PHASE != ETRAJ_PHASE_CTMC) phase = f[N - 1];
+            if (PHASE == ETRAJ_PHASE_SCTS && E > 0.0f) {
+                const float sqrtb = rsqrtf(2.0f * E);
+                const float gg = sqrtf(fmaf(2.0f * E, L2, 1.0f));
+                // the 3D reference uses x*py where x*px is meant (TrajectorySimulation.jl:463)
+                const float rp = (DIM == 2) ? fmaf(rv[0], pv[0], rv[1] * pv[1])
+                                            : fmaf(rv[0], pv[1], fmaf(rv[1], pv[1], rv[2] * pv[2]));
+                const float corr = (Z * sqrtb) * (logf(gg) + asinhf(rp / (gg * sqrtb)));
+                phase = (phase + J.target.Ip * tsamp[soa.batch[g]]) - (double)corr;
+            }
+            if (E >= 0.0f) {
+                ionized = true;
+                wion = prob;
+                const float pinf = sqrtf(2.0f * E);
+                const float inr = rsqrt_nr(fmaxf(r2, 1e-30f));
+                const float pL[3] = {pv[1] * L[2] - pv[2] * L[1], pv[2] * L[0] - pv[0] * L[2],
+                                     pv[0] * L[1] - pv[1] * L[0]};
+                float a[3];
+#pragma unroll
+                for (int i = 0; i < 3; ++i) a[i] = pL[i] - Z * rv[i] * inr;
+                const float La[3] = {L[1] * a[2] - L[2] * a[1], L[2] * a[0] - L[0] * a[2],
+                                     L[0] * a[1] - L[1] * a[0]};
+                const float fac = pinf / fmaf(pinf * pinf, L2, 1.0f);
+#pragma unroll
+                for (int i = 0; i < 3; ++i) pin[i] = fac * fmaf(pinf, La[i], -a[i]);
+                int64_t lin = 0, stride = 1;
+                bool ok = true;
+#pragma unroll
+                for (int d = 0; d < DIM; ++d) {
+                    const int64_t num = J.pnum[d];
+                    int64_t ix = 1;
+                    if (num > 1) {
+                        const float v = rintf((pin[d] + (float)J.pmax[d]) / (float)J.binw[d]);
+                        if (!(v >= 1.0f && v <= (float)num)) ok = false;
+                        else ix = (int64_t)v;
+                    }
+                    lin += (ix - 1) * stride;
+                    stride *= num;
+                }
+                if (ok) {
+                    key = (uint32_t)lin;
+                    if (PHASE == ETRAJ_PHASE_CTMC) {
+                        cre = prob;
+                    } else {
+                        // reduce mod 2 pi in FP64 (2 pi split in two parts), then FP32 sincos
+                        const double kq = rint(phase * 0.15915494309189535);
+                        const double red = fma(-kq, 1.2246467991473532e-16, fma(-kq, 6.283185307179586, phase));
+                        float sn, cs;
+                        sincosf((float)red, &sn, &cs);
+                        const float sp = sqrtf((float)prob);
+                        cre = (double)(sp * cs);
+                        cim = (double)(sp * sn);
+                    }
+                } else {
+                    wunc = prob;
+                }
+            }
+        }
+        out.key[s] = key;
+        out.c_re[s] = cre;
+        out.c_im[s] = cim;
+        out.w_ion[s] = wion;
+        out.w_unc[s] = wunc;
+        if (out.p_inf) {
+            out.p_inf[3 * s] = pin[0];
+            out.p_inf[3 * s + 1] = pin[1];
+            out.p_inf[3 * s + 2] = pin[2];
+        }
+        out.status[s] = st | (ionized ? 0x100 : 0);
     }
 }
 
@@ -449,6 +624,27 @@ int launch_bulk_t(const BulkParams& P, InitSoA soa, const double* t, const int64
 }
 
 }  // namespace
+
+int launch_collect_bulk(const DJob& J, InitSoA soa, const double* t, const int64_t* idx,
+                        const unsigned long long* count, TrajOut out, int64_t max_n, int sm_count,
+                        cudaStream_t s) {
+    const int threads = 256;
+    const int64_t want = (max_n + threads - 1) / threads;
+    const int64_t cap = (int64_t)sm_count * 8;
+    const int blocks = (int)(want < cap ? (want > 0 ? want : 1) : cap);
+#define ETRAJ_COLLECT(D, P) k_collect_bulk<D, P><<<blocks, threads, 0, s>>>(J, soa, t, idx, count, out)
+    if (J.dim == 2) {
+        if (J.phase == ETRAJ_PHASE_CTMC) ETRAJ_COLLECT(2, ETRAJ_PHASE_CTMC);
+        else if (J.phase == ETRAJ_PHASE_QTMC) ETRAJ_COLLECT(2, ETRAJ_PHASE_QTMC);
+        else ETRAJ_COLLECT(2, ETRAJ_PHASE_SCTS);
+    } else {
+        if (J.phase == ETRAJ_PHASE_CTMC) ETRAJ_COLLECT(3, ETRAJ_PHASE_CTMC);
+        else if (J.phase == ETRAJ_PHASE_QTMC) ETRAJ_COLLECT(3, ETRAJ_PHASE_QTMC);
+        else ETRAJ_COLLECT(3, ETRAJ_PHASE_SCTS);
+    }
+#undef ETRAJ_COLLECT
+    return 1;
+}
 
 int launch_field_table(const DJob& J, double T0, double h, int n_int, float4* tab, cudaStream_t s) {
     k_field_table<<<(n_int + 127) / 128, 128, 0, s>>>(J, T0, h, n_int, tab);

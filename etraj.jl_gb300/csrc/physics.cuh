@@ -153,6 +153,16 @@ __host__ __device__ __forceinline__ void laser_F_dual(const DLaser& L, double t,
 }
 
 // ---- targets -----------------------------------------------------------------------
+// exp(-b r) of the SAE potential.  For targets that pass etraj_sae_skip_exact
+// (sae_skip.h, checked on the host), every term this factor enters when
+// b r > 60 is too small to change the sum it is added to, so returning 0
+// leaves every result bit-identical and saves the evaluation at large r,
+// where trajectories spend most of their steps.
+__host__ __device__ __forceinline__ double sae_exp(const DTarget& T, double b, double r) {
+    if (T.skip_ok && b * r > 60.0) return 0.0;
+    return dm_exp(-b * r);
+}
+
 // TargetPotential (HydrogenLikeAtom.jl:75, SAEAtom.jl:264-269)
 __host__ __device__ __forceinline__ double target_V(const DTarget& T, double x, double y, double z) {
     if (T.kind == ETRAJ_TARGET_HYDROGEN_LIKE) {
@@ -160,8 +170,8 @@ __host__ __device__ __forceinline__ double target_V(const DTarget& T, double x, 
         return (-T.Z) * (1.0 / sqrt(s));
     }
     double r = sqrt((x * x + y * y) + z * z);
-    double num = ((T.Z + T.a1 * dm_exp(-T.b1 * r)) + (T.a2 * r) * dm_exp(-T.b2 * r)) +
-                 T.a3 * dm_exp(-T.b3 * r);
+    double num = ((T.Z + T.a1 * sae_exp(T, T.b1, r)) + (T.a2 * r) * sae_exp(T, T.b2, r)) +
+                 T.a3 * sae_exp(T, T.b3, r);
     return -num / sqrt(r * r + T.sc);
 }
 
@@ -185,7 +195,7 @@ __host__ __device__ __forceinline__ void rhs(const DJob& J, double t, const doub
         } else {
             double r = sqrt(x * x + y * y);
             double s = r * r + T.sc, rs = sqrt(s);
-            double e1 = dm_exp(-T.b1 * r), e2 = dm_exp(-T.b2 * r), e3 = dm_exp(-T.b3 * r);
+            double e1 = sae_exp(T, T.b1, r), e2 = sae_exp(T, T.b2, r), e3 = sae_exp(T, T.b3, r);
             double br = (T.Z + (T.a1 * (1.0 + T.b1 * r)) * e1) + (T.a3 * (1.0 + T.b3 * r)) * e3;
             double coef = -((1.0 / (s * rs)) * br + ((T.a2 * T.b2) / rs) * e2);
             tFx = x * coef;
@@ -218,7 +228,7 @@ __host__ __device__ __forceinline__ void rhs(const DJob& J, double t, const doub
         } else {
             double r = sqrt((x * x + y * y) + z * z);
             double s = r * r + T.sc, rs = sqrt(s);
-            double e1 = dm_exp(-T.b1 * r), e2 = dm_exp(-T.b2 * r), e3 = dm_exp(-T.b3 * r);
+            double e1 = sae_exp(T, T.b1, r), e2 = sae_exp(T, T.b2, r), e3 = sae_exp(T, T.b3, r);
             double br = (T.Z + (T.a1 * (1.0 + T.b1 * r)) * e1) + (T.a3 * (1.0 + T.b3 * r)) * e3;
             double coef = -((1.0 / (s * rs)) * br + ((T.a2 * T.b2) / rs) * e2);
             tFx = x * coef;

@@ -130,6 +130,20 @@ __global__ void k_batch_prepare(const __grid_constant__ DJob J, const double* __
         B.D[2 * (mp + J.l)] = D.re;
         B.D[2 * (mp + J.l) + 1] = D.im;
     }
+    B.f.Fx = (float)B.Fx;
+    B.f.Fy = (float)B.Fy;
+    B.f.dFx = (float)B.dFx;
+    B.f.dFy = (float)B.dFy;
+    B.f.F = (float)B.F;
+    B.f.sphi = (float)B.sphi;
+    B.f.cphi = (float)B.cphi;
+    B.f.c_cc = (float)B.c_cc;
+    B.f.W = (float)B.W;
+    B.f.ny0 = (float)B.ny0;
+    B.f.ny1 = (float)B.ny1;
+    B.f.nz0 = (float)B.nz0;
+    B.f.nz1 = (float)B.nz1;
+    for (int i = 0; i < 2 * 9; ++i) B.f.CD[i] = (i < 2 * (2 * J.l + 1)) ? (float)(J.C * B.D[i]) : 0.0f;
     out[b] = B;
 }
 
@@ -362,7 +376,7 @@ k_compact_scatter(const uint8_t* __restrict__ flag, int64_t n, const uint32_t* _
 }  // namespace
 
 int launch_batch_prepare(const DJob& J, const double* t, DBatch* batches, cudaStream_t s) {
-    int threads = 128;
+    int threads = 64;  // few, FP64-heavy threads: spread them over every SM
     int blocks = (int)((J.n_t + threads - 1) / threads);
     k_batch_prepare<<<blocks, threads, 0, s>>>(J, t, batches);
     return 1;

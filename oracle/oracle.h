@@ -62,6 +62,10 @@ void oracle_laser_eval_complex(const etraj_laser* laser, int64_t n, const double
 void oracle_target_eval(const etraj_target* target, int64_t n, const double* xyz, double* V,
                         double* F);
 double oracle_hartree_asymp_coeff(int Z, double Ip, int l);
+/* exp(-b r) skip of the SAE terms: the per-target exactness check and a
+ * process-wide switch (default on) used to show the skip changes nothing */
+int oracle_sae_skip_exact(const etraj_target* target);
+void oracle_set_sae_skip(int enable);
 void oracle_rhs(const etraj_job* job, double t, const double* u, double* du);
 void oracle_detmath(int fn, int64_t n, const double* x, const double* y, double* out);
 void oracle_tsit5_tableau(double* c, double* a, double* btilde);

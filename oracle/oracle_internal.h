@@ -9,6 +9,7 @@
 #include <math.h>
 #include "oracle.h"
 #include "../etraj.jl_gb300/csrc/detmath.h"
+#include "../etraj.jl_gb300/csrc/sae_skip.h"
 
 typedef struct {
     int kind;
@@ -27,8 +28,18 @@ typedef struct {
 
 typedef struct {
     int kind;
+    int skip_ok; /* exp(-b r) terms with b r > 60 may be dropped exactly (o_sae_exp) */
     double Z, Ip, sc, a1, b1, a2, b2, a3, b3;
 } o_target;
+
+/* exp(-b r) of the SAE potential.  For targets that pass
+ * etraj_sae_skip_exact, every term this factor enters when b r > 60 is too
+ * small to change the sum it is added to, so returning 0 leaves every result
+ * bit-identical and saves the evaluation. */
+static inline double o_sae_exp(const o_target* T, double b, double r) {
+    if (T->skip_ok && b * r > 60.0) return 0.0;
+    return dm_exp(-b * r);
+}
 
 typedef struct {
     int dim, phase, n;  /* n = ODE state size */

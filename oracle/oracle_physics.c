@@ -282,6 +282,14 @@ void o_laser_AF_complex(const o_laser* L, dm_cplx t, dm_cplx* Ax, dm_cplx* Ay, d
 
 /* ---- targets ---------------------------------------------------------------- */
 
+/* 0 disables the exp(-b r) skip everywhere (tests compare both settings) */
+static int g_sae_skip = 1;
+void oracle_set_sae_skip(int enable) { g_sae_skip = enable; }
+int oracle_sae_skip_exact(const etraj_target* in) {
+    double a[3] = {in->a1, in->a2, in->a3}, b[3] = {in->b1, in->b2, in->b3};
+    return etraj_sae_skip_exact((double)in->Z, a, b, in->soft_core);
+}
+
 void o_target_prepare(const etraj_target* in, o_target* T) {
     memset(T, 0, sizeof *T);
     T->kind = in->kind;
@@ -291,6 +299,10 @@ void o_target_prepare(const etraj_target* in, o_target* T) {
     T->a1 = in->a1; T->b1 = in->b1;
     T->a2 = in->a2; T->b2 = in->b2;
     T->a3 = in->a3; T->b3 = in->b3;
+    {
+        double a[3] = {in->a1, in->a2, in->a3}, b[3] = {in->b1, in->b2, in->b3};
+        T->skip_ok = g_sae_skip && etraj_sae_skip_exact((double)in->Z, a, b, in->soft_core);
+    }
 }
 
 /* TargetPotential (HydrogenLikeAtom.jl:75, SAEAtom.jl:264-269) */
@@ -300,8 +312,8 @@ double o_target_V(const o_target* T, double x, double y, double z) {
         return (-T->Z) * (1.0 / sqrt(s));
     }
     double r = sqrt((x * x + y * y) + z * z);
-    double num = ((T->Z + T->a1 * dm_exp(-T->b1 * r)) + (T->a2 * r) * dm_exp(-T->b2 * r)) +
-                 T->a3 * dm_exp(-T->b3 * r);
+    double num = ((T->Z + T->a1 * o_sae_exp(T, T->b1, r)) + (T->a2 * r) * o_sae_exp(T, T->b2, r)) +
+                 T->a3 * o_sae_exp(T, T->b3, r);
     return -num / sqrt(r * r + T->sc);
 }
 
@@ -315,9 +327,9 @@ void o_target_F(const o_target* T, double x, double y, double z, double* F) {
     }
     double r = sqrt((x * x + y * y) + z * z);
     double s = r * r + T->sc, rs = sqrt(s);
-    double br = (T->Z + (T->a1 * (1.0 + T->b1 * r)) * dm_exp(-T->b1 * r)) +
-                (T->a3 * (1.0 + T->b3 * r)) * dm_exp(-T->b3 * r);
-    double coef = -((1.0 / (s * rs)) * br + ((T->a2 * T->b2) / rs) * dm_exp(-T->b2 * r));
+    double br = (T->Z + (T->a1 * (1.0 + T->b1 * r)) * o_sae_exp(T, T->b1, r)) +
+                (T->a3 * (1.0 + T->b3 * r)) * o_sae_exp(T, T->b3, r);
+    double coef = -((1.0 / (s * rs)) * br + ((T->a2 * T->b2) / rs) * o_sae_exp(T, T->b2, r));
     F[0] = x * coef; F[1] = y * coef; F[2] = z * coef;
 }
 
@@ -347,7 +359,7 @@ void o_rhs(const o_sys* S, double t, const double* u, double* du) {
             double r = sqrt(x * x + y * y);
             s = r * r + T->sc;
             rs = sqrt(s);
-            double e1 = dm_exp(-T->b1 * r), e2 = dm_exp(-T->b2 * r), e3 = dm_exp(-T->b3 * r);
+            double e1 = o_sae_exp(T, T->b1, r), e2 = o_sae_exp(T, T->b2, r), e3 = o_sae_exp(T, T->b3, r);
             double br = (T->Z + (T->a1 * (1.0 + T->b1 * r)) * e1) + (T->a3 * (1.0 + T->b3 * r)) * e3;
             double coef = -((1.0 / (s * rs)) * br + ((T->a2 * T->b2) / rs) * e2);
             tFx = x * coef; tFy = y * coef;
@@ -376,7 +388,7 @@ void o_rhs(const o_sys* S, double t, const double* u, double* du) {
         } else {
             double r = sqrt((x * x + y * y) + z * z);
             double s = r * r + T->sc, rs = sqrt(s);
-            double e1 = dm_exp(-T->b1 * r), e2 = dm_exp(-T->b2 * r), e3 = dm_exp(-T->b3 * r);
+            double e1 = o_sae_exp(T, T->b1, r), e2 = o_sae_exp(T, T->b2, r), e3 = o_sae_exp(T, T->b3, r);
             double br = (T->Z + (T->a1 * (1.0 + T->b1 * r)) * e1) + (T->a3 * (1.0 + T->b3 * r)) * e3;
             double coef = -((1.0 / (s * rs)) * br + ((T->a2 * T->b2) / rs) * e2);
             tFx = x * coef; tFy = y * coef; tFz = z * coef;

@@ -47,6 +47,8 @@ def lib():
             "oracle_target_eval": (None, [C.POINTER(abi.Target), C.c_int64, _DP, _DP, _DP]),
             "oracle_hartree_asymp_coeff": (C.c_double, [C.c_int, C.c_double, C.c_int]),
             "oracle_rhs": (None, [_JP, C.c_double, _DP, _DP]),
+            "oracle_sae_skip_exact": (C.c_int, [C.c_void_p]),
+            "oracle_set_sae_skip": (None, [C.c_int]),
             "oracle_detmath": (None, [C.c_int, C.c_int64, _DP, _DP, _DP]),
             "oracle_tsit5_tableau": (None, [_DP, _DP, _DP]),
         }
@@ -177,6 +179,14 @@ def target_eval(target_c, xyz):
     F = np.zeros((n, 3))
     lib().oracle_target_eval(C.byref(target_c), n, _p(xyz), _p(V), _p(F))
     return V, F
+
+
+def sae_skip_exact(target_c):
+    return bool(lib().oracle_sae_skip_exact(C.byref(target_c)))
+
+
+def set_sae_skip(enable):
+    lib().oracle_set_sae_skip(1 if enable else 0)
 
 
 def rhs(job, t, u):

@@ -83,6 +83,17 @@ def test_validate_without_gpu():
     bad.target.l = 5
     bad.target.m = 0
     assert lib.etraj_validate(C.byref(bad), buf, 256) == abi.ERR_UNSUPPORTED
+    # the bulk integrator's FP32 clock covers at most 4096 periods (2^21 intervals of T/512)
+    T = 2 * 3.141592653589793 * 800.0 / 45.563352525
+    ok = job.copy()
+    ok.precision = abi.PRECISION_FP32_BULK
+    ok.traj_t_final = -100.0 + 4000 * T
+    assert lib.etraj_validate(C.byref(ok), buf, 256) == abi.OK
+    ok.traj_t_final = -100.0 + 4100 * T
+    assert lib.etraj_validate(C.byref(ok), buf, 256) == abi.ERR_UNSUPPORTED
+    assert b"4096" in buf.value
+    ok.precision = abi.PRECISION_FP64
+    assert lib.etraj_validate(C.byref(ok), buf, 256) == abi.OK
 
 
 def test_python_mirror_rejects_what_the_reference_rejects():
