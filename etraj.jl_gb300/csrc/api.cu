@@ -136,11 +136,8 @@ int validate_job(const etraj_job* job, std::string& err) {
         return fail("[TrajectorySimulationJob] `traj_t_final` must be greater than the last time point of `sample_t_intv`.");
     if (job->dimension != 2 && job->dimension != 3)
         return fail("[TrajectorySimulationJob] `dimension` must be either 2 or 3.");
-    if (job->init_cond_method == ETRAJ_SAMPLER_SPA) {
-        err = "[SPASampler] the SFA-SPA sampler is not built in this engine.";
-        return ETRAJ_ERR_UNSUPPORTED;
-    }
-    if (job->init_cond_method != ETRAJ_SAMPLER_ADK && job->init_cond_method != ETRAJ_SAMPLER_SPANE)
+    if (job->init_cond_method != ETRAJ_SAMPLER_ADK && job->init_cond_method != ETRAJ_SAMPLER_SPANE &&
+        job->init_cond_method != ETRAJ_SAMPLER_SPA)
         return fail("[ElectronSamplers] Undefined initial condition method.");
     if (job->traj_phase_method < 0 || job->traj_phase_method > 2)
         return fail("[ADKSampler] Undefined phase method.");
@@ -249,6 +246,8 @@ void prepare_job(const etraj_job* job, HostJob& H) {
     } else {
         J.laser.nmono = 1;
     }
+    // the SPA initial guess uses the laser's omega, or the mean of the two (SPASampler.jl:160-166)
+    J.spa_omega = (J.laser.nmono == 2) ? (J.laser.m[0].omega + J.laser.m[1].omega) / 2.0 : J.laser.m[0].omega;
     const etraj_target& T = job->target;
     J.target.kind = T.kind;
     J.target.Z = (double)T.Z;
@@ -576,7 +575,7 @@ int run_job(etraj_ctx* ctx, const etraj_job* job, etraj_result* res) {
     cudaEventRecord(ctx->ev0, s);
     cudaEventRecord(ctx->stage_ev[0], s);
     launches += launch_batch_prepare(J, P.t, P.batches, s);
-    if (job->precision == ETRAJ_PRECISION_FP32_BULK && J.cutoff >= kSample32MinCutoff)
+    if (job->precision == ETRAJ_PRECISION_FP32_BULK && J.method != ETRAJ_SAMPLER_SPA && J.cutoff >= kSample32MinCutoff)
         launches += launch_sample32_range(J, 0, J.n_t, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s);
     else
         launches += launch_sample_range(J, 0, J.n_t, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s);

@@ -205,23 +205,37 @@ __global__ void k_finalize_spec(const double* __restrict__ re, const double* __r
 }
 
 // One level of the 256-ary canonical tree over two arrays.  Level 0 reads
-// n = *count elements, level k reads ceil(n / 256^k).
-__global__ void k_tree_level(const double* __restrict__ a_in, const double* __restrict__ b_in,
-                             double* __restrict__ a_out, double* __restrict__ b_out,
-                             const unsigned long long* __restrict__ count, int level) {
+// n = *count elements, level k reads ceil(n / 256^k).  Each node is the sum of
+// its (up to) 256 children from 0.0, left to right.  One warp per node: the
+// warp stages the children in shared memory with coalesced loads, then lane 0
+// runs the sum of the first array and lane 1 that of the second, so the order
+// of every addition is the canonical one.
+constexpr int kTreeWarps = 8;
+__global__ void __launch_bounds__(32 * kTreeWarps)
+k_tree_level(const double* __restrict__ a_in, const double* __restrict__ b_in,
+             double* __restrict__ a_out, double* __restrict__ b_out,
+             const unsigned long long* __restrict__ count, int level) {
+    __shared__ double sh[kTreeWarps][2][256];
     int64_t m = (int64_t)*count;
     for (int k = 0; k < level; ++k) m = (m + 255) / 256;
     const int64_t nb = (m + 255) / 256;
-    for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nb;
-         b += (int64_t)gridDim.x * blockDim.x) {
-        double sa = 0.0, sb = 0.0;
-        const int64_t e = ((b + 1) * 256 < m) ? (b + 1) * 256 : m;
-        for (int64_t i = b * 256; i < e; ++i) {
-            sa = sa + a_in[i];
-            sb = sb + b_in[i];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int64_t node = (int64_t)blockIdx.x * kTreeWarps + warp; node < nb;
+         node += (int64_t)gridDim.x * kTreeWarps) {
+        const int64_t base = node * 256;
+        const int len = (int)((m - base) < 256 ? (m - base) : 256);
+        for (int j = lane; j < len; j += 32) {
+            sh[warp][0][j] = a_in[base + j];
+            sh[warp][1][j] = b_in[base + j];
         }
-        a_out[b] = sa;
-        b_out[b] = sb;
+        __syncwarp();
+        if (lane < 2) {
+            const double* v = sh[warp][lane];
+            double acc = 0.0;
+            for (int j = 0; j < len; ++j) acc = acc + v[j];
+            (lane == 0 ? a_out : b_out)[node] = acc;
+        }
+        __syncwarp();
     }
 }
 
@@ -355,8 +369,9 @@ int launch_deposit(const DJob& J, const TrajOut& out, const unsigned long long* 
         int level = 0;
         do {
             int64_t nbl = (m + 255) / 256;
-            int tb_blocks = (int)((nbl + 255) / 256);
-            k_tree_level<<<tb_blocks, 256, 0, s>>>(a, b, ta, tb, count, level);
+            int64_t want = (nbl + kTreeWarps - 1) / kTreeWarps;
+            int tb_blocks = (int)(want < 152 * 16 ? want : 152 * 16);
+            k_tree_level<<<tb_blocks, 32 * kTreeWarps, 0, s>>>(a, b, ta, tb, count, level);
             ++launches;
             a = ta;
             b = tb;

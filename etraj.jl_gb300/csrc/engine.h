@@ -63,6 +63,7 @@ struct DJob {
     int64_t n_t, n_kd, n_kz, n_cand, n_total;  // n_total = n_t * n_cand
     double Ip, Z, kappa, nstar, c, cc_base, e_pre, C, q_theta, q_phi;
     double cutoff, dkdt, mc_kd_max, mc_kz_max;
+    double spa_omega;  // SPA initial guess' angular frequency (SPASampler.jl:160-166)
     uint64_t seed;
     double Plm[2 * (2 * kMaxL + 1)];
     float fPlm[2 * (2 * kMaxL + 1)];  // FP32 copy for the bulk path's sampler

@@ -76,6 +76,107 @@ __host__ __device__ __forceinline__ double mono_env(const DMono& L, double t) {
     return (env * w1) * w2;
 }
 
+// LaserAx / LaserAy (Cos4Laser.jl:97-124, GaussianLaser.jl:105-132).
+__host__ __device__ __forceinline__ void mono_A(const DMono& L, double t, double& Ax, double& Ay) {
+    double tt = t - L.t_shift;
+    double sth, cth, pre;
+    dm_sincos(L.omega * tt + L.cep, &sth, &cth);
+    if (L.kind == ETRAJ_LASER_GAUSSIAN) {
+        pre = L.A0 * dm_exp(-(tt * tt) * L.inv_2s2);
+    } else {
+        double s, c, w1, w2;
+        dm_sincos(tt * L.w2n, &s, &c);
+        window(L, tt, w1, w2);
+        double env = (L.kind == ETRAJ_LASER_COS4) ? (c * c) * (c * c) : c * c;
+        pre = ((L.A0 * env) * w1) * w2;
+    }
+    if (L.azi_zero) {
+        Ax = pre * cth;
+        Ay = (pre * sth) * L.ellip;
+    } else {
+        double se = sth * L.ellip;
+        Ax = pre * (cth * L.cphi + se * L.sphi);
+        Ay = pre * (cth * (-L.sphi) + se * L.cphi);
+    }
+}
+
+__host__ __device__ __forceinline__ void laser_A(const DLaser& L, double t, double& Ax, double& Ay) {
+    mono_A(L.m[0], t, Ax, Ay);
+    if (L.nmono == 2) {
+        double ax2, ay2;
+        mono_A(L.m[1], t - L.delay, ax2, ay2);
+        Ax = Ax + ax2;
+        Ay = Ay + ay2;
+    }
+}
+
+// A and (optionally) F at complex time t_r + i t_i, as SPASampler.jl evaluates
+// them; the tanh windows take real(t) (Cos4Laser.jl:93).
+__host__ __device__ __forceinline__ void mono_AF_complex(const DMono& L, dm_cplx t, dm_cplx& Ax, dm_cplx& Ay,
+                                                         dm_cplx* Fx, dm_cplx* Fy) {
+    const dm_cplx tt = dm_c(t.re - L.t_shift, t.im);
+    const dm_cplx th = dm_caddr(dm_cscale(tt, L.omega), L.cep);
+    const dm_cplx sth = dm_csin(th), cth = dm_ccos(th);
+    dm_cplx preA, preF, cx, cy;
+    if (L.kind == ETRAJ_LASER_GAUSSIAN) {
+        const dm_cplx g = dm_cexp(dm_cscale(dm_cneg(dm_cmul(tt, tt)), L.inv_2s2));
+        const dm_cplx a = dm_cscale(tt, L.inv_s2);
+        preA = dm_cscale(g, L.A0);
+        preF = preA;
+        cx = dm_cadd(dm_cmul(a, cth), dm_cscale(sth, L.omega));
+        cy = dm_csub(dm_cmul(a, sth), dm_cscale(cth, L.omega));
+    } else {
+        double w1, w2;
+        const dm_cplx u = dm_cscale(tt, L.w2n);
+        const dm_cplx s = dm_csin(u), c = dm_ccos(u);
+        window(L, tt.re, w1, w2);
+        const dm_cplx c2 = dm_cmul(c, c);
+        const dm_cplx envA = (L.kind == ETRAJ_LASER_COS4) ? dm_cmul(c2, c2) : c2;
+        const dm_cplx envF = (L.kind == ETRAJ_LASER_COS4) ? dm_cmul(c2, c) : c;
+        preA = dm_cscale(dm_cscale(dm_cscale(envA, L.A0), w1), w2);
+        preF = dm_cscale(dm_cscale(dm_cscale(envF, L.F0), w1), w2);
+        const dm_cplx b = dm_cscale(s, L.cN);
+        cx = dm_cadd(dm_cmul(c, sth), dm_cmul(b, cth));
+        cy = dm_cadd(dm_cmul(dm_cneg(c), cth), dm_cmul(b, sth));
+    }
+    if (L.azi_zero) {
+        Ax = dm_cmul(preA, cth);
+        Ay = dm_cscale(dm_cmul(preA, sth), L.ellip);
+        if (Fx) {
+            *Fx = dm_cmul(preF, cx);
+            *Fy = dm_cscale(dm_cmul(preF, cy), L.ellip);
+        }
+    } else {
+        const dm_cplx se = dm_cscale(sth, L.ellip);
+        Ax = dm_cmul(preA, dm_cadd(dm_cscale(cth, L.cphi), dm_cscale(se, L.sphi)));
+        Ay = dm_cmul(preA, dm_cadd(dm_cscale(cth, -L.sphi), dm_cscale(se, L.cphi)));
+        if (Fx) {
+            const dm_cplx cye = dm_cscale(cy, L.ellip);
+            *Fx = dm_cmul(preF, dm_cadd(dm_cscale(cx, L.cphi), dm_cscale(cye, L.sphi)));
+            *Fy = dm_cmul(preF, dm_cadd(dm_cscale(cx, -L.sphi), dm_cscale(cye, L.cphi)));
+        }
+    }
+}
+
+__host__ __device__ __forceinline__ void laser_AF_complex(const DLaser& L, dm_cplx t, dm_cplx& Ax, dm_cplx& Ay,
+                                                          dm_cplx* Fx, dm_cplx* Fy) {
+    mono_AF_complex(L.m[0], t, Ax, Ay, Fx, Fy);
+    if (L.nmono == 2) {
+        dm_cplx ax2, ay2, fx2, fy2;
+        mono_AF_complex(L.m[1], dm_c(t.re - L.delay, t.im), ax2, ay2, Fx ? &fx2 : nullptr, Fx ? &fy2 : nullptr);
+        Ax = dm_cadd(Ax, ax2);
+        Ay = dm_cadd(Ay, ay2);
+        if (Fx) {
+            *Fx = dm_cadd(*Fx, fx2);
+            *Fy = dm_cadd(*Fy, fy2);
+        }
+    }
+}
+
+__host__ __device__ __forceinline__ void laser_A_complex(const DLaser& L, dm_cplx t, dm_cplx* Ax, dm_cplx* Ay) {
+    laser_AF_complex(L, t, *Ax, *Ay, nullptr, nullptr);
+}
+
 // ---- forward-mode derivative (SPANESampler.jl:168-169 differentiates F with ForwardDiff)
 struct Dual {
     double v, d;

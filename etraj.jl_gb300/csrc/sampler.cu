@@ -1,7 +1,9 @@
-// sampler.cu -- ADK and SPANE initial-condition sampling on the device.
+// sampler.cu -- ADK, SPANE and SPA initial-condition sampling on the device.
 //
-// Reference: gen_electron_batch in src/ElectronSamplers/ADKSampler.jl:167-396
-// and SPANESampler.jl:163-404, with the helpers of shared_methods.jl:4-47.
+// Reference: gen_electron_batch in src/ElectronSamplers/ADKSampler.jl:167-396,
+// SPANESampler.jl:163-404 and SPASampler.jl:150-431, with the helpers of
+// shared_methods.jl:4-47.  The SPA saddle-point solve and quadratures are in
+// spa.h, shared with the CPU oracle.
 //
 // Layout: one thread per candidate (time sample b, transverse-momentum
 // sample i), candidates in the reference's loop order (kd outer, kz inner;
@@ -19,6 +21,10 @@
 // Roofline: memory bound on the SoA writes (about 61 B per candidate).
 
 #include "physics.cuh"
+
+#define SPA_LASER_T etraj::DLaser
+#define SPA_A(L, t, ax, ay) etraj::laser_A_complex(*(L), (t), (ax), (ay))
+#include "spa.h"
 
 namespace etraj {
 namespace {
@@ -373,6 +379,95 @@ k_compact_scatter(const uint8_t* __restrict__ flag, int64_t n, const uint32_t* _
         if (f[k]) idx[pos++] = base + k;
 }
 
+// One thread per SPA candidate (SPASampler.jl:318-391): the same steps as the
+// CPU oracle's o_candidate_spa, in the same order.
+__global__ void __launch_bounds__(128)
+k_sample_spa(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double* __restrict__ kdv,
+             const double* __restrict__ kzv, const DBatch* __restrict__ batches, InitSoA soa,
+             uint8_t* __restrict__ flag) {
+    const int64_t total = nb * J.n_cand;
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t bl = q / J.n_cand, i = q - bl * J.n_cand, b = b0 + bl;
+        const DBatch& B = batches[b];
+        double kd0, kz0;
+        if (!J.mc) {
+            kd0 = kdv[i / J.n_kz];
+            kz0 = kzv[i % J.n_kz];
+        } else {
+            uint32_t c[4] = {(uint32_t)i, (uint32_t)((uint64_t)i >> 32), (uint32_t)b, 0x4B445A00u};
+            philox4x32(c, J.seed);
+            double ua = u53(c[0], c[1]), ub = u53(c[2], c[3]);
+            kd0 = ((ua - 0.5) * 2.0) * J.mc_kd_max;
+            if (J.dim == 3) {
+                kz0 = ((ub - 0.5) * 2.0) * J.mc_kz_max;
+                if (J.mc_kd_max == 0.0) kd0 = 0.0;
+                else if (J.mc_kz_max == 0.0) kz0 = 0.0;
+            } else {
+                kz0 = 0.0;
+            }
+        }
+        uint8_t keep = 0;
+        double x0 = 0.0, y0 = 0.0, kx0 = 0.0, ky0 = 0.0, rate = 0.0, ph = 0.0;
+        const double tr = B.tr, Ip = J.Ip;
+        if (B.F > 1e-3 && !(fabs(kd0) < 1e-4)) {
+            const double w = J.spa_omega, wF = w / B.F;
+            const double guess = dm_asinh(wF * sqrt((kd0 * kd0 + kz0 * kz0) + 2.0 * Ip)) / w;
+            const double ti = spa_solve_ti(&J.laser, tr, kd0, kz0, Ip, guess);
+            if (ti != 0.0) {
+                dm_cplx Ax, Ay, Fx, Fy;
+                laser_AF_complex(J.laser, dm_c(tr, ti), Ax, Ay, &Fx, &Fy);
+                double px, py;
+                spa_pxy(kd0, Ax, Ay, &px, &py);
+                spa_quad_par Q;
+                Q.L = &J.laser;
+                Q.tr = tr;
+                Q.px = px;
+                Q.py = py;
+                Q.kz = kz0;
+                Q.Ip = Ip;
+                int ok0, ok1, ok2;
+                x0 = spa_quadgk(SPA_INT_IM_AX, &Q, dm_c(0.0, 0.0), dm_c(ti, 0.0), &ok0).re;
+                y0 = spa_quadgk(SPA_INT_IM_AY, &Q, dm_c(0.0, 0.0), dm_c(ti, 0.0), &ok1).re;
+                double axr, ayr;
+                laser_A(J.laser, tr, axr, ayr);
+                kx0 = px + axr;
+                ky0 = py + ayr;
+                const dm_cplx Si = spa_quadgk(SPA_INT_ACTION, &Q, dm_c(tr, ti), dm_c(tr, 0.0), &ok2);
+                if (ok0 && ok1 && ok2) {
+                    const dm_cplx St = dm_cneg(Si);
+                    const dm_cplx iS = dm_c(0.0 * St.re - 1.0 * St.im, 0.0 * St.im + 1.0 * St.re);
+                    dm_cplx amp = dm_cscale(dm_cexp(iS), sqrt(J.dkdt));
+                    if (J.prefix & (ETRAJ_PREFIX_PRE | ETRAJ_PREFIX_PRECC)) {
+                        const dm_cplx kx = dm_c(px + Ax.re, Ax.im), ky = dm_c(py + Ay.re, Ay.im);
+                        const dm_cplx num = pre_numerator(J, B, kx, ky, dm_c(kz0, 0.0));
+                        const double cpre = (J.prefix & ETRAJ_PREFIX_PRE) ? J.c : B.c_cc;
+                        const dm_cplx kF = dm_caddr(dm_cadd(dm_cmul(kx, Fx), dm_cmul(ky, Fy)), kz0 * 0.0);
+                        const dm_cplx den = spa_cpow(kF, (J.nstar + 1.0) / 2.0);
+                        amp = dm_cmul(amp, dm_cdiv(dm_cscale(num, cpre), den));
+                    }
+                    if (J.prefix & ETRAJ_PREFIX_JAC) amp = dm_cscale(amp, sqrt(spa_jac(&J.laser, tr, kd0, kz0, Ip, wF, w)));
+                    rate = amp.re * amp.re + amp.im * amp.im;
+                    keep = (!(rate != rate) && !(rate < J.cutoff)) ? 1 : 0;
+                    if (keep && J.phase != ETRAJ_PHASE_CTMC) ph = dm_carg(amp);
+                }
+            }
+        }
+        const int64_t g = b * J.n_cand + i;
+        flag[g] = keep;
+        if (keep) {
+            soa.x[g] = x0;
+            soa.y[g] = y0;
+            soa.kx[g] = kx0;
+            soa.ky[g] = ky0;
+            soa.kz[g] = kz0;
+            soa.rate[g] = rate;
+            if (soa.phase) soa.phase[g] = ph;
+            soa.batch[g] = (int32_t)b;
+        }
+    }
+}
+
 }  // namespace
 
 int launch_batch_prepare(const DJob& J, const double* t, DBatch* batches, cudaStream_t s) {
@@ -385,6 +480,14 @@ int launch_batch_prepare(const DJob& J, const double* t, DBatch* batches, cudaSt
 int launch_sample_range(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
                         const DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
                         cudaStream_t s) {
+    if (J.method == ETRAJ_SAMPLER_SPA) {
+        const int threads = 128;
+        const int64_t want = (nb * J.n_cand + threads - 1) / threads;
+        const int64_t cap = (int64_t)sm_count * 64;
+        const int blocks = (int)(want < cap ? (want > 0 ? want : 1) : cap);
+        k_sample_spa<<<blocks, threads, 0, s>>>(J, b0, nb, kd, kz, batches, soa, flag);
+        return 1;
+    }
     int threads = 256;
     int64_t want = (nb * J.n_cand + threads - 1) / threads;
     int64_t cap = (int64_t)sm_count * 32;

@@ -5,6 +5,7 @@
  * Restates:
  *   src/ElectronSamplers/ADKSampler.jl:19-396   (ctor checks, gen_electron_batch)
  *   src/ElectronSamplers/SPANESampler.jl:19-404
+ *   src/ElectronSamplers/SPASampler.jl:19-431 (with the shared spa.h)
  *   src/ElectronSamplers/shared_methods.jl:4-47 (random points, solid
  *     harmonics, FF->MF Euler angles, field-frame axes)
  *
@@ -147,6 +148,8 @@ int o_sampler_init(const etraj_job* job, o_sampler* S) {
     S->seed = job->seed;
     o_laser_prepare(&job->laser, &S->laser);
     S->mono = (job->laser.kind != ETRAJ_LASER_BICHROMATIC);
+    /* SPA's omega: the laser's, or the mean of the two for a bichromatic one */
+    S->spa_omega = S->mono ? S->laser.m[0].omega : (S->laser.m[0].omega + S->laser.m[1].omega) / 2.0;
     const etraj_target* T = &job->target;
     S->Ip = T->Ip;
     S->Z = (double)T->Z;
@@ -347,6 +350,68 @@ int o_candidate(const o_sampler* S, const o_batch* B, double kd0, double kz0, do
     return 1;
 }
 
+/* ---- SPA ---------------------------------------------------------------------- */
+static void o_spa_A(const o_laser* L, dm_cplx t, dm_cplx* Ax, dm_cplx* Ay) {
+    dm_cplx fx, fy;
+    o_laser_AF_complex(L, t, Ax, Ay, &fx, &fy);
+}
+#define SPA_LASER_T o_laser
+#define SPA_A(L, t, ax, ay) o_spa_A((L), (t), (ax), (ay))
+#include "../etraj.jl_gb300/csrc/spa.h"
+
+/* One SPA candidate (SPASampler.jl:320-347 for the grid, :364-391 for
+ * Monte-Carlo); the batch is skipped before this when F(t_r) <= 1e-3 (:167-169). */
+int o_candidate_spa(const o_sampler* S, const o_batch* B, double kd0, double kz0, double* row) {
+    if (fabs(kd0) < 1e-4) return 0;
+    const o_laser* L = &S->laser;
+    const double tr = B->tr, Ip = S->Ip, w = S->spa_omega, wF = w / B->F;
+    /* initial guess asinh(omega/F sqrt(kd^2+kz^2+2Ip))/omega (:242) */
+    const double guess = dm_asinh(wF * sqrt((kd0 * kd0 + kz0 * kz0) + 2.0 * Ip)) / w;
+    const double ti = spa_solve_ti(L, tr, kd0, kz0, Ip, guess);
+    if (ti == 0.0) return 0;
+    dm_cplx Ax, Ay, Fx, Fy;
+    o_laser_AF_complex(L, dm_c(tr, ti), &Ax, &Ay, &Fx, &Fy);
+    double px, py;
+    spa_pxy(kd0, Ax, Ay, &px, &py);
+    spa_quad_par Q;
+    Q.L = L; Q.tr = tr; Q.px = px; Q.py = py; Q.kz = kz0; Q.Ip = Ip;
+    int ok0, ok1, ok2;
+    const double x0 = spa_quadgk(SPA_INT_IM_AX, &Q, dm_c(0.0, 0.0), dm_c(ti, 0.0), &ok0).re;
+    const double y0 = spa_quadgk(SPA_INT_IM_AY, &Q, dm_c(0.0, 0.0), dm_c(ti, 0.0), &ok1).re;
+    double axr, ayr;
+    o_laser_A(L, tr, &axr, &ayr);
+    const double kx0 = px + axr, ky0 = py + ayr;
+    /* S_tun = -quadgk(..., t_r + i t_i, t_r) (:279); amplitude = sqrt(dkdt) exp(i S_tun) [pre] [sqrt(jac)] */
+    const dm_cplx Si = spa_quadgk(SPA_INT_ACTION, &Q, dm_c(tr, ti), dm_c(tr, 0.0), &ok2);
+    if (!(ok0 && ok1 && ok2)) return 0;
+    const dm_cplx St = dm_cneg(Si);
+    const dm_cplx iS = dm_c(0.0 * St.re - 1.0 * St.im, 0.0 * St.im + 1.0 * St.re);
+    dm_cplx amp = dm_cscale(dm_cexp(iS), sqrt(S->dkdt));
+    if (S->prefix & (ETRAJ_PREFIX_PRE | ETRAJ_PREFIX_PRECC)) {
+        const dm_cplx kx = dm_c(px + Ax.re, Ax.im), ky = dm_c(py + Ay.re, Ay.im), kz = dm_c(kz0, 0.0);
+        const dm_cplx num = o_pre_numerator(S, B, kx, ky, kz);
+        const double cpre = (S->prefix & ETRAJ_PREFIX_PRE) ? S->c : B->c_cc;
+        /* (k_ts . F(t_s))^((n*+1)/2) (:257-262) */
+        const dm_cplx kF = dm_caddr(dm_cadd(dm_cmul(kx, Fx), dm_cmul(ky, Fy)), kz0 * 0.0);
+        const dm_cplx den = spa_cpow(kF, (S->n + 1.0) / 2.0);
+        amp = dm_cmul(amp, dm_cdiv(dm_cscale(num, cpre), den));
+    }
+    if (S->prefix & ETRAJ_PREFIX_JAC) amp = dm_cscale(amp, sqrt(spa_jac(L, tr, kd0, kz0, Ip, wF, w)));
+    const double rate = amp.re * amp.re + amp.im * amp.im;
+    if (dm_isnan(rate) || rate < S->cutoff) return 0;
+    int k = 0;
+    row[k++] = x0;
+    row[k++] = y0;
+    if (S->dim == 3) row[k++] = 0.0;
+    row[k++] = kx0;
+    row[k++] = ky0;
+    if (S->dim == 3) row[k++] = kz0;
+    row[k++] = tr;
+    row[k++] = rate;
+    if (S->phase != ETRAJ_PHASE_CTMC) row[k++] = dm_carg(amp);
+    return 1;
+}
+
 /* (kd0, kz0) of Monte-Carlo candidate i of batch b (shared_methods.jl:4-12,
  * ADKSampler.jl:350-363). */
 void o_mc_point(const o_sampler* S, int64_t b, int64_t i, double* kd0, double* kz0) {
@@ -369,6 +434,8 @@ int64_t o_sample_batch(const o_sampler* S, int64_t b, double* init, int64_t capa
     o_batch_prepare(S, b, &B);
     int64_t count = 0;
     double row[9];
+    const int spa = (S->method == ETRAJ_SAMPLER_SPA);
+    if (spa && B.F <= 1e-3) return 0; /* SPASampler.jl:167-169 */
     for (int64_t i = 0; i < S->n_cand; ++i) {
         double kd0, kz0;
         if (!S->mc) {
@@ -377,7 +444,7 @@ int64_t o_sample_batch(const o_sampler* S, int64_t b, double* init, int64_t capa
         } else {
             o_mc_point(S, b, i, &kd0, &kz0);
         }
-        if (o_candidate(S, &B, kd0, kz0, row)) {
+        if (spa ? o_candidate_spa(S, &B, kd0, kz0, row) : o_candidate(S, &B, kd0, kz0, row)) {
             if (count < capacity) memcpy(init + count * S->rows, row, sizeof(double) * (size_t)S->rows);
             ++count;
         }

@@ -15,6 +15,7 @@ typedef struct {
     int64_t n_t, n_kd, n_kz, n_cand;
     double *t, *kd, *kz;
     double mc_kd_max, mc_kz_max, dkdt;
+    double spa_omega; /* the SPA initial guess' angular frequency (SPASampler.jl:160-166) */
 } o_sampler;
 
 typedef struct {
@@ -30,6 +31,7 @@ int o_sampler_init(const etraj_job* job, o_sampler* S);
 void o_sampler_free(o_sampler* S);
 void o_batch_prepare(const o_sampler* S, int64_t b, o_batch* B);
 int o_candidate(const o_sampler* S, const o_batch* B, double kd0, double kz0, double* row);
+int o_candidate_spa(const o_sampler* S, const o_batch* B, double kd0, double kz0, double* row);
 void o_mc_point(const o_sampler* S, int64_t b, int64_t i, double* kd0, double* kz0);
 int64_t o_sample_batch(const o_sampler* S, int64_t b, double* init, int64_t capacity);
 

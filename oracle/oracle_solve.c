@@ -207,7 +207,6 @@ int oracle_validate(const etraj_job* job, char* msg, int len) {
     if (job->init_cond_method != ETRAJ_SAMPLER_ADK && job->init_cond_method != ETRAJ_SAMPLER_SPANE &&
         job->init_cond_method != ETRAJ_SAMPLER_SPA)
         return o_fail(msg, len, "[ElectronSamplers] Undefined initial condition method.");
-    if (job->init_cond_method == ETRAJ_SAMPLER_SPA) return ETRAJ_ERR_UNSUPPORTED;
     if (job->traj_phase_method < 0 || job->traj_phase_method > 2)
         return o_fail(msg, len, "[ADKSampler] Undefined phase method.");
     if (job->rate_prefix & ~7) return o_fail(msg, len, "[ADKSampler] Undefined tunneling rate prefix.");

@@ -104,6 +104,10 @@ SAMPLE_CASES = [
     dict(method="SPANE", dim=3, mc=True, laser="bichrom", prefix="Pre", phase="QTMC"),
     dict(method="ADK", dim=3, target="Xe", prefix=["Pre", "Jac"]),
     dict(method="SPANE", dim=2, mc=True, target="He", prefix="Exp"),
+    dict(method="SPA", dim=2, target="Ar", laser="cos2", phase="SCTS", ellip=1.0, nt=16, nkd=31),
+    dict(method="SPA", dim=3, mc=True, laser="bichrom", phase="QTMC", nt=12, nkd=8, nkz=8),
+    dict(method="SPA", dim=3, target="Xe", laser="gauss", prefix=["Pre", "Jac"], ellip=0.5, nt=12, nkd=9, nkz=5),
+    dict(method="SPA", dim=2, prefix="Exp", ellip=1.0, nt=16, nkd=31),
 ]
 
 
@@ -155,6 +159,7 @@ RUN_CASES = [
     dict(method="SPANE", dim=3, phase="CTMC", laser="bichrom", mc=True, pnum=(40, 40, 1)),
     dict(method="ADK", dim=2, pnum=(1, 50)),
     dict(method="ADK", dim=2, pmax=0.3),  # many electrons land outside the grid
+    dict(method="SPA", dim=2, phase="QTMC", ellip=1.0, nt=16, nkd=31),
 ]
 
 
