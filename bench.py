@@ -256,7 +256,8 @@ def main():
     value = eff_total.item() / (t_max.item() / 1e3)
 
     # kernel-level timing of the bulk integrator for the roofline
-    kern_ms = integrator_kernel_ms(eng, job, stream)
+    stages = stage_times(eng, job)
+    kern_ms = stages["integrate"]
 
     # ---- end to end through the C ABI with host buffers --------------------------------
     spec_host = np.zeros(grid)
@@ -293,6 +294,7 @@ def main():
             "pmd_rel_l2_vs_fp64": acc and acc["pmd_rel_l2_vs_fp64"],
             "accuracy": acc,
             "latency_ms": {"p50": float(np.percentile(ms, 50)), "p99": float(np.percentile(ms, 99))},
+            "stages_ms": stages,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * (args.t_num + 2),
                     "d2h_bytes_per_step": 8 * grid + 64},
             "gpu_launches": launches,
@@ -343,18 +345,22 @@ def accuracy_report(eng, job, job64):
     return out
 
 
-def integrator_kernel_ms(eng, job, stream):
-    """Average duration of the bulk integrator launch, from the library's own per-stage
-    events (etraj_result.elapsed_ms covers the whole job)."""
+STAGES = ("sample", "compact", "field_table", "integrate", "collect", "deposit")
+
+
+def stage_times(eng, job):
+    """Per-stage device times of one job (mean of 3 runs) from the library's own
+    events on its stream: the integrator entry is the bulk kernel's launch alone."""
     import ctypes as C
 
-    vals = []
+    acc = [[] for _ in STAGES]
     for _ in range(3):
         eng.run(job, want_spectrum=False)
         buf = (C.c_double * 8)()
-        if eng.lib.etraj_stage_times(eng.ctx, buf, 8) > 3:
-            vals.append(buf[3])
-    return statistics.mean(vals) if vals else None
+        k = eng.lib.etraj_stage_times(eng.ctx, buf, 8)
+        for i in range(min(k, len(STAGES))):
+            acc[i].append(buf[i])
+    return {name: (statistics.mean(v) if v else None) for name, v in zip(STAGES, acc)}
 
 
 if __name__ == "__main__":

@@ -205,37 +205,53 @@ __global__ void k_finalize_spec(const double* __restrict__ re, const double* __r
 }
 
 // One level of the 256-ary canonical tree over two arrays.  Level 0 reads
-// n = *count elements, level k reads ceil(n / 256^k).  Each node is the sum of
-// its (up to) 256 children from 0.0, left to right.  One warp per node: the
-// warp stages the children in shared memory with coalesced loads, then lane 0
-// runs the sum of the first array and lane 1 that of the second, so the order
-// of every addition is the canonical one.
+// n = *count elements, level k reads ceil(n / 256^k).  Each node holds 256
+// slots (absent ones +0.0) summed as a binary tree over consecutive pairs:
+// lane j of the node's warp sums slots 8j..8j+7 in three pairwise levels, and
+// five shuffle levels combine lanes (2i, 2i+1), (4i, 4i+2), ...  No chain of
+// dependent FP64 additions is longer than 8, which matters on GB300, whose
+// FP64 unit has a long latency.
 constexpr int kTreeWarps = 8;
 __global__ void __launch_bounds__(32 * kTreeWarps)
 k_tree_level(const double* __restrict__ a_in, const double* __restrict__ b_in,
              double* __restrict__ a_out, double* __restrict__ b_out,
              const unsigned long long* __restrict__ count, int level) {
-    __shared__ double sh[kTreeWarps][2][256];
     int64_t m = (int64_t)*count;
     for (int k = 0; k < level; ++k) m = (m + 255) / 256;
     const int64_t nb = (m + 255) / 256;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int64_t node = (int64_t)blockIdx.x * kTreeWarps + warp; node < nb;
          node += (int64_t)gridDim.x * kTreeWarps) {
-        const int64_t base = node * 256;
-        const int len = (int)((m - base) < 256 ? (m - base) : 256);
-        for (int j = lane; j < len; j += 32) {
-            sh[warp][0][j] = a_in[base + j];
-            sh[warp][1][j] = b_in[base + j];
+        const int64_t base = node * 256 + 8 * lane;
+        double va[8], vb[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const bool in = base + j < m;
+            va[j] = in ? a_in[base + j] : 0.0;
+            vb[j] = in ? b_in[base + j] : 0.0;
         }
-        __syncwarp();
-        if (lane < 2) {
-            const double* v = sh[warp][lane];
-            double acc = 0.0;
-            for (int j = 0; j < len; ++j) acc = acc + v[j];
-            (lane == 0 ? a_out : b_out)[node] = acc;
+#pragma unroll
+        for (int w = 4; w >= 1; w >>= 1) {
+#pragma unroll
+            for (int j = 0; j < w; ++j) {
+                va[j] = va[2 * j] + va[2 * j + 1];
+                vb[j] = vb[2 * j] + vb[2 * j + 1];
+            }
         }
-        __syncwarp();
+        double sa = va[0], sb = vb[0];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const double ra = __shfl_down_sync(0xffffffffu, sa, o);
+            const double rb = __shfl_down_sync(0xffffffffu, sb, o);
+            if ((lane & (2 * o - 1)) == 0) {
+                sa = sa + ra;
+                sb = sb + rb;
+            }
+        }
+        if (lane == 0) {
+            a_out[node] = sa;
+            b_out[node] = sb;
+        }
     }
 }
 
@@ -264,10 +280,20 @@ k_counters(const int32_t* __restrict__ status, const int32_t* __restrict__ steps
         io += __shfl_down_sync(0xffffffffu, io, o);
         st += __shfl_down_sync(0xffffffffu, st, o);
     }
+    // one atomic per block and counter
+    __shared__ unsigned long long part[3][8];
+    const int w = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) {
-        if (f) atomicAdd(&c->n_failed, f);
-        if (io) atomicAdd(&c->n_ionized, io);
-        if (st) atomicAdd(&c->n_steps, st);
+        part[0][w] = f;
+        part[1][w] = io;
+        part[2][w] = st;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        unsigned long long v = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) v += part[threadIdx.x][k];
+        unsigned long long* dst = (threadIdx.x == 0) ? &c->n_failed : (threadIdx.x == 1) ? &c->n_ionized : &c->n_steps;
+        if (v) atomicAdd(dst, v);
     }
 }
 
@@ -382,7 +408,7 @@ int launch_deposit(const DJob& J, const TrajOut& out, const unsigned long long* 
         } while (m > 1);
         k_tree_result<<<1, 1, 0, s>>>(a, b, count, sums);
         int cblocks = (int)((max_n + 255) / 256);
-        if (cblocks > 152 * 8) cblocks = 152 * 8;
+        if (cblocks > 152 * 2) cblocks = 152 * 2;
         k_counters<<<cblocks, 256, 0, s>>>(out.status, out.steps, count, counters);
         launches += 2;
     } else {

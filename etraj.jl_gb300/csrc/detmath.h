@@ -370,6 +370,15 @@ DM_FN dm_cplx dm_cpowi(dm_cplx z, int n) {
     for (int i = 0; i < n; ++i) r = dm_cmul(r, z);
     return r;
 }
+/* sin and cos of one complex argument from one sincos and one sinh/cosh
+ * (the same values as dm_csin and dm_ccos) */
+DM_FN void dm_csincos(dm_cplx a, dm_cplx* sn, dm_cplx* cs) {
+    double s, c, sh, ch;
+    dm_sincos(a.re, &s, &c);
+    dm_sinhcosh(a.im, &sh, &ch);
+    *sn = dm_c(s * ch, c * sh);
+    *cs = dm_c(c * ch, -(s * sh));
+}
 /* cos and sin of a complex argument */
 DM_FN dm_cplx dm_ccos(dm_cplx a) {
     double s, c, sh, ch;

@@ -111,12 +111,14 @@ __host__ __device__ __forceinline__ void laser_A(const DLaser& L, double t, doub
 }
 
 // A and (optionally) F at complex time t_r + i t_i, as SPASampler.jl evaluates
-// them; the tanh windows take real(t) (Cos4Laser.jl:93).
+// them; the tanh windows take real(t) (Cos4Laser.jl:93), so callers that hold
+// Re t fixed pass them precomputed in `win` (w1, w2), or nullptr.
 __host__ __device__ __forceinline__ void mono_AF_complex(const DMono& L, dm_cplx t, dm_cplx& Ax, dm_cplx& Ay,
-                                                         dm_cplx* Fx, dm_cplx* Fy) {
+                                                         dm_cplx* Fx, dm_cplx* Fy, const double* win = nullptr) {
     const dm_cplx tt = dm_c(t.re - L.t_shift, t.im);
     const dm_cplx th = dm_caddr(dm_cscale(tt, L.omega), L.cep);
-    const dm_cplx sth = dm_csin(th), cth = dm_ccos(th);
+    dm_cplx sth, cth;
+    dm_csincos(th, &sth, &cth);
     dm_cplx preA, preF, cx, cy;
     if (L.kind == ETRAJ_LASER_GAUSSIAN) {
         const dm_cplx g = dm_cexp(dm_cscale(dm_cneg(dm_cmul(tt, tt)), L.inv_2s2));
@@ -128,8 +130,14 @@ __host__ __device__ __forceinline__ void mono_AF_complex(const DMono& L, dm_cplx
     } else {
         double w1, w2;
         const dm_cplx u = dm_cscale(tt, L.w2n);
-        const dm_cplx s = dm_csin(u), c = dm_ccos(u);
-        window(L, tt.re, w1, w2);
+        dm_cplx s, c;
+        dm_csincos(u, &s, &c);
+        if (win) {
+            w1 = win[0];
+            w2 = win[1];
+        } else {
+            window(L, tt.re, w1, w2);
+        }
         const dm_cplx c2 = dm_cmul(c, c);
         const dm_cplx envA = (L.kind == ETRAJ_LASER_COS4) ? dm_cmul(c2, c2) : c2;
         const dm_cplx envF = (L.kind == ETRAJ_LASER_COS4) ? dm_cmul(c2, c) : c;
@@ -159,11 +167,12 @@ __host__ __device__ __forceinline__ void mono_AF_complex(const DMono& L, dm_cplx
 }
 
 __host__ __device__ __forceinline__ void laser_AF_complex(const DLaser& L, dm_cplx t, dm_cplx& Ax, dm_cplx& Ay,
-                                                          dm_cplx* Fx, dm_cplx* Fy) {
-    mono_AF_complex(L.m[0], t, Ax, Ay, Fx, Fy);
+                                                          dm_cplx* Fx, dm_cplx* Fy, const double* win = nullptr) {
+    mono_AF_complex(L.m[0], t, Ax, Ay, Fx, Fy, win);
     if (L.nmono == 2) {
         dm_cplx ax2, ay2, fx2, fy2;
-        mono_AF_complex(L.m[1], dm_c(t.re - L.delay, t.im), ax2, ay2, Fx ? &fx2 : nullptr, Fx ? &fy2 : nullptr);
+        mono_AF_complex(L.m[1], dm_c(t.re - L.delay, t.im), ax2, ay2, Fx ? &fx2 : nullptr, Fx ? &fy2 : nullptr,
+                        win ? win + 2 : nullptr);
         Ax = dm_cadd(Ax, ax2);
         Ay = dm_cadd(Ay, ay2);
         if (Fx) {
@@ -173,8 +182,15 @@ __host__ __device__ __forceinline__ void laser_AF_complex(const DLaser& L, dm_cp
     }
 }
 
-__host__ __device__ __forceinline__ void laser_A_complex(const DLaser& L, dm_cplx t, dm_cplx* Ax, dm_cplx* Ay) {
-    laser_AF_complex(L, t, *Ax, *Ay, nullptr, nullptr);
+// window factors (w1, w2) of each laser at real time tre
+__host__ __device__ __forceinline__ void laser_windows(const DLaser& L, double tre, double* win) {
+    window(L.m[0], tre - L.m[0].t_shift, win[0], win[1]);
+    if (L.nmono == 2) window(L.m[1], (tre - L.delay) - L.m[1].t_shift, win[2], win[3]);
+}
+
+__host__ __device__ __forceinline__ void laser_A_complex(const DLaser& L, dm_cplx t, const double* win, dm_cplx* Ax,
+                                                         dm_cplx* Ay) {
+    laser_AF_complex(L, t, *Ax, *Ay, nullptr, nullptr, win);
 }
 
 // ---- forward-mode derivative (SPANESampler.jl:168-169 differentiates F with ForwardDiff)

@@ -23,7 +23,8 @@
 #include "physics.cuh"
 
 #define SPA_LASER_T etraj::DLaser
-#define SPA_A(L, t, ax, ay) etraj::laser_A_complex(*(L), (t), (ax), (ay))
+#define SPA_WIN(L, tre, w) etraj::laser_windows(*(L), (tre), (w))
+#define SPA_AW(L, t, w, ax, ay) etraj::laser_A_complex(*(L), (t), (w), (ax), (ay))
 #include "spa.h"
 
 namespace etraj {
@@ -413,7 +414,9 @@ k_sample_spa(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const doubl
         if (B.F > 1e-3 && !(fabs(kd0) < 1e-4)) {
             const double w = J.spa_omega, wF = w / B.F;
             const double guess = dm_asinh(wF * sqrt((kd0 * kd0 + kz0 * kz0) + 2.0 * Ip)) / w;
-            const double ti = spa_solve_ti(&J.laser, tr, kd0, kz0, Ip, guess);
+            spa_win W;
+            spa_win_init(&W);
+            const double ti = spa_solve_ti(&J.laser, &W, tr, kd0, kz0, Ip, guess);
             if (ti != 0.0) {
                 dm_cplx Ax, Ay, Fx, Fy;
                 laser_AF_complex(J.laser, dm_c(tr, ti), Ax, Ay, &Fx, &Fy);
@@ -421,20 +424,20 @@ k_sample_spa(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const doubl
                 spa_pxy(kd0, Ax, Ay, &px, &py);
                 spa_quad_par Q;
                 Q.L = &J.laser;
+                Q.W = &W;
                 Q.tr = tr;
                 Q.px = px;
                 Q.py = py;
                 Q.kz = kz0;
                 Q.Ip = Ip;
-                int ok0, ok1, ok2;
-                x0 = spa_quadgk(SPA_INT_IM_AX, &Q, dm_c(0.0, 0.0), dm_c(ti, 0.0), &ok0).re;
-                y0 = spa_quadgk(SPA_INT_IM_AY, &Q, dm_c(0.0, 0.0), dm_c(ti, 0.0), &ok1).re;
+                int ok01, ok2;
+                spa_exit(&Q, ti, &x0, &y0, &ok01);
                 double axr, ayr;
                 laser_A(J.laser, tr, axr, ayr);
                 kx0 = px + axr;
                 ky0 = py + ayr;
                 const dm_cplx Si = spa_quadgk(SPA_INT_ACTION, &Q, dm_c(tr, ti), dm_c(tr, 0.0), &ok2);
-                if (ok0 && ok1 && ok2) {
+                if (ok01 && ok2) {
                     const dm_cplx St = dm_cneg(Si);
                     const dm_cplx iS = dm_c(0.0 * St.re - 1.0 * St.im, 0.0 * St.im + 1.0 * St.re);
                     dm_cplx amp = dm_cscale(dm_cexp(iS), sqrt(J.dkdt));
@@ -446,7 +449,7 @@ k_sample_spa(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const doubl
                         const dm_cplx den = spa_cpow(kF, (J.nstar + 1.0) / 2.0);
                         amp = dm_cmul(amp, dm_cdiv(dm_cscale(num, cpre), den));
                     }
-                    if (J.prefix & ETRAJ_PREFIX_JAC) amp = dm_cscale(amp, sqrt(spa_jac(&J.laser, tr, kd0, kz0, Ip, wF, w)));
+                    if (J.prefix & ETRAJ_PREFIX_JAC) amp = dm_cscale(amp, sqrt(spa_jac(&J.laser, &W, tr, kd0, kz0, Ip, wF, w)));
                     rate = amp.re * amp.re + amp.im * amp.im;
                     keep = (!(rate != rate) && !(rate < J.cutoff)) ? 1 : 0;
                     if (keep && J.phase != ETRAJ_PHASE_CTMC) ph = dm_carg(amp);

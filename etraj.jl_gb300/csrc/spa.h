@@ -27,15 +27,36 @@
  *     binary max-heap of intervals and a final re-summation in heap order.
  *
  * The including file defines
- *   SPA_LASER_T                       the laser description type, and
- *   SPA_A(L, t, ax, ay)               A_x, A_y at complex time t (dm_cplx*).
+ *   SPA_LASER_T                       the laser description type,
+ *   SPA_WIN(L, tre, w)                the tanh window factors of its lasers
+ *                                     at real time tre (double w[4]), and
+ *   SPA_AW(L, t, w, ax, ay)           A_x, A_y at complex time t (dm_cplx*)
+ *                                     with the window factors w at Re t.
+ * Re t is the same for all but a few evaluations of one electron (every
+ * quadrature node and every iterate of a solve share t_r), so the window
+ * factors are cached per thread in a spa_win keyed by Re t.
  */
 #ifndef ETRAJ_SPA_H
 #define ETRAJ_SPA_H
 
 #ifndef SPA_LASER_T
-#error "spa.h: define SPA_LASER_T and SPA_A before including"
+#error "spa.h: define SPA_LASER_T, SPA_WIN and SPA_AW before including"
 #endif
+
+typedef struct {
+    double key; /* Re t of w[] (NaN: empty) */
+    double w[4];
+} spa_win;
+
+DM_FN void spa_win_init(spa_win* W) { W->key = dm_u2d(0x7ff8000000000000ull); }
+
+DM_FN void spa_A(const SPA_LASER_T* L, spa_win* W, dm_cplx t, dm_cplx* ax, dm_cplx* ay) {
+    if (!(W->key == t.re)) {
+        SPA_WIN(L, t.re, W->w);
+        W->key = t.re;
+    }
+    SPA_AW(L, t, W->w, ax, ay);
+}
 
 /* momenta of the saddle-point solution (px_, py_, SPASampler.jl:230-231) */
 DM_FN void spa_pxy(double kd, dm_cplx Ax, dm_cplx Ay, double* px, double* py) {
@@ -45,9 +66,9 @@ DM_FN void spa_pxy(double kd, dm_cplx Ax, dm_cplx Ay, double* px, double* py) {
 }
 
 /* saddle_point_equation (SPASampler.jl:233-239) */
-DM_FN double spa_spe(const SPA_LASER_T* L, double tr, double ti, double kd, double kz, double Ip) {
+DM_FN double spa_spe(const SPA_LASER_T* L, spa_win* W, double tr, double ti, double kd, double kz, double Ip) {
     dm_cplx Ax, Ay;
-    SPA_A(L, dm_c(tr, ti), &Ax, &Ay);
+    spa_A(L, W, dm_c(tr, ti), &Ax, &Ay);
     double px, py;
     spa_pxy(kd, Ax, Ay, &px, &py);
     const double ur = px + Ax.re, ui = Ax.im, vr = py + Ay.re, vi = Ay.im;
@@ -56,22 +77,23 @@ DM_FN double spa_spe(const SPA_LASER_T* L, double tr, double ti, double kd, doub
 }
 
 /* central-difference derivative of spa_spe in t_i (FiniteDiff defaults) */
-DM_FN double spa_dspe(const SPA_LASER_T* L, double tr, double x, double kd, double kz, double Ip) {
+DM_FN double spa_dspe(const SPA_LASER_T* L, spa_win* W, double tr, double x, double kd, double kz, double Ip) {
     const double rel = 6.0554544523933395e-06; /* cbrt(eps(Float64)) */
     const double ax = fabs(x);
     const double e = (rel * ax > rel) ? rel * ax : rel;
-    const double f1 = spa_spe(L, tr, x + e, kd, kz, Ip);
-    const double f0 = spa_spe(L, tr, x - e, kd, kz, Ip);
+    const double f1 = spa_spe(L, W, tr, x + e, kd, kz, Ip);
+    const double f0 = spa_spe(L, W, tr, x - e, kd, kz, Ip);
     return (f1 - f0) / (2.0 * e);
 }
 
 /* t_i of the saddle point from the initial guess x0; returns 0 when the
  * solve does not converge or t_i <= 0 (solve_spe, SPASampler.jl:241-249). */
-DM_FN double spa_solve_ti(const SPA_LASER_T* L, double tr, double kd, double kz, double Ip, double x0) {
+DM_FN double spa_solve_ti(const SPA_LASER_T* L, spa_win* W, double tr, double kd, double kz, double Ip,
+                          double x0) {
     const double ftol = 1e-8, eta = 1e-4;
     double x = x0;
-    double r = spa_spe(L, tr, x, kd, kz, Ip);
-    double J = spa_dspe(L, tr, x, kd, kz, Ip);
+    double r = spa_spe(L, W, tr, x, kd, kz, Ip);
+    double J = spa_dspe(L, W, tr, x, kd, kz, Ip);
     if (dm_isnan(r) || dm_isinf(r)) return 0.0; /* NLsolve rejects a non-finite f(x0) */
     int converged = (fabs(r) <= ftol);
     if (dm_isnan(x)) return 0.0;
@@ -108,12 +130,12 @@ DM_FN double spa_solve_ti(const SPA_LASER_T* L, double tr, double kd, double kz,
         }
         const double xold = x;
         x = x + p;
-        const double fn = spa_spe(L, tr, x, kd, kz, Ip);
+        const double fn = spa_spe(L, W, tr, x, kd, kz, Ip);
         const double rp = J * p + r;
         const double rho = (r * r - fn * fn) / (r * r - rp * rp);
         if (rho > eta) {
             r = fn;
-            J = spa_dspe(L, tr, x, kd, kz, Ip);
+            J = spa_dspe(L, W, tr, x, kd, kz, Ip);
             const double dj = fabs(J), d1 = 0.1 * d;
             d = (d1 > dj) ? d1 : dj;
             converged = (fabs(x - xold) <= 0.0) || (fabs(r) <= ftol);
@@ -135,26 +157,31 @@ DM_FN double spa_solve_ti(const SPA_LASER_T* L, double tr, double kd, double kz,
 }
 
 /* ---- quadrature ---------------------------------------------------------- */
-enum { SPA_INT_IM_AX = 0, SPA_INT_IM_AY = 1, SPA_INT_ACTION = 2 };
+/* SPA_INT_IM_AXY evaluates the first two together (one A per node) */
+enum { SPA_INT_IM_AX = 0, SPA_INT_IM_AY = 1, SPA_INT_ACTION = 2, SPA_INT_IM_AXY = 3 };
 
 typedef struct {
     const SPA_LASER_T* L;
+    spa_win* W;
     double tr, px, py, kz, Ip;
 } spa_quad_par;
 
 /* integrands: Im A_x(t_r + i tau), Im A_y(t_r + i tau) (tau = Re t) and
- * ((p_x+A_x(t))^2 + (p_y+A_y(t))^2 + k_z^2)/2 + I_p at complex t */
-DM_FN dm_cplx spa_integrand(int kind, const spa_quad_par* P, dm_cplx t) {
+ * ((p_x+A_x(t))^2 + (p_y+A_y(t))^2 + k_z^2)/2 + I_p at complex t; v1 is the
+ * second integrand of SPA_INT_IM_AXY */
+DM_FN dm_cplx spa_integrand(int kind, const spa_quad_par* P, dm_cplx t, dm_cplx* v1) {
     dm_cplx Ax, Ay;
     if (kind != SPA_INT_ACTION) {
-        SPA_A(P->L, dm_c(P->tr, t.re), &Ax, &Ay);
-        return dm_c(kind == SPA_INT_IM_AX ? Ax.im : Ay.im, 0.0);
+        spa_A(P->L, P->W, dm_c(P->tr, t.re), &Ax, &Ay);
+        *v1 = dm_c(Ay.im, 0.0);
+        return dm_c(kind == SPA_INT_IM_AY ? Ay.im : Ax.im, 0.0);
     }
-    SPA_A(P->L, t, &Ax, &Ay);
+    spa_A(P->L, P->W, t, &Ax, &Ay);
     const dm_cplx u = dm_c(P->px + Ax.re, Ax.im), v = dm_c(P->py + Ay.re, Ay.im);
     dm_cplx s = dm_cadd(dm_cmul(u, u), dm_cmul(v, v));
     s = dm_caddr(s, P->kz * P->kz);
     s = dm_c(s.re / 2.0, s.im / 2.0);
+    *v1 = dm_c(0.0, 0.0);
     return dm_caddr(s, P->Ip);
 }
 
@@ -166,8 +193,10 @@ typedef struct {
 DM_FN double spa_norm(dm_cplx z) { return (z.im == 0.0) ? fabs(z.re) : dm_hypot(z.re, z.im); }
 
 /* Gauss-Kronrod (7, 15) rule on [a, b] (nodes and weights of the 15-point
- * Kronrod extension of the 7-point Gauss rule, Kronrod 1965). */
-DM_FN spa_seg spa_evalrule(int kind, const spa_quad_par* P, dm_cplx a, dm_cplx b) {
+ * Kronrod extension of the 7-point Gauss rule, Kronrod 1965).  g1 receives
+ * the rule of the second integrand of SPA_INT_IM_AXY (same arithmetic as a
+ * separate pass; may be NULL otherwise). */
+DM_FN spa_seg spa_evalrule2(int kind, const spa_quad_par* P, dm_cplx a, dm_cplx b, spa_seg* g1) {
     const double x[8] = {-0.991455371120812639206854697526329, -0.949107912342758524526189684047851,
                          -0.864864423359769072789712788640926, -0.741531185599394439863864773280788,
                          -0.586087235467691130294144845693013, -0.405845151377397166906606412076961,
@@ -179,28 +208,52 @@ DM_FN spa_seg spa_evalrule(int kind, const spa_quad_par* P, dm_cplx a, dm_cplx b
     const double gw[4] = {0.129484966168869693270611432679082, 0.279705391489276667901467771423780,
                           0.381830050505118944950369775488975, 0.417959183673469387755102040816327};
     const dm_cplx s = dm_cscale(dm_csub(b, a), 0.5);
-#define SPA_F2(i)                                                                   \
-    dm_cadd(spa_integrand(kind, P, dm_cadd(a, dm_cscale(s, 1.0 + x[i]))),           \
-            spa_integrand(kind, P, dm_cadd(a, dm_cscale(s, 1.0 - x[i]))))
-    dm_cplx fg = SPA_F2(1), fk = SPA_F2(0);
-    dm_cplx Ig = dm_cscale(fg, gw[0]);
-    dm_cplx Ik = dm_cadd(dm_cscale(fg, w[1]), dm_cscale(fk, w[0]));
+    dm_cplx u1, u2, fg, fk, hg, hk, Ig, Ik, Jg, Jk;
+#define SPA_F2(i, f, h)                                                                  \
+    do {                                                                                 \
+        const dm_cplx p_ = spa_integrand(kind, P, dm_cadd(a, dm_cscale(s, 1.0 + x[i])), &u1); \
+        const dm_cplx q_ = spa_integrand(kind, P, dm_cadd(a, dm_cscale(s, 1.0 - x[i])), &u2); \
+        f = dm_cadd(p_, q_);                                                             \
+        h = dm_cadd(u1, u2);                                                             \
+    } while (0)
+    SPA_F2(1, fg, hg);
+    SPA_F2(0, fk, hk);
+    Ig = dm_cscale(fg, gw[0]);
+    Ik = dm_cadd(dm_cscale(fg, w[1]), dm_cscale(fk, w[0]));
+    Jg = dm_cscale(hg, gw[0]);
+    Jk = dm_cadd(dm_cscale(hg, w[1]), dm_cscale(hk, w[0]));
     for (int i = 2; i <= 3; ++i) {
-        fg = SPA_F2(2 * i - 1);
-        fk = SPA_F2(2 * i - 2);
+        SPA_F2(2 * i - 1, fg, hg);
+        SPA_F2(2 * i - 2, fk, hk);
         Ig = dm_cadd(Ig, dm_cscale(fg, gw[i - 1]));
         Ik = dm_cadd(Ik, dm_cadd(dm_cscale(fg, w[2 * i - 1]), dm_cscale(fk, w[2 * i - 2])));
+        Jg = dm_cadd(Jg, dm_cscale(hg, gw[i - 1]));
+        Jk = dm_cadd(Jk, dm_cadd(dm_cscale(hg, w[2 * i - 1]), dm_cscale(hk, w[2 * i - 2])));
     }
-    const dm_cplx f0 = spa_integrand(kind, P, dm_cadd(a, s));
+    const dm_cplx f0 = spa_integrand(kind, P, dm_cadd(a, s), &u1);
+    const dm_cplx h0 = u1;
+    SPA_F2(6, fg, hg);
     Ig = dm_cadd(Ig, dm_cscale(f0, gw[3]));
-    Ik = dm_cadd(Ik, dm_cadd(dm_cscale(f0, w[7]), dm_cscale(SPA_F2(6), w[6])));
+    Ik = dm_cadd(Ik, dm_cadd(dm_cscale(f0, w[7]), dm_cscale(fg, w[6])));
+    Jg = dm_cadd(Jg, dm_cscale(h0, gw[3]));
+    Jk = dm_cadd(Jk, dm_cadd(dm_cscale(h0, w[7]), dm_cscale(hg, w[6])));
 #undef SPA_F2
     spa_seg g;
     g.a = a;
     g.b = b;
     g.I = dm_cmul(Ik, s);
     g.E = spa_norm(dm_csub(g.I, dm_cmul(Ig, s)));
+    if (g1) {
+        g1->a = a;
+        g1->b = b;
+        g1->I = dm_cmul(Jk, s);
+        g1->E = spa_norm(dm_csub(g1->I, dm_cmul(Jg, s)));
+    }
     return g;
+}
+
+DM_FN spa_seg spa_evalrule(int kind, const spa_quad_par* P, dm_cplx a, dm_cplx b) {
+    return spa_evalrule2(kind, P, a, b, (spa_seg*)0);
 }
 
 #define SPA_MAX_SEGS 48
@@ -230,12 +283,13 @@ DM_FN void spa_heap_down(spa_seg* h, int n, int i) {
     h[i] = x;
 }
 
-/* integral of `kind` over the segment [a, b]; *ok = 0 when the estimate is
- * not finite or the interval budget runs out before the tolerance is met */
-DM_FN dm_cplx spa_quadgk(int kind, const spa_quad_par* P, dm_cplx a, dm_cplx b, int* ok) {
+/* integral of `kind` whose first Kronrod pass over the whole segment is
+ * `first`; *ok = 0 when the estimate is not finite or the interval budget
+ * runs out before the tolerance is met */
+DM_FN dm_cplx spa_quadgk_from(int kind, const spa_quad_par* P, spa_seg first, int* ok) {
     const double rtol = 1.4901161193847656e-08; /* sqrt(eps(Float64)) */
     spa_seg h[SPA_MAX_SEGS];
-    h[0] = spa_evalrule(kind, P, a, b);
+    h[0] = first;
     dm_cplx I = h[0].I;
     double E = h[0].E;
     *ok = !(dm_isnan(E) || dm_isinf(E));
@@ -273,27 +327,41 @@ DM_FN dm_cplx spa_quadgk(int kind, const spa_quad_par* P, dm_cplx a, dm_cplx b, 
     return I;
 }
 
+DM_FN dm_cplx spa_quadgk(int kind, const spa_quad_par* P, dm_cplx a, dm_cplx b, int* ok) {
+    return spa_quadgk_from(kind, P, spa_evalrule(kind, P, a, b), ok);
+}
+
+/* x0 and y0 (SPASampler.jl:355-356): both integrals from one first pass */
+DM_FN void spa_exit(const spa_quad_par* P, double ti, double* x0, double* y0, int* ok) {
+    spa_seg sy;
+    const spa_seg sx = spa_evalrule2(SPA_INT_IM_AXY, P, dm_c(0.0, 0.0), dm_c(ti, 0.0), &sy);
+    int okx, oky;
+    *x0 = spa_quadgk_from(SPA_INT_IM_AX, P, sx, &okx).re;
+    *y0 = spa_quadgk_from(SPA_INT_IM_AY, P, sy, &oky).re;
+    *ok = okx && oky;
+}
+
 /* jac(kd, kz) (SPASampler.jl:280-292): |d(px,py)/d(tr,kd)| by central
  * differences of four saddle-point solves (a failed solve enters as t_i = 0). */
-DM_FN double spa_jac(const SPA_LASER_T* L, double tr, double kd, double kz, double Ip, double omega_over_F,
-                     double omega) {
+DM_FN double spa_jac(const SPA_LASER_T* L, spa_win* W, double tr, double kd, double kz, double Ip,
+                     double omega_over_F, double omega) {
     const double dtr = 0.01, dkd = 0.01;
 #define SPA_GUESS(k) (dm_asinh(omega_over_F * sqrt(((k) * (k) + kz * kz) + 2.0 * Ip)) / omega)
-    const double ti_tp = spa_solve_ti(L, tr + dtr, kd, kz, Ip, SPA_GUESS(kd));
-    const double ti_tm = spa_solve_ti(L, tr - dtr, kd, kz, Ip, SPA_GUESS(kd));
-    const double ti_kp = spa_solve_ti(L, tr, kd + dkd, kz, Ip, SPA_GUESS(kd + dkd));
-    const double ti_km = spa_solve_ti(L, tr, kd - dkd, kz, Ip, SPA_GUESS(kd - dkd));
+    const double ti_tp = spa_solve_ti(L, W, tr + dtr, kd, kz, Ip, SPA_GUESS(kd));
+    const double ti_tm = spa_solve_ti(L, W, tr - dtr, kd, kz, Ip, SPA_GUESS(kd));
+    const double ti_kp = spa_solve_ti(L, W, tr, kd + dkd, kz, Ip, SPA_GUESS(kd + dkd));
+    const double ti_km = spa_solve_ti(L, W, tr, kd - dkd, kz, Ip, SPA_GUESS(kd - dkd));
 #undef SPA_GUESS
     dm_cplx ax, ay;
     double pxa, pya, pxb, pyb;
-    SPA_A(L, dm_c(tr + dtr, ti_tp), &ax, &ay);
+    spa_A(L, W, dm_c(tr + dtr, ti_tp), &ax, &ay);
     spa_pxy(kd, ax, ay, &pxa, &pya);
-    SPA_A(L, dm_c(tr - dtr, ti_tm), &ax, &ay);
+    spa_A(L, W, dm_c(tr - dtr, ti_tm), &ax, &ay);
     spa_pxy(kd, ax, ay, &pxb, &pyb);
     const double dpxdtr = pxa - pxb, dpydtr = pya - pyb;
-    SPA_A(L, dm_c(tr, ti_kp), &ax, &ay);
+    spa_A(L, W, dm_c(tr, ti_kp), &ax, &ay);
     spa_pxy(kd + dkd, ax, ay, &pxa, &pya);
-    SPA_A(L, dm_c(tr, ti_km), &ax, &ay);
+    spa_A(L, W, dm_c(tr, ti_km), &ax, &ay);
     spa_pxy(kd - dkd, ax, ay, &pxb, &pyb);
     const double dpxdkd = pxa - pxb, dpydkd = pya - pyb;
     return fabs(dpxdtr * dpydkd - dpxdkd * dpydtr) / ((4.0 * dtr) * dkd);

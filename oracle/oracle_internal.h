@@ -61,6 +61,9 @@ void o_laser_F_dual(const o_laser* L, double t, double* Fx, double* Fy, double* 
 void o_laser_A(const o_laser* L, double t, double* Ax, double* Ay);
 void o_laser_AF_complex(const o_laser* L, dm_cplx t, dm_cplx* Ax, dm_cplx* Ay, dm_cplx* Fx,
                         dm_cplx* Fy);
+void o_laser_windows(const o_laser* L, double tre, double* win);
+void o_laser_AF_complex_w(const o_laser* L, dm_cplx t, const double* win, dm_cplx* Ax, dm_cplx* Ay,
+                          dm_cplx* Fx, dm_cplx* Fy);
 void o_target_prepare(const etraj_target* in, o_target* T);
 double o_target_V(const o_target* T, double x, double y, double z);
 void o_target_F(const o_target* T, double x, double y, double z, double* F);

@@ -197,8 +197,9 @@ static void o_window_c(const o_mono* L, double tt_re, double* w1, double* w2) {
     o_window(L, tt_re, w1, w2);
 }
 
-void o_mono_AF_complex(const o_mono* L, dm_cplx t, dm_cplx* Ax, dm_cplx* Ay, dm_cplx* Fx,
-                       dm_cplx* Fy) {
+/* win: the window factors (w1, w2) at Re t when the caller holds them, else NULL */
+static void o_mono_AF_complex_w(const o_mono* L, dm_cplx t, const double* win, dm_cplx* Ax, dm_cplx* Ay,
+                                dm_cplx* Fx, dm_cplx* Fy) {
     dm_cplx tt = dm_c(t.re - L->t_shift, t.im);
     dm_cplx th = dm_caddr(dm_cscale(tt, L->omega), L->cep);
     dm_cplx sth = dm_csin(th), cth = dm_ccos(th);
@@ -214,7 +215,12 @@ void o_mono_AF_complex(const o_mono* L, dm_cplx t, dm_cplx* Ax, dm_cplx* Ay, dm_
         double w1, w2;
         dm_cplx u = dm_cscale(tt, L->w2n);
         dm_cplx s = dm_csin(u), c = dm_ccos(u);
-        o_window_c(L, tt.re, &w1, &w2);
+        if (win) {
+            w1 = win[0];
+            w2 = win[1];
+        } else {
+            o_window_c(L, tt.re, &w1, &w2);
+        }
         dm_cplx c2 = dm_cmul(c, c);
         dm_cplx envA = (L->kind == ETRAJ_LASER_COS4) ? dm_cmul(c2, c2) : c2;
         dm_cplx envF = (L->kind == ETRAJ_LASER_COS4) ? dm_cmul(c2, c) : c;
@@ -237,6 +243,11 @@ void o_mono_AF_complex(const o_mono* L, dm_cplx t, dm_cplx* Ax, dm_cplx* Ay, dm_
         *Fx = dm_cmul(preF, dm_cadd(dm_cscale(cx, L->cphi), dm_cscale(cye, L->sphi)));
         *Fy = dm_cmul(preF, dm_cadd(dm_cscale(cx, -L->sphi), dm_cscale(cye, L->cphi)));
     }
+}
+
+void o_mono_AF_complex(const o_mono* L, dm_cplx t, dm_cplx* Ax, dm_cplx* Ay, dm_cplx* Fx,
+                       dm_cplx* Fy) {
+    o_mono_AF_complex_w(L, t, NULL, Ax, Ay, Fx, Fy);
 }
 
 /* ---- whole laser (bichromatic = sum, laser 2 delayed: BichromaticLaser.jl:73-85) */
@@ -269,15 +280,26 @@ void o_laser_A(const o_laser* L, double t, double* Ax, double* Ay) {
     }
 }
 
-void o_laser_AF_complex(const o_laser* L, dm_cplx t, dm_cplx* Ax, dm_cplx* Ay, dm_cplx* Fx,
-                        dm_cplx* Fy) {
-    o_mono_AF_complex(&L->m[0], t, Ax, Ay, Fx, Fy);
+void o_laser_windows(const o_laser* L, double tre, double* win) {
+    o_window(&L->m[0], tre - L->m[0].t_shift, &win[0], &win[1]);
+    if (L->nmono == 2) o_window(&L->m[1], (tre - L->delay) - L->m[1].t_shift, &win[2], &win[3]);
+}
+
+void o_laser_AF_complex_w(const o_laser* L, dm_cplx t, const double* win, dm_cplx* Ax, dm_cplx* Ay,
+                          dm_cplx* Fx, dm_cplx* Fy) {
+    o_mono_AF_complex_w(&L->m[0], t, win, Ax, Ay, Fx, Fy);
     if (L->nmono == 2) {
         dm_cplx ax2, ay2, fx2, fy2;
-        o_mono_AF_complex(&L->m[1], dm_c(t.re - L->delay, t.im), &ax2, &ay2, &fx2, &fy2);
+        o_mono_AF_complex_w(&L->m[1], dm_c(t.re - L->delay, t.im), win ? win + 2 : NULL, &ax2, &ay2, &fx2,
+                            &fy2);
         *Ax = dm_cadd(*Ax, ax2); *Ay = dm_cadd(*Ay, ay2);
         *Fx = dm_cadd(*Fx, fx2); *Fy = dm_cadd(*Fy, fy2);
     }
+}
+
+void o_laser_AF_complex(const o_laser* L, dm_cplx t, dm_cplx* Ax, dm_cplx* Ay, dm_cplx* Fx,
+                        dm_cplx* Fy) {
+    o_laser_AF_complex_w(L, t, NULL, Ax, Ay, Fx, Fy);
 }
 
 /* ---- targets ---------------------------------------------------------------- */

@@ -351,12 +351,13 @@ int o_candidate(const o_sampler* S, const o_batch* B, double kd0, double kz0, do
 }
 
 /* ---- SPA ---------------------------------------------------------------------- */
-static void o_spa_A(const o_laser* L, dm_cplx t, dm_cplx* Ax, dm_cplx* Ay) {
+static void o_spa_AW(const o_laser* L, dm_cplx t, const double* win, dm_cplx* Ax, dm_cplx* Ay) {
     dm_cplx fx, fy;
-    o_laser_AF_complex(L, t, Ax, Ay, &fx, &fy);
+    o_laser_AF_complex_w(L, t, win, Ax, Ay, &fx, &fy);
 }
 #define SPA_LASER_T o_laser
-#define SPA_A(L, t, ax, ay) o_spa_A((L), (t), (ax), (ay))
+#define SPA_WIN(L, tre, w) o_laser_windows((L), (tre), (w))
+#define SPA_AW(L, t, w, ax, ay) o_spa_AW((L), (t), (w), (ax), (ay))
 #include "../etraj.jl_gb300/csrc/spa.h"
 
 /* One SPA candidate (SPASampler.jl:320-347 for the grid, :364-391 for
@@ -367,23 +368,25 @@ int o_candidate_spa(const o_sampler* S, const o_batch* B, double kd0, double kz0
     const double tr = B->tr, Ip = S->Ip, w = S->spa_omega, wF = w / B->F;
     /* initial guess asinh(omega/F sqrt(kd^2+kz^2+2Ip))/omega (:242) */
     const double guess = dm_asinh(wF * sqrt((kd0 * kd0 + kz0 * kz0) + 2.0 * Ip)) / w;
-    const double ti = spa_solve_ti(L, tr, kd0, kz0, Ip, guess);
+    spa_win W;
+    spa_win_init(&W);
+    const double ti = spa_solve_ti(L, &W, tr, kd0, kz0, Ip, guess);
     if (ti == 0.0) return 0;
     dm_cplx Ax, Ay, Fx, Fy;
     o_laser_AF_complex(L, dm_c(tr, ti), &Ax, &Ay, &Fx, &Fy);
     double px, py;
     spa_pxy(kd0, Ax, Ay, &px, &py);
     spa_quad_par Q;
-    Q.L = L; Q.tr = tr; Q.px = px; Q.py = py; Q.kz = kz0; Q.Ip = Ip;
-    int ok0, ok1, ok2;
-    const double x0 = spa_quadgk(SPA_INT_IM_AX, &Q, dm_c(0.0, 0.0), dm_c(ti, 0.0), &ok0).re;
-    const double y0 = spa_quadgk(SPA_INT_IM_AY, &Q, dm_c(0.0, 0.0), dm_c(ti, 0.0), &ok1).re;
+    Q.L = L; Q.W = &W; Q.tr = tr; Q.px = px; Q.py = py; Q.kz = kz0; Q.Ip = Ip;
+    int ok01, ok2;
+    double x0, y0;
+    spa_exit(&Q, ti, &x0, &y0, &ok01);
     double axr, ayr;
     o_laser_A(L, tr, &axr, &ayr);
     const double kx0 = px + axr, ky0 = py + ayr;
     /* S_tun = -quadgk(..., t_r + i t_i, t_r) (:279); amplitude = sqrt(dkdt) exp(i S_tun) [pre] [sqrt(jac)] */
     const dm_cplx Si = spa_quadgk(SPA_INT_ACTION, &Q, dm_c(tr, ti), dm_c(tr, 0.0), &ok2);
-    if (!(ok0 && ok1 && ok2)) return 0;
+    if (!(ok01 && ok2)) return 0;
     const dm_cplx St = dm_cneg(Si);
     const dm_cplx iS = dm_c(0.0 * St.re - 1.0 * St.im, 0.0 * St.im + 1.0 * St.re);
     dm_cplx amp = dm_cscale(dm_cexp(iS), sqrt(S->dkdt));
@@ -396,7 +399,7 @@ int o_candidate_spa(const o_sampler* S, const o_batch* B, double kd0, double kz0
         const dm_cplx den = spa_cpow(kF, (S->n + 1.0) / 2.0);
         amp = dm_cmul(amp, dm_cdiv(dm_cscale(num, cpre), den));
     }
-    if (S->prefix & ETRAJ_PREFIX_JAC) amp = dm_cscale(amp, sqrt(spa_jac(L, tr, kd0, kz0, Ip, wF, w)));
+    if (S->prefix & ETRAJ_PREFIX_JAC) amp = dm_cscale(amp, sqrt(spa_jac(L, &W, tr, kd0, kz0, Ip, wF, w)));
     const double rate = amp.re * amp.re + amp.im * amp.im;
     if (dm_isnan(rate) || rate < S->cutoff) return 0;
     int k = 0;

@@ -17,8 +17,9 @@
  * Deterministic reductions (the reference sums per Julia thread in a
  * schedule-dependent order; this is the fixed order the device reproduces):
  *   spectrum bin     -- 0.0 + contributions in trajectory order;
- *   ion_prob, ...    -- 256-ary tree over trajectory order, each node summed
- *                       left to right starting from 0.0.
+ *   ion_prob, ...    -- 256-ary tree over trajectory order; each node is a
+ *                       binary tree over its 256 slots (absent slots +0.0),
+ *                       so no chain of dependent additions exceeds 8.
  */
 #include "oracle_internal.h"
 #include "oracle_sampler.h"
@@ -394,7 +395,17 @@ int oracle_contributions(const etraj_job* job, int64_t n, const double* init, co
     return 0;
 }
 
-/* 256-ary tree sum over v[0..n), each node summed left to right from 0.0 */
+/* one node of the canonical tree: v[0..len) (len <= 256) in 256 slots, absent
+ * slots +0.0, summed as a binary tree over consecutive pairs */
+static double o_node_sum(const double* v, int64_t len) {
+    double t[256];
+    for (int i = 0; i < 256; ++i) t[i] = (i < len) ? v[i] : 0.0;
+    for (int w = 128; w >= 1; w >>= 1)
+        for (int i = 0; i < w; ++i) t[i] = t[2 * i] + t[2 * i + 1];
+    return t[0];
+}
+
+/* 256-ary tree over v[0..n) whose nodes are o_node_sum */
 static double o_canon_sum(const double* v, int64_t n) {
     if (n == 0) return 0.0;
     double* cur = (double*)malloc(sizeof(double) * (size_t)n);
@@ -403,10 +414,8 @@ static double o_canon_sum(const double* v, int64_t n) {
     do {
         int64_t nb = (m + 255) / 256;
         for (int64_t b = 0; b < nb; ++b) {
-            double s = 0.0;
             int64_t e = (b + 1) * 256 < m ? (b + 1) * 256 : m;
-            for (int64_t i = b * 256; i < e; ++i) s = s + cur[i];
-            cur[b] = s;
+            cur[b] = o_node_sum(cur + b * 256, e - b * 256);
         }
         m = nb;
     } while (m > 1);
