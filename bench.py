@@ -45,6 +45,7 @@ WORKLOAD = ("SAE Ar, Cos2 800 nm 1.2e14 W/cm^2 2 cyc CP, SPANE Monte-Carlo 1e4 t
 
 
 def make_job(precision="fp32_bulk", seed=0, t_num=10000, kt_num=1000):
+    """Headline workload: 1e7 SPANE Monte-Carlo candidates, Ar, Cos2 CP, SCTS, 1000^2."""
     laser = et.Cos2Laser(peak_int=1.2e14, wave_len=800.0, cyc_num=2, ellip=1.0)
     T = laser.Period()
     half = laser.CycNum() * T / 2  # the Cos2 envelope spans [-N T/2, N T/2]
@@ -53,6 +54,44 @@ def make_job(precision="fp32_bulk", seed=0, t_num=10000, kt_num=1000):
                        final_p_max=(2.0, 2.0), final_p_num=(1000, 1000), sample_monte_carlo=True,
                        mc_kt_num=kt_num, mc_kd_max=1.0, traj_phase_method="SCTS", seed=seed,
                        precision=precision)
+
+
+def make_job_spa_bichromatic(precision="fp32_bulk", seed=0, t_num=30000, kt_num=1000):
+    """Uneven-step workload: H, counter-rotating CP 800 nm (Cos4, 8 cycles) + 400 nm
+    (16 cycles), 5e13 W/cm^2 each; SPA Monte-Carlo 3D (t_num x kt_num candidates,
+    3e7 in full), QTMC, coherent 256^3 PMD +-2 a.u."""
+    l1 = et.Cos4Laser(peak_int=5e13, wave_len=800.0, cyc_num=8, ellip=1.0)
+    l2 = et.Cos4Laser(peak_int=5e13, wave_len=400.0, cyc_num=16, ellip=-1.0)
+    T = l1.Period()
+    return et.make_job(init_cond_method="SPA", laser=et.BichromaticLaser(l1, l2, delay=0.0),
+                       target=et.get_atom("H"), dimension=3, sample_t_intv=(-4 * T, 4 * T),
+                       sample_t_num=t_num, traj_t_final=6 * T, final_p_max=(2.0, 2.0, 2.0),
+                       final_p_num=(256, 256, 256), sample_monte_carlo=True, mc_kt_num=kt_num,
+                       mc_kd_max=1.0, mc_kz_max=1.0, traj_phase_method="QTMC", seed=seed,
+                       precision=precision)
+
+
+def make_job_adk_h(precision="fp32_bulk", seed=0, t_num=2000, kt_num=None):
+    """Small plain workload: H, Cos4 800 nm 1e14 W/cm^2 2 cycles LP; ADK grid of t_num
+    time samples x 21 x 21 (kd, kz) in [-1, 1]; CTMC; 500 x 500 PMD +-1.5 a.u."""
+    laser = et.Cos4Laser(peak_int=1e14, wave_len=800.0, cyc_num=2, ellip=0.0)
+    T = laser.Period()
+    return et.make_job(init_cond_method="ADK", laser=laser, target=et.get_atom("H"), dimension=3,
+                       sample_t_intv=(-T, T), sample_t_num=t_num, traj_t_final=3 * T,
+                       final_p_max=(1.5, 1.5, 1.0), final_p_num=(500, 500, 1), ss_kd_max=1.0,
+                       ss_kd_num=21, ss_kz_max=1.0, ss_kz_num=21, traj_phase_method="CTMC",
+                       seed=seed, precision=precision)
+
+
+WORKLOADS = {
+    "ar_spane_scts_2d": (make_job, 10000, 1000, WORKLOAD),
+    "h_spa_bichromatic_3d": (make_job_spa_bichromatic, 30000, 1000,
+                             "H, counter-rotating CP 800+400 nm 5e13 W/cm^2 each (Cos4, 8 cycles at "
+                             "800 nm), SPA Monte-Carlo 3D, QTMC, coherent 256^3 PMD +-2 a.u."),
+    "h_adk_cos4_3d": (make_job_adk_h, 2000, 441,
+                      "H, Cos4 800 nm 1e14 W/cm^2 2 cycles LP, ADK grid t x 21 x 21, CTMC, "
+                      "incoherent 500 x 500 PMD +-1.5 a.u."),
+}
 
 
 # FP32 operations of one Tsit5 step of the bulk integrator for 2D SAE SCTS, counted
@@ -132,7 +171,7 @@ def measured_peaks():
         return {}
 
 
-def cpu_baseline(job_fn, seconds_target=15.0):
+def cpu_baseline(job_fn, t_full=10000, seconds_target=15.0):
     """Times the CPU oracle (the reference's algorithm restated in C, OpenMP over time
     samples) on a bounded sample of the workload: a slice of the time samples."""
     sys.path.insert(0, os.path.join(ROOT, "tests"))
@@ -146,20 +185,23 @@ def cpu_baseline(job_fn, seconds_target=15.0):
         t0 = time.perf_counter()
         _, _, sc = _oracle.run(job)
         dt = time.perf_counter() - t0
-        if dt > seconds_target / 4 or t_num >= 10000:
+        if dt > seconds_target / 4 or t_num >= t_full:
             break
-        t_num = min(10000, int(t_num * max(2.0, seconds_target / 3 / max(dt, 1e-3))))
+        t_num = min(t_full, int(t_num * max(2.0, seconds_target / 3 / max(dt, 1e-3))))
     return {"value": sc["num_effective"] / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "%d of 10000 time samples x 1000 kd (%d effective trajectories, %.1f s)"
-                      % (t_num, int(sc["num_effective"]), dt)}
+            "sample": "%d of %d time samples (%d effective trajectories, %.1f s)"
+                      % (t_num, t_full, int(sc["num_effective"]), dt)}
 
 
 def run_reference(args):
     rank, world, _ = rank_env()
     if rank != 0:
         return 0
-    job_fn = lambda n: make_job("fp64", seed=0, t_num=n)  # noqa: E731
-    base = cpu_baseline(job_fn, seconds_target=12.0)
+    maker, t_full, _, workload_text = WORKLOADS[args.workload]
+    job_fn = lambda n: maker("fp64", seed=0, t_num=n)  # noqa: E731
+    # each step a bounded sample: about 120 s for the whole run, at most ~3 s a step
+    per_step = min(3.0, 120.0 / max(1, args.steps + args.warmup))
+    base = cpu_baseline(job_fn, t_full, seconds_target=4.0 * per_step)
     n = int(base["sample"].split(" ")[0])
     times, effs = [], []
     sys.path.insert(0, os.path.join(ROOT, "tests"))
@@ -167,7 +209,7 @@ def run_reference(args):
 
     sys.path.pop(0)
     for i in range(args.warmup + args.steps):
-        job = make_job("fp64", seed=i, t_num=n)
+        job = maker("fp64", seed=i, t_num=n)
         t0 = time.perf_counter()
         _, _, sc = _oracle.run(job)
         dt = time.perf_counter() - t0
@@ -178,7 +220,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 0,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": {"workload": WORKLOAD, "sample": base["sample"]},
+            "data": "synthetic", "config": {"workload": workload_text, "sample": base["sample"]},
             "cpu_baseline": dict(base, value=value),
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "reference = the C restatement of eTraj.jl's algorithm on the host cores "
@@ -194,10 +236,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--t-num", type=int, default=10000,
-                    help="time samples (x 1000 kd candidates); 10000 is the full workload")
+    ap.add_argument("--workload", default="ar_spane_scts_2d", choices=sorted(WORKLOADS),
+                    help="ar_spane_scts_2d is the headline workload; the others are the uneven-step "
+                         "SPA workload and the small ADK workload")
+    ap.add_argument("--t-num", type=int, default=None,
+                    help="time samples (default: the workload's full size)")
     ap.add_argument("--precision", default="fp32_bulk", choices=["fp32_bulk", "fp64"],
                     help="path timed as `value` (fp64 profiles the plain kernel)")
+    ap.add_argument("--no-serving", action="store_true",
+                    help="skip the serving-loop replay (512 Poisson arrivals at 20/s)")
     ap.add_argument("--no-fp64-compare", action="store_true",
                     help="skip the FP64 run used for the speed ratio and PMD error (profiling)")
     args = ap.parse_args()
@@ -216,8 +263,12 @@ def main():
     stream = torch.cuda.Stream(device=dev)
     eng.set_stream(stream.cuda_stream)
 
-    job = make_job(args.precision, seed=rank, t_num=args.t_num)
-    job64 = make_job("fp64", seed=rank, t_num=args.t_num)
+    maker, t_full, kt_per_t, workload_text = WORKLOADS[args.workload]
+    if args.t_num is None:
+        args.t_num = t_full
+    headline = (args.workload == "ar_spane_scts_2d")
+    job = maker(args.precision, seed=rank, t_num=args.t_num)
+    job64 = maker("fp64", seed=rank, t_num=args.t_num)
     grid = job.grid_size
 
     # accuracy: FP32-bulk against the FP64 plain path on the same sampled electrons
@@ -279,14 +330,16 @@ def main():
         fp32_peak = n_sm * 128 * 2 * (peaks.get("sm_max_mhz", 2070.0) * 1e6) / 1e12
         steps_per_job = steps_total / args.steps
         flops = steps_per_job * FLOPS_PER_STEP_SAE_2D_SCTS
-        achieved = flops / (kern_ms / 1e3) / 1e12 if kern_ms else None
+        # the flop count per step is the headline workload's (2D SAE SCTS)
+        achieved = flops / (kern_ms / 1e3) / 1e12 if (kern_ms and headline) else None
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": statistics.mean(ms), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 stages + f64 collection/deposit",
             "data": "synthetic",
-            "config": {"workload": WORKLOAD, "effective_trajectories_per_step": statistics.mean(effs),
-                       "candidates_per_step": args.t_num * 1000, "l2_flush": "outputs 1e7 x 64 B > L2",
+            "config": {"workload": workload_text, "effective_trajectories_per_step": statistics.mean(effs),
+                       "candidates_per_step": args.t_num * kt_per_t,
+                       "l2_flush": "per-electron buffers of every step exceed L2 (1e7 x ~100 B)",
                        "parallelism": "weak: one Monte-Carlo shard per GPU (seed = rank)"},
             "precision": args.precision,
             "fp64_plain": acc and acc["fp64_plain"],
@@ -308,8 +361,10 @@ def main():
             "clocks": clocks,
             "wall_s": t_wall,
         }
+        if not args.no_serving and world == 1:
+            line["serving"] = serving_report()
         if not args.no_cpu_baseline:
-            line["cpu_baseline"] = cpu_baseline(lambda n: make_job("fp64", seed=0, t_num=n))
+            line["cpu_baseline"] = cpu_baseline(lambda n: maker("fp64", seed=0, t_num=n), t_full)
         print(json.dumps(line))
     eng.close()
     if world > 1:
@@ -330,9 +385,15 @@ def accuracy_report(eng, job, job64):
     def l2(a, b):
         return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
+    dims = [int(job.final_p_num[d]) for d in range(job.dimension)]
+
     def rebin(P, f):
-        n = int(round(math.sqrt(P.size)))
-        return P.reshape(n, n).reshape(n // f, f, n // f, f).sum(axis=(1, 3))
+        # Julia column-major grid: x fastest
+        a = P.reshape(tuple(reversed(dims)))
+        for ax in range(a.ndim):
+            if a.shape[ax] > 1:
+                a = np.add.reduceat(a, np.arange(0, a.shape[ax], f), axis=ax)
+        return a.ravel()
 
     out = {"fp64_plain": {"value": res64.num_effective_traj / (res64.elapsed_ms / 1e3), "unit": UNIT,
                           "ms_per_step": res64.elapsed_ms},
@@ -343,6 +404,103 @@ def accuracy_report(eng, job, job64):
         out["pmd_rel_l2_vs_fp64_rebin%d" % f] = l2(rebin(spec, f), rebin(spec64, f))
         out["fp64_rtol1e-7_vs_rtol1e-6_rebin%d" % f] = l2(rebin(spec64b, f), rebin(spec64, f))
     return out
+
+
+def serving_requests(n=512, rate=20.0, seed=2024):
+    """The serving workload: n requests with Poisson arrivals at `rate` per second,
+    each a random mix of target {H, Ar}, laser {Cos4 LP, Cos2 CP, counter-rotating
+    CP bichromatic (lambda, lambda/2)}, wavelength U(400, 1600) nm, intensity
+    log-U(5e13, 3e14) W/cm^2, 1-8 cycles, sampler {ADK, SPANE}, phase {CTMC, QTMC,
+    SCTS}, log-U(1e4, 3e7) Monte-Carlo candidates and a 2D grid of 256^2-1000^2."""
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+    reqs = []
+    for i in range(n):
+        lam = rng.uniform(400.0, 1600.0)
+        inten = float(np.exp(rng.uniform(np.log(5e13), np.log(3e14))))
+        cyc = int(rng.integers(1, 9))
+        kind = int(rng.integers(0, 3))
+        if kind == 0:
+            laser = et.Cos4Laser(peak_int=inten, wave_len=lam, cyc_num=cyc, ellip=0.0)
+        elif kind == 1:
+            laser = et.Cos2Laser(peak_int=inten, wave_len=lam, cyc_num=cyc, ellip=1.0)
+        else:
+            laser = et.BichromaticLaser(et.Cos4Laser(peak_int=inten, wave_len=lam, cyc_num=cyc, ellip=1.0),
+                                        et.Cos4Laser(peak_int=inten, wave_len=lam / 2, cyc_num=2 * cyc,
+                                                     ellip=-1.0), delay=0.0)
+        T = 2 * np.pi * lam / 45.563352525
+        half = cyc * T / 2 if kind == 1 else cyc * T
+        ncand = float(np.exp(rng.uniform(np.log(1e4), np.log(3e7))))
+        t_num = max(10, int(round(ncand / 1000)))
+        grid = int(rng.integers(256, 1001))
+        job = et.make_job(init_cond_method=("ADK", "SPANE")[int(rng.integers(0, 2))], laser=laser,
+                          target=et.get_atom(("H", "Ar")[int(rng.integers(0, 2))]), dimension=2,
+                          sample_t_intv=(-half, half), sample_t_num=t_num, traj_t_final=half + 2 * T,
+                          final_p_max=(2.0, 2.0), final_p_num=(grid, grid), sample_monte_carlo=True,
+                          mc_kt_num=1000, mc_kd_max=1.0,
+                          traj_phase_method=("CTMC", "QTMC", "SCTS")[int(rng.integers(0, 3))],
+                          seed=i, precision="fp32_bulk")
+        reqs.append(job)
+    return arrivals, reqs
+
+
+def serving_report(n=512, rate=20.0, slots=8, fp64_seconds=20.0):
+    """Replays the request stream in real time against an etraj server (bulk
+    path) and reports arrival-to-result latency and aggregate throughput; then
+    serves the stream's first requests one at a time on the FP64 path, for
+    about `fp64_seconds` (a request's time is set by its slowest trajectory)."""
+    arrivals, reqs = serving_requests(n, rate)
+    srv = et.Server(device=0, slots=slots)
+    # warm-up: one small job per slot
+    for t in [srv.submit(reqs[k]) for k in range(slots)]:
+        srv.wait(t, timeout=600.0)
+    lat, effs, pending = [], [], {}
+    t0 = time.perf_counter()
+    i = 0
+    max_running = max_queued = 0
+    while i < n or pending:
+        now = time.perf_counter() - t0
+        while i < n and arrivals[i] <= now:
+            pending[srv.submit(reqs[i])] = arrivals[i]
+            i += 1
+        running, queued, _ = srv.stats()
+        max_running, max_queued = max(max_running, running), max(max_queued, queued)
+        done = []
+        for tk, arr in pending.items():
+            out = srv.poll(tk)
+            if out is not None:
+                lat.append(time.perf_counter() - t0 - arr)
+                effs.append(out[0].num_effective_traj)
+                done.append(tk)
+        for tk in done:
+            del pending[tk]
+        if not done:
+            time.sleep(0.0005)
+    span = time.perf_counter() - t0 - arrivals[0]
+    srv.close()
+    eng = et.Engine(device=0)
+    fp64_ms, fp64_eff = [], []
+    for job in reqs:
+        j = job.copy()
+        j.precision = abi.PRECISION_FP64
+        t1 = time.perf_counter()
+        r, _, _ = eng.run(j, want_spectrum=True)
+        fp64_ms.append(1e3 * (time.perf_counter() - t1))
+        fp64_eff.append(r.num_effective_traj)
+        if sum(fp64_ms) > 1e3 * fp64_seconds:
+            break
+    eng.close()
+    lat_ms = 1e3 * np.array(lat)
+    fp64_rate = sum(fp64_eff) / (sum(fp64_ms) / 1e3)
+    return {"requests": n, "arrival_rate_per_s": rate, "slots": slots,
+            "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99)),
+                           "max": float(lat_ms.max())},
+            "trajectories_per_s": float(sum(effs) / span), "effective_trajectories": int(sum(effs)),
+            "span_s": float(span), "max_running": max_running, "max_queued": max_queued,
+            "fp64_one_at_a_time": {"requests": len(fp64_ms), "trajectories_per_s": fp64_rate,
+                                   "mean_service_ms": float(np.mean(fp64_ms)),
+                                   "offered_load_vs_capacity": float(rate * np.mean(fp64_ms) / 1e3)},
+            "workload": serving_requests.__doc__.split("\n\n")[0].replace("\n    ", " ")}
 
 
 STAGES = ("sample", "compact", "field_table", "integrate", "collect", "deposit")

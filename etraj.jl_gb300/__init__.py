@@ -9,11 +9,11 @@ from .lasers import (Laser, MonochromaticLaser, Cos4Laser, Cos2Laser, GaussianLa
                      BichromaticLaser)
 from .targets import (Target, SAEAtomBase, HydrogenLikeAtom, SAEAtom, get_atom,
                       get_available_atoms, hartree_asymp_coeff)
-from .simulation import (perform_traj_simulation, make_job, rate_prefix_bits, Engine,
+from .simulation import (perform_traj_simulation, make_job, rate_prefix_bits, Engine, Server,
                          EtrajError, default_engine)
 
 __all__ = ["load_library", "Laser", "MonochromaticLaser", "Cos4Laser", "Cos2Laser",
            "GaussianLaser", "BichromaticLaser", "Target", "SAEAtomBase", "HydrogenLikeAtom",
            "SAEAtom", "get_atom", "get_available_atoms", "hartree_asymp_coeff",
-           "perform_traj_simulation", "make_job", "rate_prefix_bits", "Engine", "EtrajError",
-           "default_engine"]
+           "perform_traj_simulation", "make_job", "rate_prefix_bits", "Engine", "Server",
+           "EtrajError", "default_engine"]

@@ -114,6 +114,13 @@ SIGNATURES = [
     ("etraj_submit", C.c_int, [C.c_void_p, C.POINTER(Job), C.POINTER(Result), C.POINTER(C.c_uint64)]),
     ("etraj_poll", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(Result)]),
     ("etraj_wait", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(Result)]),
+    ("etraj_server_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_size_t]),
+    ("etraj_server_destroy", None, [C.c_void_p]),
+    ("etraj_server_submit", C.c_int, [C.c_void_p, C.POINTER(Job), C.POINTER(Result), C.POINTER(C.c_uint64)]),
+    ("etraj_server_poll", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(Result)]),
+    ("etraj_server_wait", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(Result), C.c_double]),
+    ("etraj_server_stats", C.c_int, [C.c_void_p, _I64P, _I64P, C.POINTER(C.c_size_t)]),
+    ("etraj_server_last_error", C.c_char_p, [C.c_void_p]),
     ("etraj_stage_times", C.c_int, [C.c_void_p, _DP, C.c_int]),
     ("etraj_deposit_noalloc", C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                         C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -17,7 +17,10 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <chrono>
+#include <deque>
 #include <mutex>
+#include <thread>
 #include <string>
 #include <vector>
 
@@ -342,10 +345,27 @@ struct DevBuf {
     size_t bytes = 0;
 };
 
-struct AsyncJob {
-    int status;
-    etraj_result result;
+// One enqueued job.  Its results land either straight in the caller's
+// buffers (synchronous etraj_run) or in a pinned staging block that is copied
+// out when the job completes (asynchronous submit and the server).
+struct JobRec {
+    int status = ETRAJ_OK;       // enqueue status; an error completes the job at once
     std::string error;
+    etraj_result res{};          // the caller's output pointers; scalars filled at completion
+    int64_t grid = 0;
+    bool coherent = false;
+    int launches = 0;
+    bool staged = false;
+    void* pinned = nullptr;      // staged: sums[2] | Counters | mspec[grid] | amplitude[2 grid]
+    size_t pinned_bytes = 0;
+    cudaEvent_t ev_start = nullptr, ev_done = nullptr;
+    double direct_sums[2] = {0.0, 0.0};
+    Counters direct_cnt{};
+};
+
+struct PinnedBlock {
+    void* p = nullptr;
+    size_t bytes = 0;
 };
 
 }  // namespace
@@ -366,7 +386,12 @@ struct etraj_ctx {
     cudaEvent_t stage_ev[kStages + 1] = {};
     bool stage_valid = false;
     uint64_t next_ticket = 1;
-    std::map<uint64_t, AsyncJob> jobs;
+    std::map<uint64_t, JobRec> jobs;       // asynchronous tickets of this context
+    std::vector<PinnedBlock> pinned_pool;  // staging blocks for reuse
+    std::vector<cudaEvent_t> event_pool;
+    // sizing without allocating: ensure() only adds up the growth
+    bool dry = false;
+    size_t dry_bytes = 0;
     std::mutex mu;
 };
 
@@ -384,6 +409,13 @@ int cuda_err(etraj_ctx* ctx, cudaError_t e, const char* where) {
 // Grow-only named device buffer, counted against the context's HBM budget.
 int ensure(etraj_ctx* ctx, const char* name, size_t bytes, void** out) {
     if (bytes == 0) bytes = 256;
+    if (ctx->dry) {
+        auto it = ctx->bufs.find(name);
+        const size_t have = (it == ctx->bufs.end()) ? 0 : it->second.bytes;
+        if (have < bytes) ctx->dry_bytes += (bytes + bytes / 8) - have;
+        *out = nullptr;
+        return ETRAJ_OK;
+    }
     DevBuf& b = ctx->bufs[name];
     if (b.bytes >= bytes) {
         *out = b.p;
@@ -398,14 +430,15 @@ int ensure(etraj_ctx* ctx, const char* name, size_t bytes, void** out) {
                                std::to_string(bytes) + " bytes; budget " + std::to_string(ctx->budget) +
                                ", in use " + std::to_string(ctx->used) + ")");
     }
+    // stream-ordered (de)allocation: a context's growth never waits for the
+    // work of other contexts (cudaFree would synchronize the whole device)
     if (b.p) {
-        cudaStreamSynchronize(ctx->stream);
-        cudaFree(b.p);
+        cudaFreeAsync(b.p, ctx->stream);
         ctx->used -= b.bytes;
         b.p = nullptr;
         b.bytes = 0;
     }
-    cudaError_t e = cudaMalloc(&b.p, grow);
+    cudaError_t e = cudaMallocAsync(&b.p, grow, ctx->stream);
     if (e != cudaSuccess) {
         cudaGetLastError();
         return set_err(ctx, ETRAJ_ERR_OUT_OF_MEMORY, std::string("cudaMalloc ") + name + ": " + cudaGetErrorString(e));
@@ -545,6 +578,7 @@ int launch_integrate(etraj_ctx* ctx, const DJob& J, const InitSoA& soa, const do
     }
     BulkParams B;
     prepare_bulk(J, tmin, B);
+    B.max_n = max_n;
     float4* tab = nullptr;
     ETRAJ_TRY(ensure_t(ctx, "field_table", (size_t)B.n_int * 2, &tab));
     B.table = tab;
@@ -557,7 +591,84 @@ int launch_integrate(etraj_ctx* ctx, const DJob& J, const InitSoA& soa, const do
     return ETRAJ_OK;
 }
 
-int run_job(etraj_ctx* ctx, const etraj_job* job, etraj_result* res) {
+// ---- pinned staging and events, pooled per context ---------------------------------
+int get_pinned(etraj_ctx* ctx, size_t bytes, PinnedBlock* out) {
+    for (size_t i = 0; i < ctx->pinned_pool.size(); ++i) {
+        if (ctx->pinned_pool[i].bytes >= bytes) {
+            *out = ctx->pinned_pool[i];
+            ctx->pinned_pool.erase(ctx->pinned_pool.begin() + (long)i);
+            return ETRAJ_OK;
+        }
+    }
+    void* p = nullptr;
+    cudaError_t e = cudaMallocHost(&p, bytes);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(ctx, ETRAJ_ERR_OUT_OF_MEMORY, std::string("cudaMallocHost: ") + cudaGetErrorString(e));
+    }
+    out->p = p;
+    out->bytes = bytes;
+    return ETRAJ_OK;
+}
+
+void put_pinned(etraj_ctx* ctx, void* p, size_t bytes) {
+    if (!p) return;
+    if (ctx->pinned_pool.size() < 8) ctx->pinned_pool.push_back(PinnedBlock{p, bytes});
+    else cudaFreeHost(p);
+}
+
+cudaEvent_t get_event(etraj_ctx* ctx) {
+    if (!ctx->event_pool.empty()) {
+        cudaEvent_t e = ctx->event_pool.back();
+        ctx->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return e;
+}
+
+void release_job(etraj_ctx* ctx, JobRec& r) {
+    if (r.staged) {
+        put_pinned(ctx, r.pinned, r.pinned_bytes);
+        if (r.ev_start) ctx->event_pool.push_back(r.ev_start);
+        if (r.ev_done) ctx->event_pool.push_back(r.ev_done);
+    }
+    r.pinned = nullptr;
+    r.ev_start = r.ev_done = nullptr;
+}
+
+// Device bytes a job would add to this context's buffers (0 for an invalid job,
+// whose error comes at enqueue).
+size_t plan_growth(etraj_ctx* ctx, const etraj_job* job) {
+    std::string err;
+    if (validate_job(job, err) != ETRAJ_OK) return 0;
+    HostJob H;
+    prepare_job(job, H);
+    Pipeline P;
+    ctx->dry = true;
+    ctx->dry_bytes = 0;
+    alloc_sampling(ctx, H, P);
+    const bool bulk = (job->precision == ETRAJ_PRECISION_FP32_BULK);
+    alloc_outputs(ctx, H.J, H.J.n_total, bulk, P);
+    if (bulk) {
+        BulkParams B;
+        prepare_bulk(H.J, H.t.front(), B);
+        float4* tab = nullptr;
+        ensure_t(ctx, "field_table", (size_t)B.n_int * 2, &tab);
+    }
+    ctx->dry = false;
+    return ctx->dry_bytes;
+}
+
+// Enqueues one whole job on the context's stream: host set-up, copies of the
+// time and momentum samples, every kernel, and the copies of the results.  With
+// r.staged the results go to a pinned block and r.ev_done marks completion;
+// otherwise they go straight to the caller's buffers.
+int enqueue_job(etraj_ctx* ctx, const etraj_job* job, JobRec& r) {
     std::string err;
     int st = validate_job(job, err);
     if (st != ETRAJ_OK) return set_err(ctx, st, err);
@@ -567,12 +678,40 @@ int run_job(etraj_ctx* ctx, const etraj_job* job, etraj_result* res) {
     Pipeline P;
     ETRAJ_TRY(alloc_sampling(ctx, H, P));
     ETRAJ_TRY(alloc_outputs(ctx, J, J.n_total, job->precision == ETRAJ_PRECISION_FP32_BULK, P));
+    r.grid = J.grid;
+    r.coherent = (J.phase != ETRAJ_PHASE_CTMC);
+    const bool want_spec = r.res.momentum_spec != nullptr;
+    const bool want_amp = r.res.amplitude != nullptr && r.coherent;
+    double* dst_sums = r.direct_sums;
+    Counters* dst_cnt = &r.direct_cnt;
+    double* dst_spec = r.res.momentum_spec;
+    double* dst_amp = r.res.amplitude;
+    if (r.staged) {
+        const size_t bytes = 2 * sizeof(double) + sizeof(Counters) + (want_spec ? (size_t)J.grid * 8 : 0) +
+                             (want_amp ? (size_t)J.grid * 16 : 0);
+        PinnedBlock blk;
+        ETRAJ_TRY(get_pinned(ctx, bytes, &blk));
+        r.pinned = blk.p;
+        r.pinned_bytes = blk.bytes;
+        char* base = (char*)blk.p;
+        dst_sums = (double*)base;
+        dst_cnt = (Counters*)(base + 2 * sizeof(double));
+        char* rest = base + 2 * sizeof(double) + sizeof(Counters);
+        dst_spec = want_spec ? (double*)rest : nullptr;
+        dst_amp = want_amp ? (double*)(rest + (want_spec ? (size_t)J.grid * 8 : 0)) : nullptr;
+        r.ev_start = get_event(ctx);
+        r.ev_done = get_event(ctx);
+        if (!r.ev_start || !r.ev_done) return set_err(ctx, ETRAJ_ERR_CUDA, "cudaEventCreate failed");
+    } else {
+        r.ev_start = ctx->ev0;
+        r.ev_done = ctx->ev1;
+    }
     cudaStream_t s = ctx->stream;
     int launches = 0;
     cudaMemcpyAsync(P.t, H.t.data(), H.t.size() * sizeof(double), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(P.kd, H.kd.data(), H.kd.size() * sizeof(double), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(P.kz, H.kz.data(), H.kz.size() * sizeof(double), cudaMemcpyHostToDevice, s);
-    cudaEventRecord(ctx->ev0, s);
+    cudaEventRecord(r.ev_start, s);
     cudaEventRecord(ctx->stage_ev[0], s);
     launches += launch_batch_prepare(J, P.t, P.batches, s);
     if (job->precision == ETRAJ_PRECISION_FP32_BULK && J.method != ETRAJ_SAMPLER_SPA && J.cutoff >= kSample32MinCutoff)
@@ -588,34 +727,61 @@ int run_job(etraj_ctx* ctx, const etraj_job* job, etraj_result* res) {
     launches += launch_deposit(J, P.out, P.count, J.n_total, P.dep, P.spec_re, P.spec_im, P.mspec, P.sums,
                                P.counters, s);
     cudaEventRecord(ctx->stage_ev[6], s);
-    cudaEventRecord(ctx->ev1, s);
     ctx->stage_valid = true;
+    cudaMemcpyAsync(dst_sums, P.sums, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(dst_cnt, P.counters, sizeof(Counters), cudaMemcpyDeviceToHost, s);
+    if (dst_spec) cudaMemcpyAsync(dst_spec, P.mspec, (size_t)J.grid * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (dst_amp) {
+        cudaMemcpy2DAsync(dst_amp, 2 * sizeof(double), P.spec_re, sizeof(double), sizeof(double), (size_t)J.grid,
+                          cudaMemcpyDeviceToHost, s);
+        cudaMemcpy2DAsync(dst_amp + 1, 2 * sizeof(double), P.spec_im, sizeof(double), sizeof(double), (size_t)J.grid,
+                          cudaMemcpyDeviceToHost, s);
+    }
+    cudaEventRecord(r.ev_done, s);
+    r.launches = launches;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_err(ctx, e, "kernel launch");
-    double sums[2] = {0.0, 0.0};
-    Counters cnt{};
-    cudaMemcpyAsync(sums, P.sums, sizeof sums, cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(&cnt, P.counters, sizeof cnt, cudaMemcpyDeviceToHost, s);
-    if (res->momentum_spec)
-        cudaMemcpyAsync(res->momentum_spec, P.mspec, (size_t)J.grid * sizeof(double), cudaMemcpyDeviceToHost, s);
-    if (res->amplitude && J.phase != ETRAJ_PHASE_CTMC) {
-        cudaMemcpy2DAsync(res->amplitude, 2 * sizeof(double), P.spec_re, sizeof(double), sizeof(double),
-                          (size_t)J.grid, cudaMemcpyDeviceToHost, s);
-        cudaMemcpy2DAsync(res->amplitude + 1, 2 * sizeof(double), P.spec_im, sizeof(double), sizeof(double),
-                          (size_t)J.grid, cudaMemcpyDeviceToHost, s);
+    return ETRAJ_OK;
+}
+
+// Completes a job whose ev_done has been reached: fills the caller's result.
+int finish_job(etraj_ctx* ctx, JobRec& r) {
+    const double* sums = r.direct_sums;
+    const Counters* cnt = &r.direct_cnt;
+    if (r.staged) {
+        const char* base = (const char*)r.pinned;
+        sums = (const double*)base;
+        cnt = (const Counters*)(base + 2 * sizeof(double));
+        const char* rest = base + 2 * sizeof(double) + sizeof(Counters);
+        if (r.res.momentum_spec) {
+            std::memcpy(r.res.momentum_spec, rest, (size_t)r.grid * 8);
+            rest += (size_t)r.grid * 8;
+        }
+        if (r.res.amplitude && r.coherent) std::memcpy(r.res.amplitude, rest, (size_t)r.grid * 16);
     }
-    e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return cuda_err(ctx, e, "etraj_run");
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
-    res->ion_prob = sums[0];
-    res->ion_prob_uncollected = sums[1];
-    res->num_effective_traj = (int64_t)cnt.n_eff;
-    res->num_failed_traj = (int64_t)cnt.n_failed;
-    res->num_ionized_traj = (int64_t)cnt.n_ionized;
-    res->num_steps = (int64_t)cnt.n_steps;
-    res->num_kernel_launches = launches;
-    res->elapsed_ms = ms;
+    cudaEventElapsedTime(&ms, r.ev_start, r.ev_done);
+    r.res.ion_prob = sums[0];
+    r.res.ion_prob_uncollected = sums[1];
+    r.res.num_effective_traj = (int64_t)cnt->n_eff;
+    r.res.num_failed_traj = (int64_t)cnt->n_failed;
+    r.res.num_ionized_traj = (int64_t)cnt->n_ionized;
+    r.res.num_steps = (int64_t)cnt->n_steps;
+    r.res.num_kernel_launches = r.launches;
+    r.res.elapsed_ms = ms;
+    release_job(ctx, r);
+    return ETRAJ_OK;
+}
+
+int run_job(etraj_ctx* ctx, const etraj_job* job, etraj_result* res) {
+    JobRec r;
+    r.res = *res;
+    r.staged = false;
+    ETRAJ_TRY(enqueue_job(ctx, job, r));
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "etraj_run");
+    ETRAJ_TRY(finish_job(ctx, r));
+    *res = r.res;
     return ETRAJ_OK;
 }
 
@@ -702,6 +868,16 @@ int etraj_create(etraj_ctx** out, int device, size_t hbm_budget_bytes) {
     etraj_ctx* ctx = new etraj_ctx();
     ctx->device = device;
     cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    {
+        // keep freed stream-ordered memory in this process's pool instead of
+        // returning it at every synchronization (process-local setting)
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+            uint64_t keep = ~0ull;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        cudaGetLastError();
+    }
     size_t free_b = 0, total_b = 0;
     cudaMemGetInfo(&free_b, &total_b);
     const size_t reserve = (size_t)1 << 30;
@@ -725,8 +901,12 @@ void etraj_destroy(etraj_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    for (auto& kv : ctx->jobs) release_job(ctx, kv.second);
+    for (auto& b : ctx->pinned_pool) cudaFreeHost(b.p);
+    for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
     for (auto& kv : ctx->bufs)
-        if (kv.second.p) cudaFree(kv.second.p);
+        if (kv.second.p) cudaFreeAsync(kv.second.p, ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     for (int i = 0; i <= etraj_ctx::kStages; ++i)
@@ -739,6 +919,11 @@ const char* etraj_last_error(const etraj_ctx* ctx) { return ctx ? ctx->err.c_str
 
 int etraj_set_stream(etraj_ctx* ctx, void* cuda_stream) {
     if (!ctx) return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    // buffers are stream-ordered allocations: finish everything queued on the
+    // old stream before the new one may touch them
+    cudaStreamSynchronize(ctx->stream);
     ctx->stream = cuda_stream ? (cudaStream_t)cuda_stream : ctx->own_stream;
     return ETRAJ_OK;
 }
@@ -858,39 +1043,317 @@ int etraj_integrate(etraj_ctx* ctx, const etraj_job* job, int64_t n, const doubl
     return ETRAJ_OK;
 }
 
-// The asynchronous interface runs each submitted job to completion on the
-// context's stream; results are kept until polled.
+// Asynchronous jobs on one context: enqueued on its stream in submission order
+// (the host set-up of the next job overlaps the device work of the previous
+// one); results are staged in pinned memory and copied out at poll/wait.
 int etraj_submit(etraj_ctx* ctx, const etraj_job* job, etraj_result* out, uint64_t* ticket) {
     if (!ctx || !job || !ticket || !out) return ETRAJ_ERR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> lk(ctx->mu);
     cudaSetDevice(ctx->device);
-    uint64_t tk = ctx->next_ticket++;
-    AsyncJob aj;
-    aj.result = *out;
-    aj.status = run_job(ctx, job, &aj.result);
-    aj.error = ctx->err;
-    ctx->jobs[tk] = aj;
+    const uint64_t tk = ctx->next_ticket++;
+    JobRec& r = ctx->jobs[tk];
+    r.res = *out;
+    r.staged = true;
+    r.status = enqueue_job(ctx, job, r);
+    if (r.status != ETRAJ_OK) {
+        r.error = ctx->err;
+        release_job(ctx, r);
+    }
     *ticket = tk;
     return ETRAJ_OK;
 }
 
-int etraj_poll(etraj_ctx* ctx, uint64_t ticket, etraj_result* out) {
-    if (!ctx || !out) return ETRAJ_ERR_INVALID_ARGUMENT;
-    std::lock_guard<std::mutex> lk(ctx->mu);
-    auto it = ctx->jobs.find(ticket);
+namespace {
+// Completes ticket tk of ctx if it is done (blocking when `block`).
+int poll_locked(etraj_ctx* ctx, uint64_t tk, etraj_result* out, bool block) {
+    auto it = ctx->jobs.find(tk);
     if (it == ctx->jobs.end()) return set_err(ctx, ETRAJ_ERR_NOT_FOUND, "unknown ticket");
+    JobRec& r = it->second;
+    int st = r.status;
+    if (st == ETRAJ_OK) {
+        cudaError_t e = block ? cudaEventSynchronize(r.ev_done) : cudaEventQuery(r.ev_done);
+        if (e == cudaErrorNotReady) {
+            cudaGetLastError();
+            return ETRAJ_ERR_NOT_READY;
+        }
+        if (e != cudaSuccess) {
+            st = cuda_err(ctx, e, "etraj_poll");
+            release_job(ctx, r);
+        } else {
+            st = finish_job(ctx, r);
+        }
+    } else {
+        ctx->err = r.error;
+    }
     double* ms = out->momentum_spec;
     double* amp = out->amplitude;
-    *out = it->second.result;
+    *out = r.res;
     out->momentum_spec = ms;
     out->amplitude = amp;
-    int st = it->second.status;
-    if (st != ETRAJ_OK) ctx->err = it->second.error;
     ctx->jobs.erase(it);
     return st;
 }
+}  // namespace
 
-int etraj_wait(etraj_ctx* ctx, uint64_t ticket, etraj_result* out) { return etraj_poll(ctx, ticket, out); }
+int etraj_poll(etraj_ctx* ctx, uint64_t ticket, etraj_result* out) {
+    if (!ctx || !out) return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    return poll_locked(ctx, ticket, out, false);
+}
+
+int etraj_wait(etraj_ctx* ctx, uint64_t ticket, etraj_result* out) {
+    if (!ctx || !out) return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    return poll_locked(ctx, ticket, out, true);
+}
+
+// ---- server: continuous batching of many jobs on one GPU -----------------------------
+// `slots` contexts, each with its own stream and buffers.  A submitted job waits
+// in a FIFO queue until a slot is free and the device bytes it would add fit in
+// the server's HBM budget; it is then enqueued on that slot and overlaps on the
+// device with the jobs of the other slots.  A job's result depends on nothing
+// but the job: no state is shared between slots.
+}  // extern "C"
+
+struct etraj_server {
+    int device = 0;
+    size_t budget = 0;
+    std::vector<etraj_ctx*> slot;
+    std::vector<uint64_t> slot_ticket;  // 0: free
+    struct Req {
+        etraj_job job;
+        etraj_result res;
+        uint64_t ticket;
+    };
+    std::deque<Req> queue;
+    std::map<uint64_t, JobRec> running;
+    std::map<uint64_t, int> running_slot;
+    struct Done {
+        int status;
+        std::string error;
+        etraj_result res;
+    };
+    std::map<uint64_t, Done> done;
+    uint64_t next_ticket = 1;
+    std::string err;
+    std::mutex mu;
+};
+
+namespace {
+
+size_t server_used(const etraj_server* srv) {
+    size_t u = 0;
+    for (const etraj_ctx* c : srv->slot) u += c->used;
+    return u;
+}
+
+void free_ctx_buffers(etraj_ctx* ctx) {
+    for (auto& kv : ctx->bufs)
+        if (kv.second.p) cudaFreeAsync(kv.second.p, ctx->stream);
+    ctx->bufs.clear();
+    ctx->used = 0;
+}
+
+// Retires finished jobs and admits queued ones (server lock held).
+void server_progress(etraj_server* srv) {
+    cudaSetDevice(srv->device);
+    for (size_t i = 0; i < srv->slot.size(); ++i) {
+        const uint64_t tk = srv->slot_ticket[i];
+        if (!tk) continue;
+        etraj_ctx* ctx = srv->slot[i];
+        JobRec& r = srv->running[tk];
+        cudaError_t e = cudaEventQuery(r.ev_done);
+        if (e == cudaErrorNotReady) {
+            cudaGetLastError();
+            continue;
+        }
+        etraj_server::Done d;
+        if (e == cudaSuccess) {
+            d.status = finish_job(ctx, r);
+        } else {
+            d.status = cuda_err(ctx, e, "server job");
+            release_job(ctx, r);
+        }
+        d.error = (d.status == ETRAJ_OK) ? std::string() : ctx->err;
+        d.res = r.res;
+        srv->done[tk] = d;
+        srv->running.erase(tk);
+        srv->running_slot.erase(tk);
+        srv->slot_ticket[i] = 0;
+    }
+    while (!srv->queue.empty()) {
+        int free_slot = -1;
+        for (size_t i = 0; i < srv->slot.size(); ++i)
+            if (!srv->slot_ticket[i]) {
+                free_slot = (int)i;
+                break;
+            }
+        if (free_slot < 0) return;
+        etraj_server::Req& q = srv->queue.front();
+        etraj_ctx* ctx = srv->slot[(size_t)free_slot];
+        size_t growth = plan_growth(ctx, &q.job);
+        if (server_used(srv) + growth > srv->budget) {
+            // give back the buffers of idle slots, then re-plan
+            for (size_t i = 0; i < srv->slot.size(); ++i)
+                if (!srv->slot_ticket[i] && (int)i != free_slot) free_ctx_buffers(srv->slot[i]);
+            growth = plan_growth(ctx, &q.job);
+            if (server_used(srv) + growth > srv->budget) {
+                free_ctx_buffers(ctx);
+                growth = plan_growth(ctx, &q.job);
+            }
+            if (server_used(srv) + growth > srv->budget) {
+                if (!srv->running.empty()) return;  // wait for memory
+                etraj_server::Done d;
+                d.status = ETRAJ_ERR_OUT_OF_MEMORY;
+                d.error = "job needs " + std::to_string(growth) + " device bytes; server budget " +
+                          std::to_string(srv->budget);
+                d.res = q.res;
+                srv->done[q.ticket] = d;
+                srv->queue.pop_front();
+                continue;
+            }
+        }
+        JobRec r;
+        r.res = q.res;
+        r.staged = true;
+        const int st = enqueue_job(ctx, &q.job, r);
+        if (st != ETRAJ_OK) {
+            release_job(ctx, r);
+            etraj_server::Done d;
+            d.status = st;
+            d.error = ctx->err;
+            d.res = q.res;
+            srv->done[q.ticket] = d;
+        } else {
+            srv->running[q.ticket] = r;
+            srv->running_slot[q.ticket] = free_slot;
+            srv->slot_ticket[(size_t)free_slot] = q.ticket;
+        }
+        srv->queue.pop_front();
+    }
+}
+
+// Takes a finished ticket's result (server lock held); NOT_READY while queued or running.
+int server_take(etraj_server* srv, uint64_t tk, etraj_result* out) {
+    auto it = srv->done.find(tk);
+    if (it == srv->done.end()) {
+        if (srv->running.count(tk)) return ETRAJ_ERR_NOT_READY;
+        for (const auto& q : srv->queue)
+            if (q.ticket == tk) return ETRAJ_ERR_NOT_READY;
+        srv->err = "unknown ticket";
+        return ETRAJ_ERR_NOT_FOUND;
+    }
+    double* ms = out->momentum_spec;
+    double* amp = out->amplitude;
+    *out = it->second.res;
+    out->momentum_spec = ms;
+    out->amplitude = amp;
+    const int st = it->second.status;
+    if (st != ETRAJ_OK) srv->err = it->second.error;
+    srv->done.erase(it);
+    return st;
+}
+
+}  // namespace
+
+extern "C" {
+
+int etraj_server_create(etraj_server** out, int device, int slots, size_t hbm_budget_bytes) {
+    if (!out || slots < 1 || slots > 64) return ETRAJ_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    etraj_server* srv = new etraj_server();
+    srv->device = device;
+    for (int i = 0; i < slots; ++i) {
+        etraj_ctx* c = nullptr;
+        const int st = etraj_create(&c, device, hbm_budget_bytes);
+        if (st != ETRAJ_OK) {
+            for (etraj_ctx* d : srv->slot) etraj_destroy(d);
+            delete srv;
+            return st;
+        }
+        srv->slot.push_back(c);
+        srv->slot_ticket.push_back(0);
+    }
+    // the server enforces one budget over all slots
+    srv->budget = srv->slot[0]->budget;
+    for (etraj_ctx* c : srv->slot) c->budget = (size_t)-1 / 2;
+    *out = srv;
+    return ETRAJ_OK;
+}
+
+void etraj_server_destroy(etraj_server* srv) {
+    if (!srv) return;
+    {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        cudaSetDevice(srv->device);
+        for (size_t i = 0; i < srv->slot.size(); ++i) {
+            const uint64_t tk = srv->slot_ticket[i];
+            if (!tk) continue;
+            cudaEventSynchronize(srv->running[tk].ev_done);
+            release_job(srv->slot[i], srv->running[tk]);
+        }
+    }
+    for (etraj_ctx* c : srv->slot) etraj_destroy(c);
+    delete srv;
+}
+
+int etraj_server_submit(etraj_server* srv, const etraj_job* job, etraj_result* out, uint64_t* ticket) {
+    if (!srv || !job || !out || !ticket) return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::string err;
+    const int st = validate_job(job, err);
+    if (st != ETRAJ_OK) {
+        std::lock_guard<std::mutex> lk(srv->mu);
+        srv->err = err;
+        return st;
+    }
+    std::lock_guard<std::mutex> lk(srv->mu);
+    const uint64_t tk = srv->next_ticket++;
+    srv->queue.push_back(etraj_server::Req{*job, *out, tk});
+    server_progress(srv);
+    *ticket = tk;
+    return ETRAJ_OK;
+}
+
+int etraj_server_poll(etraj_server* srv, uint64_t ticket, etraj_result* out) {
+    if (!srv || !out) return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(srv->mu);
+    server_progress(srv);
+    return server_take(srv, ticket, out);
+}
+
+int etraj_server_wait(etraj_server* srv, uint64_t ticket, etraj_result* out, double timeout_s) {
+    if (!srv || !out) return ETRAJ_ERR_INVALID_ARGUMENT;
+    const auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        {
+            std::lock_guard<std::mutex> lk(srv->mu);
+            server_progress(srv);
+            const int st = server_take(srv, ticket, out);
+            if (st != ETRAJ_ERR_NOT_READY) return st;
+        }
+        const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (timeout_s >= 0.0 && el > timeout_s) {
+            std::lock_guard<std::mutex> lk(srv->mu);
+            srv->err = "etraj_server_wait: timed out";
+            return ETRAJ_ERR_TIMEOUT;
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+}
+
+int etraj_server_stats(etraj_server* srv, int64_t* running, int64_t* queued, size_t* hbm_in_use) {
+    if (!srv) return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(srv->mu);
+    server_progress(srv);
+    if (running) *running = (int64_t)srv->running.size();
+    if (queued) *queued = (int64_t)srv->queue.size();
+    if (hbm_in_use) *hbm_in_use = server_used(srv);
+    return ETRAJ_OK;
+}
+
+const char* etraj_server_last_error(const etraj_server* srv) { return srv ? srv->err.c_str() : "no server"; }
 
 int etraj_stage_times(etraj_ctx* ctx, double* ms, int n) {
     if (!ctx || !ms) return 0;

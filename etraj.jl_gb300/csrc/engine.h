@@ -135,6 +135,7 @@ struct BulkParams {
     int n_int;          // field-table intervals
     int table_in_smem;  // 1: stage the table in shared memory
     int threads, blocks_per_sm, refill_min;
+    int64_t max_n;      // upper bound of the electron count (grid sizing)
     const float4* table;
     double T0, inv_h_d, t_final;
     float h, inv_h, rtol;

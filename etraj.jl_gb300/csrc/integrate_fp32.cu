@@ -618,7 +618,14 @@ int launch_bulk_t(const BulkParams& P, InitSoA soa, const double* t, const int64
     const size_t smem = P.table_in_smem ? (size_t)P.n_int * 2 * sizeof(float4) : 0;
     auto kern = k_integrate_bulk<DIM, PHASE, TGT>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    const int blocks = sm_count * P.blocks_per_sm;
+    // persistent grid, but no more blocks than the job can keep busy (at least ~4
+    // electrons per lane): a block holds its SM's registers until its last warp
+    // exits, so an oversized grid for a small job would fence off the whole GPU
+    // from concurrent jobs for as long as its slowest trajectory runs
+    const int64_t lanes_per_block = (int64_t)P.threads * 4;
+    const int64_t want = (P.max_n + lanes_per_block - 1) / lanes_per_block;
+    const int64_t cap = (int64_t)sm_count * P.blocks_per_sm;
+    const int blocks = (int)(want < 1 ? 1 : (want < cap ? want : cap));
     kern<<<blocks, P.threads, smem, s>>>(P, soa, t, idx, count, queue, out);
     return 1;
 }

@@ -207,6 +207,79 @@ class Engine:
         self._check(self.lib.etraj_wait(self.ctx, ticket, C.byref(res)))
 
 
+class Server:
+    """An etraj_server: continuous batching of many jobs on one GPU.  Jobs are
+    queued first-in first-out and admitted to `slots` contexts (own stream, own
+    buffers) as slots and HBM free up; their work overlaps on the device."""
+
+    def __init__(self, device=0, slots=4, hbm_budget_bytes=0):
+        self.lib = abi.load_library()
+        self.srv = C.c_void_p()
+        st = self.lib.etraj_server_create(C.byref(self.srv), device, slots, hbm_budget_bytes)
+        if st != abi.OK:
+            raise EtrajError(st, "etraj_server_create failed on device %d" % device)
+        self._pending = {}
+
+    def close(self):
+        if self.srv:
+            self.lib.etraj_server_destroy(self.srv)
+            self.srv = C.c_void_p()
+            self._pending.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, st):
+        if st != abi.OK:
+            msg = self.lib.etraj_server_last_error(self.srv)
+            raise EtrajError(st, msg.decode() if msg else "")
+
+    def submit(self, job, want_spectrum=True, want_amplitude=False):
+        """Queue a copy of `job`; returns its ticket.  The output arrays are held
+        here until the ticket is retired by poll or wait."""
+        res = abi.Result()
+        spec = amp = None
+        if want_spectrum:
+            spec = np.zeros(job.grid_size, dtype=np.float64)
+            res.momentum_spec = abi.dptr(spec)
+        if want_amplitude and job.traj_phase_method != abi.PHASE_CTMC:
+            amp = np.zeros(2 * job.grid_size, dtype=np.float64)
+            res.amplitude = abi.dptr(amp)
+        t = C.c_uint64()
+        self._check(self.lib.etraj_server_submit(self.srv, C.byref(job), C.byref(res), C.byref(t)))
+        self._pending[t.value] = (res, spec, amp)
+        return t.value
+
+    def _finish(self, ticket, st):
+        res, spec, amp = self._pending.pop(ticket)
+        self._check(st)
+        return res, spec, amp
+
+    def poll(self, ticket):
+        """(result, spectrum, amplitude) when the job is done, else None."""
+        res = self._pending[ticket][0]
+        st = self.lib.etraj_server_poll(self.srv, ticket, C.byref(res))
+        if st == abi.ERR_NOT_READY:
+            return None
+        return self._finish(ticket, st)
+
+    def wait(self, ticket, timeout=-1.0):
+        res = self._pending[ticket][0]
+        st = self.lib.etraj_server_wait(self.srv, ticket, C.byref(res), float(timeout))
+        if st == abi.ERR_TIMEOUT:
+            raise EtrajError(st, "timed out")
+        return self._finish(ticket, st)
+
+    def stats(self):
+        """(running, queued, device bytes held by the slots)."""
+        r, q, m = C.c_int64(), C.c_int64(), C.c_size_t()
+        self._check(self.lib.etraj_server_stats(self.srv, C.byref(r), C.byref(q), C.byref(m)))
+        return r.value, q.value, m.value
+
+
 _default_engine = None
 
 

@@ -203,12 +203,43 @@ int etraj_sample_all(etraj_ctx* ctx, const etraj_job* job,
 int etraj_integrate(etraj_ctx* ctx, const etraj_job* job, int64_t n, const double* init,
                     double* final_state, int32_t* status, int32_t* steps);
 
-/* ---- asynchronous jobs (serving loop) ----------------------------------------
- * etraj_submit queues a job; `out` supplies the caller-owned output pointers
- * (momentum_spec, amplitude), which must stay valid until etraj_poll or
- * etraj_wait has returned ETRAJ_OK for the ticket.  etraj_poll returns
- * ETRAJ_ERR_NOT_READY while the job runs; both fill the scalars of `out`
- * (its pointers are left as they are) and release the ticket. */
+/* ---- asynchronous jobs on one context -----------------------------------------
+ * No counterpart in the reference.  etraj_submit enqueues a job on the
+ * context's stream and returns; jobs run in submission order, and the host
+ * set-up of one overlaps the device work of the one before.  `out` supplies the
+ * caller-owned output pointers (momentum_spec, amplitude), which must stay
+ * valid until etraj_poll or etraj_wait has returned for the ticket.
+ * etraj_poll returns ETRAJ_ERR_NOT_READY while the job runs; poll and wait
+ * fill the scalars of `out` (its pointers are left as they are), copy the
+ * spectra out of the library's pinned staging and release the ticket.  A job
+ * that fails its checks reports the error at poll/wait. */
+int etraj_submit(etraj_ctx* ctx, const etraj_job* job, etraj_result* out, uint64_t* ticket);
+int etraj_poll(etraj_ctx* ctx, uint64_t ticket, etraj_result* out);
+int etraj_wait(etraj_ctx* ctx, uint64_t ticket, etraj_result* out);
+
+/* ---- serving: continuous batching on one GPU ---------------------------------
+ * No counterpart in the reference, which runs one job per call.  A server owns
+ * `slots` (1..64) contexts, each with its own stream and device buffers, and
+ * one HBM budget over all of them (0 = free memory less 1 GiB).  A submitted
+ * job is checked (errors return at once), queued first-in first-out, and
+ * enqueued as soon as a slot is free and the device bytes it would add fit in
+ * the budget (idle slots give their buffers back when memory is short; a job
+ * that cannot fit even on an empty server fails with ETRAJ_ERR_OUT_OF_MEMORY).
+ * Jobs on different slots overlap on the device; nothing is shared between
+ * slots, so a job's result is the same alone and in any mix.  Every call
+ * retires finished jobs and admits queued ones.  etraj_server_poll returns
+ * ETRAJ_ERR_NOT_READY while the job is queued or running; etraj_server_wait
+ * blocks up to timeout_s seconds (negative: no limit), then returns
+ * ETRAJ_ERR_TIMEOUT.  Output pointers follow the rules of etraj_submit. */
+typedef struct etraj_server etraj_server;
+int etraj_server_create(etraj_server** out, int device, int slots, size_t hbm_budget_bytes);
+void etraj_server_destroy(etraj_server* srv);
+int etraj_server_submit(etraj_server* srv, const etraj_job* job, etraj_result* out, uint64_t* ticket);
+int etraj_server_poll(etraj_server* srv, uint64_t ticket, etraj_result* out);
+int etraj_server_wait(etraj_server* srv, uint64_t ticket, etraj_result* out, double timeout_s);
+int etraj_server_stats(etraj_server* srv, int64_t* running, int64_t* queued, size_t* hbm_in_use);
+const char* etraj_server_last_error(const etraj_server* srv);
+
 /* ---- diagnostics ----------------------------------------------------------------
  * Device time (ms) of the stages of the last etraj_run on this context: sampling,
  * compaction, field table, integrator, collection, deposit.  Writes up to n
@@ -240,10 +271,6 @@ int etraj_stage_times(etraj_ctx* ctx, double* ms, int n);
 int etraj_deposit_noalloc(int64_t n, const uint32_t* key, const double* c_re, const double* c_im,
                           int64_t grid, int coherent, double* spec_re, double* spec_im,
                           double* momentum_spec, void* cuda_stream);
-
-int etraj_submit(etraj_ctx* ctx, const etraj_job* job, etraj_result* out, uint64_t* ticket);
-int etraj_poll(etraj_ctx* ctx, uint64_t ticket, etraj_result* out);
-int etraj_wait(etraj_ctx* ctx, uint64_t ticket, etraj_result* out);
 
 #ifdef __cplusplus
 }
