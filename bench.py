@@ -243,6 +243,8 @@ def main():
                     help="time samples (default: the workload's full size)")
     ap.add_argument("--precision", default="fp32_bulk", choices=["fp32_bulk", "fp64"],
                     help="path timed as `value` (fp64 profiles the plain kernel)")
+    ap.add_argument("--no-multi-instance", action="store_true",
+                    help="skip the 64-instance batched intensity scan")
     ap.add_argument("--no-serving", action="store_true",
                     help="skip the serving-loop replay (512 Poisson arrivals at 20/s)")
     ap.add_argument("--no-fp64-compare", action="store_true",
@@ -361,6 +363,8 @@ def main():
             "clocks": clocks,
             "wall_s": t_wall,
         }
+        if not args.no_multi_instance and world == 1:
+            line["multi_instance"] = multi_instance_report(eng)
         if not args.no_serving and world == 1:
             line["serving"] = serving_report()
         if not args.no_cpu_baseline:
@@ -501,6 +505,56 @@ def serving_report(n=512, rate=20.0, slots=8, fp64_seconds=20.0):
                                    "mean_service_ms": float(np.mean(fp64_ms)),
                                    "offered_load_vs_capacity": float(rate * np.mean(fp64_ms) / 1e3)},
             "workload": serving_requests.__doc__.split("\n\n")[0].replace("\n    ", " ")}
+
+
+def multi_instance_jobs(n=64, seed=7):
+    """Focal-volume intensity scan: n instances of Ar, Gaussian 800 nm (8 cycles
+    FWHM) linear polarization, peak intensity log-U(5e13, 4e14) W/cm^2,
+    log-U(1e4, 2e6) ADK Monte-Carlo candidates in 3D (kd, kz), SCTS, each with
+    a 500 x 500 x 1 grid +-2 a.u.; weights I^-1.5 (a focal volume's dV/dI shape)."""
+    rng = np.random.default_rng(seed)
+    jobs, ints = [], []
+    for i in range(n):
+        inten = float(np.exp(rng.uniform(np.log(5e13), np.log(4e14))))
+        count = float(np.exp(rng.uniform(np.log(1e4), np.log(2e6))))
+        T = 2 * np.pi * 800.0 / 45.563352525
+        laser = et.GaussianLaser(peak_int=inten, wave_len=800.0, FWHM_duration=8 * T, ellip=0.0)
+        fw = 8 * T
+        jobs.append(et.make_job(init_cond_method="ADK", laser=laser, target=et.get_atom("Ar"), dimension=3,
+                                sample_t_intv=(-1.5 * fw, 1.5 * fw), sample_t_num=max(10, int(round(count / 1000))),
+                                traj_t_final=1.5 * fw + 2 * T, final_p_max=(2.0, 2.0, 1.0),
+                                final_p_num=(500, 500, 1), sample_monte_carlo=True, mc_kt_num=1000,
+                                mc_kd_max=1.0, mc_kz_max=1.0, traj_phase_method="SCTS", seed=1000 + i,
+                                precision="fp32_bulk"))
+        ints.append(inten)
+    ints = np.array(ints)
+    return jobs, (ints / ints.max()) ** -1.5
+
+
+def multi_instance_report(eng):
+    """The 64-instance scan as one batch (one integrator launch whose work stealing
+    spans every instance, plus the weighted PMD) against the same 64 jobs run one
+    after another; device times from the library's events."""
+    jobs, w = multi_instance_jobs()
+    eng.run_batch(jobs[:4])  # warm-up
+    t0 = time.perf_counter()
+    outs, wsum = eng.run_batch(jobs, want_spectrum=True, weights=w)
+    wall_batch = time.perf_counter() - t0
+    eff = sum(r.num_effective_traj for r, _, _ in outs)
+    dev_batch = outs[0][0].elapsed_ms
+    t0 = time.perf_counter()
+    dev_seq = 0.0
+    for job in jobs:
+        r, _, _ = eng.run(job, want_spectrum=True)
+        dev_seq += r.elapsed_ms
+    wall_seq = time.perf_counter() - t0
+    return {"instances": len(jobs), "effective_trajectories": int(eff),
+            "batched": {"device_ms": dev_batch, "wall_ms": 1e3 * wall_batch,
+                        "trajectories_per_s": eff / (dev_batch / 1e3), "kernel_launches": outs[0][0].num_kernel_launches},
+            "one_job_at_a_time": {"device_ms": dev_seq, "wall_ms": 1e3 * wall_seq,
+                                  "trajectories_per_s": eff / (dev_seq / 1e3)},
+            "weighted_pmd_sum": float(wsum.sum()),
+            "workload": multi_instance_jobs.__doc__.replace("\n    ", " ")}
 
 
 STAGES = ("sample", "compact", "field_table", "integrate", "collect", "deposit")

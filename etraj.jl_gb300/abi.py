@@ -114,6 +114,7 @@ SIGNATURES = [
     ("etraj_submit", C.c_int, [C.c_void_p, C.POINTER(Job), C.POINTER(Result), C.POINTER(C.c_uint64)]),
     ("etraj_poll", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(Result)]),
     ("etraj_wait", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(Result)]),
+    ("etraj_run_batch", C.c_int, [C.c_void_p, C.POINTER(Job), C.c_int, C.POINTER(Result), _DP, _DP]),
     ("etraj_server_create", C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_size_t]),
     ("etraj_server_destroy", None, [C.c_void_p]),
     ("etraj_server_submit", C.c_int, [C.c_void_p, C.POINTER(Job), C.POINTER(Result), C.POINTER(C.c_uint64)]),

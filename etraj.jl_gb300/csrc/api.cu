@@ -785,6 +785,189 @@ int run_job(etraj_ctx* ctx, const etraj_job* job, etraj_result* res) {
     return ETRAJ_OK;
 }
 
+// ---- multi-instance batch: many jobs in one integrator launch ------------------------
+// The instances' time samples, candidates and field tables are concatenated;
+// sampling runs per instance, then one compaction, one bulk-integrator launch
+// whose work stealing spans every instance, one collection, one deposit into
+// an instance-major grid, and per-instance reductions.  Every per-instance
+// result equals that of the same job run alone.
+int run_batch(etraj_ctx* ctx, const etraj_job* jobs, int n, etraj_result* res, const double* weights,
+              double* wspec) {
+    if (!jobs || !res || n < 1 || n > kMaxInstances)
+        return set_err(ctx, ETRAJ_ERR_INVALID_ARGUMENT, "etraj_run_batch: 1 to 64 jobs");
+    if ((weights == nullptr) != (wspec == nullptr))
+        return set_err(ctx, ETRAJ_ERR_INVALID_ARGUMENT, "etraj_run_batch: weights and weighted_spec go together");
+    const etraj_job& j0 = jobs[0];
+    for (int i = 0; i < n; ++i) {
+        std::string err;
+        const int st = validate_job(&jobs[i], err);
+        if (st != ETRAJ_OK) return set_err(ctx, st, "job " + std::to_string(i) + ": " + err);
+        const etraj_job& ji = jobs[i];
+        bool same = ji.precision == ETRAJ_PRECISION_FP32_BULK && ji.dimension == j0.dimension &&
+                    ji.traj_phase_method == j0.traj_phase_method && ji.traj_rtol == j0.traj_rtol &&
+                    std::memcmp(&ji.target, &j0.target, sizeof ji.target) == 0;
+        for (int d = 0; d < 3; ++d)
+            same = same && ji.final_p_num[d] == j0.final_p_num[d] && ji.final_p_max[d] == j0.final_p_max[d];
+        if (!same)
+            return set_err(ctx, ETRAJ_ERR_INVALID_ARGUMENT,
+                           "etraj_run_batch: job " + std::to_string(i) +
+                               " differs from job 0 in precision (must be FP32_BULK), dimension, phase method, "
+                               "rtol, target or momentum grid");
+    }
+    std::vector<HostJob> H((size_t)n);
+    for (int i = 0; i < n; ++i) prepare_job(&jobs[i], H[(size_t)i]);
+    const int64_t grid1 = H[0].J.grid;
+    if ((int64_t)n * grid1 >= (int64_t)0xFFFFFFFFll)
+        return set_err(ctx, ETRAJ_ERR_INVALID_ARGUMENT, "etraj_run_batch: instances x grid >= 2^32 bins");
+    std::vector<int64_t> toff(n + 1, 0), koff(n + 1, 0), zoff(n + 1, 0), coff(n + 1, 0), tab_off(n + 1, 0);
+    std::vector<BulkParams> B((size_t)n);
+    for (int i = 0; i < n; ++i) {
+        const HostJob& h = H[(size_t)i];
+        toff[i + 1] = toff[i] + (int64_t)h.t.size();
+        koff[i + 1] = koff[i] + (int64_t)h.kd.size();
+        zoff[i + 1] = zoff[i] + (int64_t)h.kz.size();
+        coff[i + 1] = coff[i] + h.J.n_total;
+        prepare_bulk(h.J, h.t.front(), B[(size_t)i]);
+        tab_off[i + 1] = tab_off[i] + 2 * (int64_t)B[(size_t)i].n_int;
+    }
+    const int64_t N = coff[n];
+    if (toff[n] >= (int64_t)1 << 31)
+        return set_err(ctx, ETRAJ_ERR_INVALID_ARGUMENT, "etraj_run_batch: more than 2^31 time samples");
+    std::vector<double> t_all((size_t)toff[n]), kd_all((size_t)koff[n]), kz_all((size_t)zoff[n]);
+    for (int i = 0; i < n; ++i) {
+        const HostJob& h = H[(size_t)i];
+        std::copy(h.t.begin(), h.t.end(), t_all.begin() + toff[i]);
+        std::copy(h.kd.begin(), h.kd.end(), kd_all.begin() + koff[i]);
+        std::copy(h.kz.begin(), h.kz.end(), kz_all.begin() + zoff[i]);
+    }
+    // buffers (the single-job names, sized for the whole batch)
+    Pipeline P;
+    DJob Jgrid = H[0].J;
+    Jgrid.grid = (int64_t)n * grid1;
+    HostJob Hsz;
+    Hsz.J = Jgrid;
+    Hsz.J.n_total = N;
+    Hsz.J.n_t = toff[n];
+    Hsz.t = t_all;
+    Hsz.kd = kd_all;
+    Hsz.kz = kz_all;
+    ETRAJ_TRY(alloc_sampling(ctx, Hsz, P));
+    ETRAJ_TRY(alloc_outputs(ctx, Jgrid, N, true, P));
+    float4* tab = nullptr;
+    BulkInst* d_inst = nullptr;
+    int64_t* d_seg = nullptr;
+    double *d_scr = nullptr, *d_isums = nullptr, *d_w = nullptr, *d_wout = nullptr;
+    Counters* d_icnt = nullptr;
+    ETRAJ_TRY(ensure_t(ctx, "field_table", (size_t)tab_off[n], &tab));
+    ETRAJ_TRY(ensure_t(ctx, "batch.inst", (size_t)n, &d_inst));
+    ETRAJ_TRY(ensure_t(ctx, "batch.seg", (size_t)n + 1, &d_seg));
+    ETRAJ_TRY(ensure_t(ctx, "batch.scratch", instance_scratch_doubles(N, n), &d_scr));
+    ETRAJ_TRY(ensure_t(ctx, "batch.sums", (size_t)2 * n, &d_isums));
+    ETRAJ_TRY(ensure_t(ctx, "batch.counters", (size_t)n, &d_icnt));
+    if (weights) {
+        ETRAJ_TRY(ensure_t(ctx, "batch.w", (size_t)n, &d_w));
+        ETRAJ_TRY(ensure_t(ctx, "batch.wout", (size_t)grid1, &d_wout));
+    }
+    std::vector<BulkInst> inst((size_t)n);
+    for (int i = 0; i < n; ++i) {
+        const BulkParams& b = B[(size_t)i];
+        BulkInst& q = inst[(size_t)i];
+        q.table = tab + tab_off[i];
+        q.cand_end = coff[i + 1];
+        q.T0 = b.T0;
+        q.inv_h_d = b.inv_h_d;
+        q.t_final = b.t_final;
+        q.t_off = (int)toff[i];
+        q.n_int = b.n_int;
+        q.nf = b.nf;
+        q.ff = b.ff;
+        q.h = b.h;
+        q.inv_h = b.inv_h;
+    }
+    cudaStream_t s = ctx->stream;
+    int launches = 0;
+    cudaMemcpyAsync(P.t, t_all.data(), t_all.size() * 8, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(P.kd, kd_all.data(), kd_all.size() * 8, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(P.kz, kz_all.data(), kz_all.size() * 8, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_inst, inst.data(), inst.size() * sizeof(BulkInst), cudaMemcpyHostToDevice, s);
+    if (weights) cudaMemcpyAsync(d_w, weights, (size_t)n * 8, cudaMemcpyHostToDevice, s);
+    cudaEventRecord(ctx->ev0, s);
+    cudaEventRecord(ctx->stage_ev[0], s);
+    for (int i = 0; i < n; ++i) {
+        const DJob& J = H[(size_t)i].J;
+        DBatch* bat = P.batches + toff[i];
+        launches += launch_batch_prepare(J, P.t + toff[i], bat, s);
+        InitSoA so = P.soa;
+        const int64_t c = coff[i];
+        so.x += c; so.y += c; so.kx += c; so.ky += c; so.kz += c; so.rate += c; so.batch += c;
+        if (so.phase) so.phase += c;
+        if (J.method != ETRAJ_SAMPLER_SPA && J.cutoff >= kSample32MinCutoff)
+            launches += launch_sample32_range(J, 0, J.n_t, P.kd + koff[i], P.kz + zoff[i], bat, so, P.flag + c,
+                                              ctx->sm_count, s);
+        else
+            launches += launch_sample_range(J, 0, J.n_t, P.kd + koff[i], P.kz + zoff[i], bat, so, P.flag + c,
+                                            ctx->sm_count, s);
+    }
+    cudaEventRecord(ctx->stage_ev[1], s);
+    launches += launch_compact(P.flag, N, P.idx, P.block_sums, compact_blocks(N) + 1, P.count, s);
+    cudaEventRecord(ctx->stage_ev[2], s);
+    for (int i = 0; i < n; ++i) {
+        const BulkParams& b = B[(size_t)i];
+        launches += launch_field_table(H[(size_t)i].J, b.T0, 1.0 / b.inv_h_d, b.n_int, tab + tab_off[i], s);
+    }
+    BulkParams M = B[0];
+    M.table = nullptr;
+    M.table_in_smem = 0;
+    M.max_n = N;
+    M.inst = d_inst;
+    M.n_inst = n;
+    cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), s);
+    cudaEventRecord(ctx->stage_ev[3], s);
+    launches += launch_integrate_bulk(M, P.soa, P.t, P.idx, P.count, P.work, P.out, ctx->sm_count, s);
+    cudaEventRecord(ctx->stage_ev[4], s);
+    launches += launch_collect_bulk(H[0].J, P.soa, P.t, P.idx, P.count, P.out, N, ctx->sm_count, s, d_inst, n);
+    cudaEventRecord(ctx->stage_ev[5], s);
+    launches += launch_deposit(Jgrid, P.out, P.count, N, P.dep, P.spec_re, P.spec_im, P.mspec, P.sums, P.counters, s);
+    launches += launch_instance_reductions(P.out, P.idx, P.count, d_inst, n, d_seg, d_scr, d_isums, d_icnt, s);
+    if (weights) launches += launch_weighted_sum(P.mspec, n, grid1, d_w, d_wout, s);
+    cudaEventRecord(ctx->stage_ev[6], s);
+    cudaEventRecord(ctx->ev1, s);
+    ctx->stage_valid = true;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_err(ctx, e, "batch launch");
+    std::vector<double> isums((size_t)2 * n);
+    std::vector<Counters> icnt((size_t)n);
+    cudaMemcpyAsync(isums.data(), d_isums, isums.size() * 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(icnt.data(), d_icnt, icnt.size() * sizeof(Counters), cudaMemcpyDeviceToHost, s);
+    const bool coherent = (H[0].J.phase != ETRAJ_PHASE_CTMC);
+    for (int i = 0; i < n; ++i) {
+        const int64_t o = (int64_t)i * grid1;
+        if (res[i].momentum_spec)
+            cudaMemcpyAsync(res[i].momentum_spec, P.mspec + o, (size_t)grid1 * 8, cudaMemcpyDeviceToHost, s);
+        if (res[i].amplitude && coherent) {
+            cudaMemcpy2DAsync(res[i].amplitude, 16, P.spec_re + o, 8, 8, (size_t)grid1, cudaMemcpyDeviceToHost, s);
+            cudaMemcpy2DAsync(res[i].amplitude + 1, 16, P.spec_im + o, 8, 8, (size_t)grid1, cudaMemcpyDeviceToHost, s);
+        }
+    }
+    if (weights) cudaMemcpyAsync(wspec, d_wout, (size_t)grid1 * 8, cudaMemcpyDeviceToHost, s);
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "etraj_run_batch");
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    for (int i = 0; i < n; ++i) {
+        etraj_result& r = res[i];
+        r.ion_prob = isums[(size_t)2 * i];
+        r.ion_prob_uncollected = isums[(size_t)2 * i + 1];
+        r.num_effective_traj = (int64_t)icnt[(size_t)i].n_eff;
+        r.num_failed_traj = (int64_t)icnt[(size_t)i].n_failed;
+        r.num_ionized_traj = (int64_t)icnt[(size_t)i].n_ionized;
+        r.num_steps = (int64_t)icnt[(size_t)i].n_steps;
+        r.num_kernel_launches = launches;
+        r.elapsed_ms = ms;
+    }
+    return ETRAJ_OK;
+}
+
 // Copies sampled candidates back and assembles the reference's `init` columns.
 int gather_rows(etraj_ctx* ctx, const HostJob& H, const Pipeline& P, int64_t g0, int64_t ng, double* init,
                 int64_t capacity, int64_t* count) {
@@ -1354,6 +1537,14 @@ int etraj_server_stats(etraj_server* srv, int64_t* running, int64_t* queued, siz
 }
 
 const char* etraj_server_last_error(const etraj_server* srv) { return srv ? srv->err.c_str() : "no server"; }
+
+int etraj_run_batch(etraj_ctx* ctx, const etraj_job* jobs, int n_jobs, etraj_result* results,
+                    const double* weights, double* weighted_spec) {
+    if (!ctx) return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    return run_batch(ctx, jobs, n_jobs, results, weights, weighted_spec);
+}
 
 int etraj_stage_times(etraj_ctx* ctx, double* ms, int n) {
     if (!ctx || !ms) return 0;

@@ -422,6 +422,186 @@ int launch_deposit(const DJob& J, const TrajOut& out, const unsigned long long* 
     return launches;
 }
 
+// ---- per-instance results of a multi-instance launch ---------------------------------
+// Survivors are ordered by candidate index and the instances' candidates are
+// concatenated, so each instance's survivors form one segment [seg[i], seg[i+1]).
+
+namespace {
+
+__global__ void k_inst_segments(const int64_t* __restrict__ idx, const unsigned long long* __restrict__ count,
+                                const BulkInst* __restrict__ inst, int n_inst, int64_t* __restrict__ seg) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > n_inst) return;
+    const int64_t n = (int64_t)*count;
+    if (i == 0) {
+        seg[0] = 0;
+        return;
+    }
+    // first survivor whose candidate index is >= cand_end of instance i-1
+    const int64_t key = inst[i - 1].cand_end;
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        const int64_t mid = (lo + hi) >> 1;
+        if (idx[mid] < key) lo = mid + 1;
+        else hi = mid;
+    }
+    seg[i] = lo;
+}
+
+// The canonical ion_prob tree (k_tree_level's node rule) over one instance's
+// segment per block, levels ping-ponging between two scratch regions.
+__global__ void __launch_bounds__(256)
+k_inst_tree(const double* __restrict__ wa, const double* __restrict__ wb, const int64_t* __restrict__ seg,
+            double* __restrict__ scratch, int64_t region, double* __restrict__ sums) {
+    const int inst = blockIdx.x;
+    const int64_t b0 = seg[inst], len = seg[inst + 1] - b0;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // per instance: 4 arrays of ceil(len/256)+1 doubles (a, b in each of two
+    // buffers) from 4 * (ceil(b0/256) + 2 inst); since ceil(x) + ceil(y) <=
+    // ceil(x+y) + 1 the regions of consecutive instances do not overlap
+    double* bufA = scratch + 4 * (((b0 + 255) >> 8) + 2 * (int64_t)inst);
+    (void)region;
+    const double* ina = wa + b0;
+    const double* inb = wb + b0;
+    double* outa = bufA;
+    double* outb = bufA + ((len + 255) >> 8) + 1;
+    double* alta = outb + ((len + 255) >> 8) + 1;
+    double* altb = alta + ((len + 255) >> 8) + 1;
+    int64_t m = len;
+    if (m == 0) {
+        if (threadIdx.x == 0) {
+            sums[2 * inst] = 0.0;
+            sums[2 * inst + 1] = 0.0;
+        }
+        return;
+    }
+    for (;;) {
+        const int64_t nb = (m + 255) >> 8;
+        for (int64_t node = warp; node < nb; node += (int64_t)(blockDim.x >> 5)) {
+            const int64_t base = node * 256 + 8 * lane;
+            double va[8], vb[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const bool in = base + j < m;
+                va[j] = in ? ina[base + j] : 0.0;
+                vb[j] = in ? inb[base + j] : 0.0;
+            }
+#pragma unroll
+            for (int w = 4; w >= 1; w >>= 1) {
+#pragma unroll
+                for (int j = 0; j < w; ++j) {
+                    va[j] = va[2 * j] + va[2 * j + 1];
+                    vb[j] = vb[2 * j] + vb[2 * j + 1];
+                }
+            }
+            double sa = va[0], sb = vb[0];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const double ra = __shfl_down_sync(0xffffffffu, sa, o);
+                const double rb = __shfl_down_sync(0xffffffffu, sb, o);
+                if ((lane & (2 * o - 1)) == 0) {
+                    sa = sa + ra;
+                    sb = sb + rb;
+                }
+            }
+            if (lane == 0) {
+                outa[node] = sa;
+                outb[node] = sb;
+            }
+        }
+        __syncthreads();
+        if (nb == 1) break;
+        m = nb;
+        ina = outa;
+        inb = outb;
+        double* ta = alta;
+        double* tb = altb;
+        alta = outa;
+        altb = outb;
+        outa = ta;
+        outb = tb;
+    }
+    if (threadIdx.x == 0) {
+        sums[2 * inst] = outa[0];
+        sums[2 * inst + 1] = outb[0];
+    }
+}
+
+__global__ void __launch_bounds__(256)
+k_inst_counters(const int32_t* __restrict__ status, const int32_t* __restrict__ steps,
+                const int64_t* __restrict__ seg, Counters* __restrict__ c) {
+    const int inst = blockIdx.x;
+    const int64_t b0 = seg[inst], b1 = seg[inst + 1];
+    unsigned long long f = 0, io = 0, st = 0;
+    for (int64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
+        const int32_t v = status[i];
+        f += ((v & 0xff) != 0) ? 1ull : 0ull;
+        io += (v & 0x100) ? 1ull : 0ull;
+        st += (unsigned long long)steps[i];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        f += __shfl_down_sync(0xffffffffu, f, o);
+        io += __shfl_down_sync(0xffffffffu, io, o);
+        st += __shfl_down_sync(0xffffffffu, st, o);
+    }
+    __shared__ unsigned long long part[3][8];
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        part[0][w] = f;
+        part[1][w] = io;
+        part[2][w] = st;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long a = 0, b = 0, d = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) {
+            a += part[0][k];
+            b += part[1][k];
+            d += part[2][k];
+        }
+        c[inst].n_eff = (unsigned long long)(b1 - b0);
+        c[inst].n_failed = a;
+        c[inst].n_ionized = b;
+        c[inst].n_steps = d;
+    }
+}
+
+// out[b] = sum_i w[i] * mspec[i * grid + b], instances in order from 0.0
+__global__ void k_weighted_sum(const double* __restrict__ mspec, int n_inst, int64_t grid,
+                               const double* __restrict__ w, double* __restrict__ out) {
+    for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < grid;
+         b += (int64_t)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+        for (int i = 0; i < n_inst; ++i) acc = acc + w[i] * mspec[(int64_t)i * grid + b];
+        out[b] = acc;
+    }
+}
+
+}  // namespace
+
+size_t instance_scratch_doubles(int64_t max_n, int n_inst) {
+    // regions up to 4 * (ceil(n/256) + 2 n_inst) (see k_inst_tree)
+    return (size_t)4 * (size_t)(((max_n + 255) >> 8) + 2 * (int64_t)n_inst + 2);
+}
+
+int launch_instance_reductions(const TrajOut& out, const int64_t* idx, const unsigned long long* count,
+                               const BulkInst* inst, int n_inst, int64_t* seg, double* scratch,
+                               double* sums, Counters* counters, cudaStream_t s) {
+    k_inst_segments<<<1, 128, 0, s>>>(idx, count, inst, n_inst, seg);
+    k_inst_tree<<<n_inst, 256, 0, s>>>(out.w_ion, out.w_unc, seg, scratch, 0, sums);
+    k_inst_counters<<<n_inst, 256, 0, s>>>(out.status, out.steps, seg, counters);
+    return 3;
+}
+
+int launch_weighted_sum(const double* mspec, int n_inst, int64_t grid, const double* w, double* out,
+                        cudaStream_t s) {
+    int64_t blocks = (grid + 255) / 256;
+    if (blocks > 152 * 8) blocks = 152 * 8;
+    k_weighted_sum<<<(int)(blocks > 0 ? blocks : 1), 256, 0, s>>>(mspec, n_inst, grid, w, out);
+    return 1;
+}
+
 }  // namespace etraj
 
 // ---- deposit without allocation ------------------------------------------------------

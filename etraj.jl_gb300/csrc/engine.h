@@ -129,6 +129,18 @@ int launch_collect_fp64(const DJob& J, InitSoA soa, const double* t, const int64
                         const unsigned long long* count, TrajOut out, int64_t max_n, int sm_count,
                         cudaStream_t s);
 
+// One instance of a multi-instance bulk launch: its field table and clock, and
+// where its candidates and time samples sit in the concatenated arrays.
+struct BulkInst {
+    const float4* table;
+    int64_t cand_end;  // the instance owns candidates [cand_end of the one before, cand_end)
+    double T0, inv_h_d, t_final;
+    int t_off;         // its first time sample in the concatenated array
+    int n_int, nf;
+    float ff, h, inv_h;
+};
+constexpr int kMaxInstances = 64;
+
 // Parameters of the FP32 bulk integrator (integrate_fp32.cu).
 struct BulkParams {
     int dim, phase, tgt;
@@ -136,6 +148,8 @@ struct BulkParams {
     int table_in_smem;  // 1: stage the table in shared memory
     int threads, blocks_per_sm, refill_min;
     int64_t max_n;      // upper bound of the electron count (grid sizing)
+    const BulkInst* inst;  // multi-instance launch: n_inst instances (else nullptr, 0)
+    int n_inst;
     const float4* table;
     double T0, inv_h_d, t_final;
     float h, inv_h, rtol;
@@ -144,9 +158,19 @@ struct BulkParams {
     float Z, Ip, sc, a1, b1, a2, b2, a3, b3, a2b2;
 };
 int launch_field_table(const DJob& J, double T0, double h, int n_int, float4* tab, cudaStream_t s);
-// FP32 collection of the bulk integrator's final states.
+// FP32 collection of the bulk integrator's final states.  With inst (n_inst
+// instances of one grid J.grid) the keys are instance * J.grid + bin and the
+// "not deposited" key is n_inst * J.grid.
 int launch_collect_bulk(const DJob& J, InitSoA soa, const double* t, const int64_t* idx,
                         const unsigned long long* count, TrajOut out, int64_t max_n, int sm_count,
+                        cudaStream_t s, const BulkInst* inst = nullptr, int n_inst = 0);
+// Per-instance results of a multi-instance launch (deposit.cu): survivor
+// segments, canonical ion_prob sums, counters, and the weighted sum of spectra.
+int launch_instance_reductions(const TrajOut& out, const int64_t* idx, const unsigned long long* count,
+                               const BulkInst* inst, int n_inst, int64_t* seg, double* scratch,
+                               double* sums /* 2 per instance */, Counters* counters, cudaStream_t s);
+size_t instance_scratch_doubles(int64_t max_n, int n_inst);
+int launch_weighted_sum(const double* mspec, int n_inst, int64_t grid, const double* w, double* out,
                         cudaStream_t s);
 int launch_integrate_bulk(const BulkParams& P, InitSoA soa, const double* t, const int64_t* idx,
                           const unsigned long long* count, unsigned long long* queue, TrajOut out,

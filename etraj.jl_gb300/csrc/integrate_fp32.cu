@@ -137,11 +137,11 @@ __device__ __forceinline__ void field(const float4* __restrict__ tab, int n_int,
 // (for the rounding-noise bound of the error estimate; unused outputs of the
 // inlined call are removed by the compiler).
 template <int DIM, int PHASE, int TGT>
-__device__ __forceinline__ void accel(const BulkParams& P, const float4* __restrict__ tab, int ni, float fi,
-                                      const float* X, const float* Pm, float* K, float& kph, float& mK,
+__device__ __forceinline__ void accel(const BulkParams& P, const float4* __restrict__ tab, int n_int, int ni,
+                                      float fi, const float* X, const float* Pm, float* K, float& kph, float& mK,
                                       float& mph) {
     float Fx, Fy;
-    field(tab, P.n_int, ni, fi, Fx, Fy);
+    field(tab, n_int, ni, fi, Fx, Fy);
     const float r2 = (DIM == 3) ? fmaf(X[0], X[0], fmaf(X[1], X[1], X[2] * X[2])) : fmaf(X[0], X[0], X[1] * X[1]);
     float coef, V = 0.0f;
     if (TGT == ETRAJ_TARGET_HYDROGEN_LIKE) {
@@ -192,7 +192,13 @@ __device__ __forceinline__ float small_int_to_float(int k) {
     return __int_as_float(__float_as_int(kMagic) + k) - kMagic;
 }
 
-template <int DIM, int PHASE, int TGT>
+// MULTI: one launch over the electrons of P.n_inst instances (different
+// lasers, same target, dimension, phase and tolerance).  Each lane finds its
+// electron's instance when it loads it (binary search of the candidate index
+// over the instances' ranges, held in shared memory) and reads that instance's
+// table and clock there, so one warp may integrate electrons of several
+// instances at once: the work stealing spans all of them.
+template <int DIM, int PHASE, int TGT, bool MULTI>
 __global__ void __launch_bounds__(256, 2)
 k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double* __restrict__ tsamp,
                  const int64_t* __restrict__ idx, const unsigned long long* __restrict__ count,
@@ -200,12 +206,17 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
     constexpr bool HASPH = (PHASE != ETRAJ_PHASE_CTMC);
     constexpr int N = 2 * DIM + (HASPH ? 1 : 0);
     extern __shared__ float4 s_tab[];
+    __shared__ BulkInst s_inst[MULTI ? kMaxInstances : 1];
     const float4* tab = P.table;
-    if (P.table_in_smem) {
+    if (MULTI) {
+        for (int i = threadIdx.x; i < P.n_inst; i += blockDim.x) s_inst[i] = P.inst[i];
+        __syncthreads();
+    } else if (P.table_in_smem) {
         for (int i = threadIdx.x; i < 2 * P.n_int; i += blockDim.x) s_tab[i] = P.table[i];
         __syncthreads();
         tab = s_tab;
     }
+    int my = 0;  // the lane's instance (MULTI)
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
@@ -254,13 +265,31 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
                         fh = (float)f0;
                         flo = (float)(f0 - (double)fh);
                     }
-                    const double t0 = tsamp[soa.batch[g]];
-                    const double q0 = (t0 - P.T0) * P.inv_h_d;
+                    double T0 = P.T0, inv_h_d = P.inv_h_d, t_final = P.t_final;
+                    int toff = 0;
+                    if (MULTI) {
+                        int lo = 0, hi = P.n_inst - 1;
+                        while (lo < hi) {
+                            const int mid = (lo + hi) >> 1;
+                            if (g < s_inst[mid].cand_end) hi = mid;
+                            else lo = mid + 1;
+                        }
+                        my = lo;
+                        T0 = s_inst[my].T0;
+                        inv_h_d = s_inst[my].inv_h_d;
+                        t_final = s_inst[my].t_final;
+                        toff = s_inst[my].t_off;
+                    }
+                    const float4* tabi = MULTI ? s_inst[my].table : tab;
+                    const int nint = MULTI ? s_inst[my].n_int : P.n_int;
+                    const float hh = MULTI ? s_inst[my].h : P.h, ihh = MULTI ? s_inst[my].inv_h : P.inv_h;
+                    const double t0 = tsamp[toff + soa.batch[g]];
+                    const double q0 = (t0 - T0) * inv_h_d;
                     const double fl = floor(q0);
                     tn = (int)fl;
                     tfr = (float)(q0 - fl);
-                    dthmax = (float)((P.t_final - t0) * P.inv_h_d);
-                    accel<DIM, PHASE, TGT>(P, tab, tn, tfr, xh, ph, K1, kph1, mK1, mph1);
+                    dthmax = (float)((t_final - t0) * inv_h_d);
+                    accel<DIM, PHASE, TGT>(P, tabi, nint, tn, tfr, xh, ph, K1, kph1, mK1, mph1);
                     // d0 = |u0/sk|, d1 = |f0/sk| (f0 = (p, K, phase rate))
                     float skx[DIM], skp[DIM], skf = 0.0f, a0 = 0.0f, a1 = 0.0f;
 #pragma unroll
@@ -281,7 +310,7 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
                     }
                     const float d0 = sqrtf(a0 * (1.0f / N)), d1 = sqrtf(a1 * (1.0f / N));
                     float dt0 = (d0 < 1e-5f || d1 < 1e-5f) ? 1e-6f : (d0 / d1) * 0.01f;
-                    dt0 = fminf(dt0, dthmax * P.h);
+                    dt0 = fminf(dt0, dthmax * hh);
                     // f1 at u1 = u0 + dt0 f0; f1 - f0 for the position rows is dt0 K exactly
                     float X1[DIM], P1[DIM], K1b[DIM], kph1b;
 #pragma unroll
@@ -291,9 +320,9 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
                     }
                     int n1;
                     float f1r;
-                    advance(tn, tfr, dt0 * P.inv_h, n1, f1r);
+                    advance(tn, tfr, dt0 * ihh, n1, f1r);
                     float unused_m, unused_p;
-                    accel<DIM, PHASE, TGT>(P, tab, n1, f1r, X1, P1, K1b, kph1b, unused_m, unused_p);
+                    accel<DIM, PHASE, TGT>(P, tabi, nint, n1, f1r, X1, P1, K1b, kph1b, unused_m, unused_p);
                     float a2 = 0.0f;
 #pragma unroll
                     for (int d = 0; d < DIM; ++d) {
@@ -308,7 +337,7 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
                     const float md = fmaxf(d1, d2);
                     const float dt1 = (md <= 1e-15f) ? fmaxf(1e-6f, dt0 * 1e-3f)
                                                      : exp2f(-(2.0f + log10f(md)) * (3.321928094887362f / 5.0f));
-                    dth = fminf(fminf(100.0f * dt0, dt1), dthmax * P.h) * P.inv_h;
+                    dth = fminf(fminf(100.0f * dt0, dt1), dthmax * hh) * ihh;
                     dthp = dth;
                     lqold = LOG2_QOLDINIT;
                     q11 = 1.0f;
@@ -329,7 +358,12 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
             }
             ++iter;
             dth = fminf(dth, dthmax);
-            const float remaining = small_int_to_float(P.nf - tn) + (P.ff - tfr);
+            const float4* tabi = MULTI ? s_inst[my].table : tab;
+            const int nint = MULTI ? s_inst[my].n_int : P.n_int;
+            const int nfi = MULTI ? s_inst[my].nf : P.nf;
+            const float ffi = MULTI ? s_inst[my].ff : P.ff;
+            const float hh = MULTI ? s_inst[my].h : P.h;
+            const float remaining = small_int_to_float(nfi - tn) + (ffi - tfr);
             const bool last = dth >= remaining;
             if (last) dth = remaining;
             int status = 0;
@@ -337,13 +371,13 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
             else if (iter > MAXITERS) status = 1;
             else if (dth < kDthMin && !last) status = 2;
             if (status == 0) {
-                const float dt = dth * P.h, dt2 = dt * dt;
+                const float dt = dth * hh, dt2 = dt * dt;
                 float K[7][DIM], kph[7], X[DIM], Pm[DIM], mK7 = 0.0f, mph7 = 0.0f;
                 int n1 = 0;
                 float f1 = 0.0f;
                 if (last) {
-                    n1 = P.nf;
-                    f1 = P.ff;
+                    n1 = nfi;
+                    f1 = ffi;
                 } else {
                     advance(tn, tfr, dth, n1, f1);
                 }
@@ -366,7 +400,7 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
                     int ni = n1;
                     float fi = f1;
                     if (st < 5) advance(tn, tfr, cC[st] * dth, ni, fi);
-                    accel<DIM, PHASE, TGT>(P, tab, ni, fi, X, Pm, K[st], kph[st], mK7, mph7);
+                    accel<DIM, PHASE, TGT>(P, tabi, nint, ni, fi, X, Pm, K[st], kph[st], mK7, mph7);
                 }
                 // X, Pm now hold the new position and momentum (stage 7 = solution)
                 float incf = 0.0f, phnew = 0.0f;
@@ -483,16 +517,34 @@ template <int DIM, int PHASE>
 __global__ void __launch_bounds__(256)
 k_collect_bulk(const __grid_constant__ DJob J, InitSoA soa, const double* __restrict__ tsamp,
                const int64_t* __restrict__ idx, const unsigned long long* __restrict__ count,
-               TrajOut out) {
+               TrajOut out, const BulkInst* __restrict__ inst, int n_inst) {
     constexpr int N = 2 * DIM + (PHASE != ETRAJ_PHASE_CTMC ? 1 : 0);
+    __shared__ int64_t s_end[kMaxInstances];
+    __shared__ int s_toff[kMaxInstances];
+    for (int i = threadIdx.x; i < n_inst; i += blockDim.x) {
+        s_end[i] = inst[i].cand_end;
+        s_toff[i] = inst[i].t_off;
+    }
+    __syncthreads();
     const int64_t n = (int64_t)(*count);
     const float Z = (float)J.target.Z, sc = (float)J.target.sc;
+    const uint32_t sentinel = (uint32_t)(n_inst > 0 ? (int64_t)n_inst * J.grid : J.grid);
     for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n;
          s += (int64_t)gridDim.x * blockDim.x) {
         const int st = out.status[s] & 0xff;
         const int64_t g = idx ? idx[s] : s;
+        int my = 0;
+        if (n_inst > 0) {
+            int lo = 0, hi = n_inst - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (g < s_end[mid]) hi = mid;
+                else lo = mid + 1;
+            }
+            my = lo;
+        }
         const double prob = soa.rate[g];
-        uint32_t key = (uint32_t)J.grid;
+        uint32_t key = sentinel;
         double cre = 0.0, cim = 0.0, wion = 0.0, wunc = 0.0;
         float pin[3] = {0.0f, 0.0f, 0.0f};
         bool ionized = false;
@@ -530,7 +582,8 @@ k_collect_bulk(const __grid_constant__ DJob J, InitSoA soa, const double* __rest
                 const float rp = (DIM == 2) ? fmaf(rv[0], pv[0], rv[1] * pv[1])
                                             : fmaf(rv[0], pv[1], fmaf(rv[1], pv[1], rv[2] * pv[2]));
                 const float corr = (Z * sqrtb) * (logf(gg) + asinhf(rp / (gg * sqrtb)));
-                phase = (phase + J.target.Ip * tsamp[soa.batch[g]]) - (double)corr;
+                const int toff = (n_inst > 0) ? s_toff[my] : 0;
+                phase = (phase + J.target.Ip * tsamp[toff + soa.batch[g]]) - (double)corr;
             }
             if (E >= 0.0f) {
                 ionized = true;
@@ -562,7 +615,7 @@ k_collect_bulk(const __grid_constant__ DJob J, InitSoA soa, const double* __rest
                     stride *= num;
                 }
                 if (ok) {
-                    key = (uint32_t)lin;
+                    key = (uint32_t)((int64_t)my * J.grid + lin);
                     if (PHASE == ETRAJ_PHASE_CTMC) {
                         cre = prob;
                     } else {
@@ -611,12 +664,12 @@ __global__ void k_field_table(const __grid_constant__ DJob J, double T0, double 
     tab[2 * k + 1] = herm(fya, fyb, dfya, dfyb);
 }
 
-template <int DIM, int PHASE, int TGT>
+template <int DIM, int PHASE, int TGT, bool MULTI>
 int launch_bulk_t(const BulkParams& P, InitSoA soa, const double* t, const int64_t* idx,
                   const unsigned long long* count, unsigned long long* queue, TrajOut out, int sm_count,
                   cudaStream_t s) {
-    const size_t smem = P.table_in_smem ? (size_t)P.n_int * 2 * sizeof(float4) : 0;
-    auto kern = k_integrate_bulk<DIM, PHASE, TGT>;
+    const size_t smem = (!MULTI && P.table_in_smem) ? (size_t)P.n_int * 2 * sizeof(float4) : 0;
+    auto kern = k_integrate_bulk<DIM, PHASE, TGT, MULTI>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     // persistent grid, but no more blocks than the job can keep busy (at least ~4
     // electrons per lane): a block holds its SM's registers until its last warp
@@ -634,12 +687,12 @@ int launch_bulk_t(const BulkParams& P, InitSoA soa, const double* t, const int64
 
 int launch_collect_bulk(const DJob& J, InitSoA soa, const double* t, const int64_t* idx,
                         const unsigned long long* count, TrajOut out, int64_t max_n, int sm_count,
-                        cudaStream_t s) {
+                        cudaStream_t s, const BulkInst* inst, int n_inst) {
     const int threads = 256;
     const int64_t want = (max_n + threads - 1) / threads;
     const int64_t cap = (int64_t)sm_count * 8;
     const int blocks = (int)(want < cap ? (want > 0 ? want : 1) : cap);
-#define ETRAJ_COLLECT(D, P) k_collect_bulk<D, P><<<blocks, threads, 0, s>>>(J, soa, t, idx, count, out)
+#define ETRAJ_COLLECT(D, P) k_collect_bulk<D, P><<<blocks, threads, 0, s>>>(J, soa, t, idx, count, out, inst, n_inst)
     if (J.dim == 2) {
         if (J.phase == ETRAJ_PHASE_CTMC) ETRAJ_COLLECT(2, ETRAJ_PHASE_CTMC);
         else if (J.phase == ETRAJ_PHASE_QTMC) ETRAJ_COLLECT(2, ETRAJ_PHASE_QTMC);
@@ -661,11 +714,14 @@ int launch_field_table(const DJob& J, double T0, double h, int n_int, float4* ta
 int launch_integrate_bulk(const BulkParams& P, InitSoA soa, const double* t, const int64_t* idx,
                           const unsigned long long* count, unsigned long long* queue, TrajOut out,
                           int sm_count, cudaStream_t s) {
-#define ETRAJ_BULK_TGT(D, PH)                                                                       \
-    return (P.tgt == ETRAJ_TARGET_HYDROGEN_LIKE)                                                    \
-               ? launch_bulk_t<D, PH, ETRAJ_TARGET_HYDROGEN_LIKE>(P, soa, t, idx, count, queue, out, \
-                                                                  sm_count, s)                      \
-               : launch_bulk_t<D, PH, ETRAJ_TARGET_SAE>(P, soa, t, idx, count, queue, out, sm_count, s);
+#define ETRAJ_BULK_M(D, PH, TG)                                                                    \
+    return (P.n_inst > 0) ? launch_bulk_t<D, PH, TG, true>(P, soa, t, idx, count, queue, out, sm_count, s) \
+                          : launch_bulk_t<D, PH, TG, false>(P, soa, t, idx, count, queue, out, sm_count, s);
+#define ETRAJ_BULK_TGT(D, PH)                                      \
+    if (P.tgt == ETRAJ_TARGET_HYDROGEN_LIKE) {                     \
+        ETRAJ_BULK_M(D, PH, ETRAJ_TARGET_HYDROGEN_LIKE)            \
+    }                                                              \
+    ETRAJ_BULK_M(D, PH, ETRAJ_TARGET_SAE)
     if (P.dim == 2) {
         if (P.phase == ETRAJ_PHASE_CTMC) { ETRAJ_BULK_TGT(2, ETRAJ_PHASE_CTMC) }
         if (P.phase == ETRAJ_PHASE_QTMC) { ETRAJ_BULK_TGT(2, ETRAJ_PHASE_QTMC) }
@@ -676,6 +732,7 @@ int launch_integrate_bulk(const BulkParams& P, InitSoA soa, const double* t, con
         ETRAJ_BULK_TGT(3, ETRAJ_PHASE_SCTS)
     }
 #undef ETRAJ_BULK_TGT
+#undef ETRAJ_BULK_M
 }
 
 }  // namespace etraj

@@ -189,6 +189,31 @@ class Engine:
                                              abi.i32ptr(status), abi.i32ptr(steps)))
         return fin, status, steps
 
+    def run_batch(self, jobs, want_spectrum=True, want_amplitude=False, weights=None):
+        """Run up to 64 FP32-bulk jobs (same dimension, phase, rtol, target and grid)
+        as one batch; returns [(result, spectrum, amplitude)] and, with `weights`,
+        the weighted sum of the spectra."""
+        n = len(jobs)
+        arr = (abi.Job * n)(*jobs)
+        res = (abi.Result * n)()
+        outs = []
+        for i, job in enumerate(jobs):
+            spec = amp = None
+            if want_spectrum:
+                spec = np.zeros(job.grid_size, dtype=np.float64)
+                res[i].momentum_spec = abi.dptr(spec)
+            if want_amplitude and job.traj_phase_method != abi.PHASE_CTMC:
+                amp = np.zeros(2 * job.grid_size, dtype=np.float64)
+                res[i].amplitude = abi.dptr(amp)
+            outs.append((spec, amp))
+        w = wout = None
+        if weights is not None:
+            w = np.ascontiguousarray(weights, dtype=np.float64)
+            assert w.size == n
+            wout = np.zeros(jobs[0].grid_size, dtype=np.float64)
+        self._check(self.lib.etraj_run_batch(self.ctx, arr, n, res, abi.dptr(w), abi.dptr(wout)))
+        return [(res[i], outs[i][0], outs[i][1]) for i in range(n)], wout
+
     def submit(self, job, res):
         """Queue `job`; `res` (an abi.Result) carries the output pointers, which must stay
         valid until poll/wait reports the ticket done."""

@@ -217,6 +217,22 @@ int etraj_submit(etraj_ctx* ctx, const etraj_job* job, etraj_result* out, uint64
 int etraj_poll(etraj_ctx* ctx, uint64_t ticket, etraj_result* out);
 int etraj_wait(etraj_ctx* ctx, uint64_t ticket, etraj_result* out);
 
+/* ---- multi-instance batch ------------------------------------------------------
+ * No counterpart in the reference, which runs one simulation per call.  Runs
+ * n_jobs (1..64) FP32-bulk jobs as one batch: per-instance sampling, then one
+ * compaction, ONE bulk-integrator launch whose work stealing spans the
+ * electrons of every instance, one collection and one deposit into an
+ * instance-major grid.  The jobs may differ in laser and sampler; they must
+ * share precision (FP32_BULK), dimension, phase method, rtol, target and
+ * momentum grid (else ETRAJ_ERR_INVALID_ARGUMENT).  results[i] receives job
+ * i's scalars and, through its own pointers, its spectrum and amplitude;
+ * each equals the result of running job i alone.  With weights (n_jobs
+ * values), weighted_spec (one grid) receives sum_i weights[i] *
+ * momentum_spec_i, summed in instance order (e.g. an intensity-weighted
+ * focal-volume average); pass NULL for both to skip it.  Blocking. */
+int etraj_run_batch(etraj_ctx* ctx, const etraj_job* jobs, int n_jobs, etraj_result* results,
+                    const double* weights, double* weighted_spec);
+
 /* ---- serving: continuous batching on one GPU ---------------------------------
  * No counterpart in the reference, which runs one job per call.  A server owns
  * `slots` (1..64) contexts, each with its own stream and device buffers, and
