@@ -365,6 +365,8 @@ def main():
         }
         if not args.no_multi_instance and world == 1:
             line["multi_instance"] = multi_instance_report(eng)
+            line["autotune"] = autotune_report(eng, job, multi_instance_jobs()[0])
+            line["graphs"] = graphs_report(lambda n: maker(args.precision, seed=rank, t_num=n or args.t_num))
         if not args.no_serving and world == 1:
             line["serving"] = serving_report()
         if not args.no_cpu_baseline:
@@ -555,6 +557,58 @@ def multi_instance_report(eng):
                                   "trajectories_per_s": eff / (dev_seq / 1e3)},
             "weighted_pmd_sum": float(wsum.sum()),
             "workload": multi_instance_jobs.__doc__.replace("\n    ", " ")}
+
+
+def autotune_report(eng, job, batch_jobs):
+    """Integrator time with the autotuner's launch shape against the fixed 256 x 2 x 4,
+    for the headline job and for the 64-instance batch."""
+    fixed = et.Engine(device=0)
+    fixed.set_autotune(False)
+    out = {}
+    for name, run in (("headline", lambda e: e.run(job, want_spectrum=False)),
+                      ("multi_instance", lambda e: e.run_batch(batch_jobs, want_spectrum=False))):
+        row = {}
+        for tag, e in (("tuned", eng), ("fixed", fixed)):
+            run(e)
+            vals = []
+            for _ in range(3):
+                run(e)
+                import ctypes as C
+                buf = (C.c_double * 8)()
+                if e.lib.etraj_stage_times(e.ctx, buf, 8) > 3:
+                    vals.append(buf[3])
+            row[tag + "_integrate_ms"] = statistics.mean(vals) if vals else None
+        j0 = job if name == "headline" else batch_jobs[0]
+        t, b, r, tuned = eng.bulk_tile(j0.dimension, j0.traj_phase_method, j0.target.kind, name != "headline")
+        row["tile"] = {"threads": t, "blocks_per_sm": b, "refill_min": r, "tuned": tuned}
+        out[name] = row
+    fixed.close()
+    return out
+
+
+def graphs_report(job_fn):
+    """Per-job device and wall time with and without CUDA-graph replay, for the
+    headline job and a 1e5-candidate job of the same workload (where launch
+    overhead matters)."""
+    out = {}
+    for name, t_num in (("1e5_candidates", 100), ("headline", None)):
+        job = job_fn(t_num)
+        row = {}
+        for tag, on in (("direct", False), ("graph", True)):
+            e = et.Engine(device=0)
+            e.set_graphs(on)
+            for _ in range(3):
+                e.run(job, want_spectrum=False)
+            dev, wall = [], []
+            for _ in range(20):
+                t0 = time.perf_counter()
+                r, _, _ = e.run(job, want_spectrum=False)
+                wall.append(1e3 * (time.perf_counter() - t0))
+                dev.append(r.elapsed_ms)
+            e.close()
+            row[tag] = {"device_ms": statistics.median(dev), "wall_ms": statistics.median(wall)}
+        out[name] = row
+    return out
 
 
 STAGES = ("sample", "compact", "field_table", "integrate", "collect", "deposit")

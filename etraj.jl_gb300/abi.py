@@ -122,6 +122,9 @@ SIGNATURES = [
     ("etraj_server_wait", C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(Result), C.c_double]),
     ("etraj_server_stats", C.c_int, [C.c_void_p, _I64P, _I64P, C.POINTER(C.c_size_t)]),
     ("etraj_server_last_error", C.c_char_p, [C.c_void_p]),
+    ("etraj_set_graphs", C.c_int, [C.c_void_p, C.c_int]),
+    ("etraj_set_autotune", C.c_int, [C.c_void_p, C.c_int]),
+    ("etraj_bulk_tile", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, _I32P, _I32P, _I32P]),
     ("etraj_stage_times", C.c_int, [C.c_void_p, _DP, C.c_int]),
     ("etraj_deposit_noalloc", C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                         C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

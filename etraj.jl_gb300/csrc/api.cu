@@ -368,6 +368,11 @@ struct PinnedBlock {
     size_t bytes = 0;
 };
 
+// Launch shape of the bulk integrator.
+struct BulkTile {
+    int threads, blocks_per_sm, refill_min;
+};
+
 }  // namespace
 
 struct etraj_ctx {
@@ -389,6 +394,16 @@ struct etraj_ctx {
     std::map<uint64_t, JobRec> jobs;       // asynchronous tickets of this context
     std::vector<PinnedBlock> pinned_pool;  // staging blocks for reuse
     std::vector<cudaEvent_t> event_pool;
+    // CUDA-graph replay of the per-job kernel sequence (opt-in): the graph of
+    // the last captured job and the launch parameters it was captured with
+    bool graphs = false;
+    bool capturing = false;
+    cudaGraphExec_t gexec = nullptr;
+    std::vector<unsigned char> gkey;
+    int glaunches = 0;
+    // bulk-integrator launch shapes chosen by the autotuner, per kernel variant
+    bool autotune = true;
+    std::map<int, BulkTile> tiles;
     // sizing without allocating: ensure() only adds up the growth
     bool dry = false;
     size_t dry_bytes = 0;
@@ -565,15 +580,93 @@ void prepare_bulk(const DJob& J, double tmin, BulkParams& B) {
     B.a2b2 = (float)(T_.a2 * T_.b2);
 }
 
+// ---- autotuner of the bulk integrator's launch shape ----------------------------------
+// Candidates: threads per block x blocks per SM (128 registers per thread fix
+// 16 warps per SM) x the number of free lanes a warp waits for before it
+// refills.  Each variant (dimension, phase, target, single/multi-instance) is
+// tuned once per context, on the first 2^18 electrons of its first job with
+// enough work, by timing every candidate twice with events; results do not
+// depend on the launch shape (one electron per lane, deterministic deposit).
+cudaEvent_t get_event(etraj_ctx* ctx);
+
+constexpr BulkTile kTileCandidates[] = {{256, 2, 4}, {256, 2, 8}, {256, 2, 2}, {256, 2, 16},
+                                        {128, 4, 4}, {128, 4, 8}, {128, 3, 4}, {64, 8, 4}};
+constexpr BulkTile kTileDefault = {256, 2, 4};
+
+// Stage events: inside a stream capture they become event-record nodes of the graph.
+void rec(etraj_ctx* ctx, cudaEvent_t e, cudaStream_t s) {
+    if (ctx->capturing) cudaEventRecordWithFlags(e, s, cudaEventRecordExternal);
+    else cudaEventRecord(e, s);
+}
+
+int tile_key(const BulkParams& B) { return ((B.n_inst > 0) ? 1000 : 0) + B.dim * 100 + B.phase * 10 + B.tgt; }
+
+void apply_tile(BulkParams& B, const BulkTile& t) {
+    B.threads = t.threads;
+    B.blocks_per_sm = t.blocks_per_sm;
+    B.refill_min = t.refill_min;
+    const size_t tb = (size_t)B.n_int * 2 * sizeof(float4);
+    B.table_in_smem = (B.n_inst == 0 && tb <= (size_t)96 * 1024 && tb * (size_t)t.blocks_per_sm <= (size_t)200 * 1024)
+                          ? 1 : 0;
+}
+
+int tuned_bulk_launch(etraj_ctx* ctx, BulkParams& B, const InitSoA& soa, const double* t, const int64_t* idx,
+                      const unsigned long long* count, unsigned long long* work, const TrajOut& out,
+                      int* launches, cudaEvent_t* ev) {
+    cudaStream_t s = ctx->stream;
+    const int key = tile_key(B);
+    auto it = ctx->tiles.find(key);
+    if (it == ctx->tiles.end() && ctx->autotune && B.max_n >= ((int64_t)1 << 18)) {
+        unsigned long long* sub = nullptr;
+        ETRAJ_TRY(ensure_t(ctx, "tune.count", 1, &sub));
+        *launches += launch_clamp_count(count, 1ull << 18, sub, s);
+        const int nc = (int)(sizeof kTileCandidates / sizeof kTileCandidates[0]);
+        std::vector<cudaEvent_t> evs((size_t)4 * nc);
+        for (auto& e : evs) e = get_event(ctx);
+        for (int rep = 0; rep < 2; ++rep) {
+            for (int c = 0; c < nc; ++c) {
+                BulkParams Bc = B;
+                apply_tile(Bc, kTileCandidates[c]);
+                cudaMemsetAsync(work, 0, sizeof(unsigned long long), s);
+                cudaEventRecord(evs[(size_t)(4 * c + 2 * rep)], s);
+                *launches += launch_integrate_bulk(Bc, soa, t, idx, sub, work, out, ctx->sm_count, s);
+                cudaEventRecord(evs[(size_t)(4 * c + 2 * rep + 1)], s);
+            }
+        }
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) return cuda_err(ctx, e, "autotune");
+        float best = 1e30f;
+        BulkTile bt = kTileDefault;
+        for (int c = 0; c < nc; ++c) {
+            float m0 = 0.f, m1 = 0.f;
+            cudaEventElapsedTime(&m0, evs[(size_t)(4 * c)], evs[(size_t)(4 * c + 1)]);
+            cudaEventElapsedTime(&m1, evs[(size_t)(4 * c + 2)], evs[(size_t)(4 * c + 3)]);
+            const float m = m0 < m1 ? m0 : m1;
+            if (m < best) {
+                best = m;
+                bt = kTileCandidates[c];
+            }
+        }
+        for (auto& ev_ : evs) ctx->event_pool.push_back(ev_);
+        it = ctx->tiles.emplace(key, bt).first;
+    }
+    apply_tile(B, it != ctx->tiles.end() ? it->second : kTileDefault);
+    cudaMemsetAsync(work, 0, sizeof(unsigned long long), s);
+    if (ev) rec(ctx, ev[0], s);
+    *launches += launch_integrate_bulk(B, soa, t, idx, count, work, out, ctx->sm_count, s);
+    if (ev) rec(ctx, ev[1], s);
+    return ETRAJ_OK;
+}
+
 int launch_integrate(etraj_ctx* ctx, const DJob& J, const InitSoA& soa, const double* t, const int64_t* idx,
                      const unsigned long long* count, const TrajOut& out, int64_t max_n, unsigned long long* work,
                      int precision, double tmin, int* launches, cudaEvent_t* ev = nullptr) {
     // ev (optional): events recorded after the field table [0] and the integrator [1]
     cudaStream_t s = ctx->stream;
     if (precision != ETRAJ_PRECISION_FP32_BULK) {
-        if (ev) cudaEventRecord(ev[0], s);
+        if (ev) rec(ctx, ev[0], s);
         *launches += launch_integrate_fp64(J, soa, t, idx, count, out, max_n, ctx->sm_count, s);
-        if (ev) cudaEventRecord(ev[1], s);
+        if (ev) rec(ctx, ev[1], s);
         return ETRAJ_OK;
     }
     BulkParams B;
@@ -583,10 +676,7 @@ int launch_integrate(etraj_ctx* ctx, const DJob& J, const InitSoA& soa, const do
     ETRAJ_TRY(ensure_t(ctx, "field_table", (size_t)B.n_int * 2, &tab));
     B.table = tab;
     *launches += launch_field_table(J, B.T0, (double)1.0 / B.inv_h_d, B.n_int, tab, s);
-    cudaMemsetAsync(work, 0, sizeof(unsigned long long), s);
-    if (ev) cudaEventRecord(ev[0], s);
-    *launches += launch_integrate_bulk(B, soa, t, idx, count, work, out, ctx->sm_count, s);
-    if (ev) cudaEventRecord(ev[1], s);
+    ETRAJ_TRY(tuned_bulk_launch(ctx, B, soa, t, idx, count, work, out, launches, ev));
     *launches += launch_collect_bulk(J, soa, t, idx, count, out, max_n, ctx->sm_count, s);
     return ETRAJ_OK;
 }
@@ -664,6 +754,101 @@ size_t plan_growth(etraj_ctx* ctx, const etraj_job* job) {
     return ctx->dry_bytes;
 }
 
+// The device work of one job, from the per-batch prologue to the deposit.
+int enqueue_kernels(etraj_ctx* ctx, const etraj_job* job, const HostJob& H, const Pipeline& P, int* nl) {
+    const DJob& J = H.J;
+    cudaStream_t s = ctx->stream;
+    int launches = 0;
+    rec(ctx, ctx->stage_ev[0], s);
+    launches += launch_batch_prepare(J, P.t, P.batches, s);
+    if (job->precision == ETRAJ_PRECISION_FP32_BULK && J.method != ETRAJ_SAMPLER_SPA && J.cutoff >= kSample32MinCutoff)
+        launches += launch_sample32_range(J, 0, J.n_t, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s);
+    else
+        launches += launch_sample_range(J, 0, J.n_t, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s);
+    rec(ctx, ctx->stage_ev[1], s);
+    launches += launch_compact(P.flag, J.n_total, P.idx, P.block_sums, compact_blocks(J.n_total) + 1, P.count, s);
+    rec(ctx, ctx->stage_ev[2], s);
+    ETRAJ_TRY(launch_integrate(ctx, J, P.soa, P.t, P.idx, P.count, P.out, J.n_total, P.work, job->precision,
+                               H.t.front(), &launches, ctx->stage_ev + 3));
+    rec(ctx, ctx->stage_ev[5], s);
+    launches += launch_deposit(J, P.out, P.count, J.n_total, P.dep, P.spec_re, P.spec_im, P.mspec, P.sums,
+                               P.counters, s);
+    rec(ctx, ctx->stage_ev[6], s);
+    ctx->stage_valid = true;
+    *nl = launches;
+    return ETRAJ_OK;
+}
+
+// With ctx->graphs the kernel sequence is captured once into a CUDA graph and
+// replayed while the launch parameters (device job, buffer addresses, bulk
+// launch shape, table size) stay the same; a job that needs an autotuning pass
+// first runs without a graph.
+int enqueue_kernels_maybe_graph(etraj_ctx* ctx, const etraj_job* job, const HostJob& H, const Pipeline& P,
+                                int* launches) {
+    const DJob& J = H.J;
+    bool use_graph = ctx->graphs;
+    int tile_k = -1;
+    size_t n_int = 0;
+    if (use_graph && job->precision == ETRAJ_PRECISION_FP32_BULK) {
+        BulkParams B;
+        prepare_bulk(J, H.t.front(), B);
+        B.max_n = J.n_total;
+        n_int = (size_t)B.n_int;
+        tile_k = tile_key(B);
+        if (ctx->autotune && !ctx->tiles.count(tile_k) && B.max_n >= ((int64_t)1 << 18)) use_graph = false;
+        float4* tab = nullptr;  // allocate the field table outside the capture
+        ETRAJ_TRY(ensure_t(ctx, "field_table", n_int * 2, &tab));
+    }
+    if (!use_graph) return enqueue_kernels(ctx, job, H, P, launches);
+    void* tab_ptr = ctx->bufs.count("field_table") ? ctx->bufs["field_table"].p : nullptr;
+    std::vector<unsigned char> key(sizeof J + sizeof P + sizeof(int) * 3 + sizeof(size_t) + sizeof(void*));
+    unsigned char* k = key.data();
+    std::memcpy(k, &J, sizeof J);
+    k += sizeof J;
+    std::memcpy(k, &P, sizeof P);
+    k += sizeof P;
+    const BulkTile t = ctx->tiles.count(tile_k) ? ctx->tiles[tile_k] : kTileDefault;
+    const int extra[3] = {job->precision, t.threads * 1000 + t.blocks_per_sm, t.refill_min};
+    std::memcpy(k, extra, sizeof extra);
+    k += sizeof extra;
+    std::memcpy(k, &n_int, sizeof n_int);
+    k += sizeof n_int;
+    std::memcpy(k, &tab_ptr, sizeof tab_ptr);
+    cudaStream_t s = ctx->stream;
+    if (ctx->gexec && key == ctx->gkey) {
+        cudaError_t e = cudaGraphLaunch(ctx->gexec, s);
+        if (e != cudaSuccess) return cuda_err(ctx, e, "cudaGraphLaunch");
+        *launches = ctx->glaunches;
+        ctx->stage_valid = true;
+        return ETRAJ_OK;
+    }
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        cudaGetLastError();
+        return enqueue_kernels(ctx, job, H, P, launches);
+    }
+    ctx->capturing = true;
+    const int st = enqueue_kernels(ctx, job, H, P, launches);
+    ctx->capturing = false;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    cudaGraphExec_t ex = nullptr;
+    if (st == ETRAJ_OK && e == cudaSuccess && g && cudaGraphInstantiate(&ex, g, 0) == cudaSuccess) {
+        cudaGraphDestroy(g);
+        if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
+        ctx->gexec = ex;
+        ctx->gkey = key;
+        ctx->glaunches = *launches;
+        e = cudaGraphLaunch(ex, s);
+        if (e != cudaSuccess) return cuda_err(ctx, e, "cudaGraphLaunch");
+        return ETRAJ_OK;
+    }
+    // capture failed: run the sequence directly
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    if (st != ETRAJ_OK) return st;
+    return enqueue_kernels(ctx, job, H, P, launches);
+}
+
 // Enqueues one whole job on the context's stream: host set-up, copies of the
 // time and momentum samples, every kernel, and the copies of the results.  With
 // r.staged the results go to a pinned block and r.ev_done marks completion;
@@ -707,27 +892,12 @@ int enqueue_job(etraj_ctx* ctx, const etraj_job* job, JobRec& r) {
         r.ev_done = ctx->ev1;
     }
     cudaStream_t s = ctx->stream;
-    int launches = 0;
     cudaMemcpyAsync(P.t, H.t.data(), H.t.size() * sizeof(double), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(P.kd, H.kd.data(), H.kd.size() * sizeof(double), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(P.kz, H.kz.data(), H.kz.size() * sizeof(double), cudaMemcpyHostToDevice, s);
     cudaEventRecord(r.ev_start, s);
-    cudaEventRecord(ctx->stage_ev[0], s);
-    launches += launch_batch_prepare(J, P.t, P.batches, s);
-    if (job->precision == ETRAJ_PRECISION_FP32_BULK && J.method != ETRAJ_SAMPLER_SPA && J.cutoff >= kSample32MinCutoff)
-        launches += launch_sample32_range(J, 0, J.n_t, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s);
-    else
-        launches += launch_sample_range(J, 0, J.n_t, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s);
-    cudaEventRecord(ctx->stage_ev[1], s);
-    launches += launch_compact(P.flag, J.n_total, P.idx, P.block_sums, compact_blocks(J.n_total) + 1, P.count, s);
-    cudaEventRecord(ctx->stage_ev[2], s);
-    ETRAJ_TRY(launch_integrate(ctx, J, P.soa, P.t, P.idx, P.count, P.out, J.n_total, P.work, job->precision,
-                               H.t.front(), &launches, ctx->stage_ev + 3));
-    cudaEventRecord(ctx->stage_ev[5], s);
-    launches += launch_deposit(J, P.out, P.count, J.n_total, P.dep, P.spec_re, P.spec_im, P.mspec, P.sums,
-                               P.counters, s);
-    cudaEventRecord(ctx->stage_ev[6], s);
-    ctx->stage_valid = true;
+    int launches = 0;
+    ETRAJ_TRY(enqueue_kernels_maybe_graph(ctx, job, H, P, &launches));
     cudaMemcpyAsync(dst_sums, P.sums, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(dst_cnt, P.counters, sizeof(Counters), cudaMemcpyDeviceToHost, s);
     if (dst_spec) cudaMemcpyAsync(dst_spec, P.mspec, (size_t)J.grid * sizeof(double), cudaMemcpyDeviceToHost, s);
@@ -921,10 +1091,7 @@ int run_batch(etraj_ctx* ctx, const etraj_job* jobs, int n, etraj_result* res, c
     M.max_n = N;
     M.inst = d_inst;
     M.n_inst = n;
-    cudaMemsetAsync(P.work, 0, sizeof(unsigned long long), s);
-    cudaEventRecord(ctx->stage_ev[3], s);
-    launches += launch_integrate_bulk(M, P.soa, P.t, P.idx, P.count, P.work, P.out, ctx->sm_count, s);
-    cudaEventRecord(ctx->stage_ev[4], s);
+    ETRAJ_TRY(tuned_bulk_launch(ctx, M, P.soa, P.t, P.idx, P.count, P.work, P.out, &launches, ctx->stage_ev + 3));
     launches += launch_collect_bulk(H[0].J, P.soa, P.t, P.idx, P.count, P.out, N, ctx->sm_count, s, d_inst, n);
     cudaEventRecord(ctx->stage_ev[5], s);
     launches += launch_deposit(Jgrid, P.out, P.count, N, P.dep, P.spec_re, P.spec_im, P.mspec, P.sums, P.counters, s);
@@ -1090,6 +1257,7 @@ void etraj_destroy(etraj_ctx* ctx) {
     for (auto& kv : ctx->bufs)
         if (kv.second.p) cudaFreeAsync(kv.second.p, ctx->stream);
     cudaStreamSynchronize(ctx->stream);
+    if (ctx->gexec) cudaGraphExecDestroy(ctx->gexec);
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     for (int i = 0; i <= etraj_ctx::kStages; ++i)
@@ -1544,6 +1712,40 @@ int etraj_run_batch(etraj_ctx* ctx, const etraj_job* jobs, int n_jobs, etraj_res
     std::lock_guard<std::mutex> lk(ctx->mu);
     cudaSetDevice(ctx->device);
     return run_batch(ctx, jobs, n_jobs, results, weights, weighted_spec);
+}
+
+int etraj_set_graphs(etraj_ctx* ctx, int enable) {
+    if (!ctx) return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->graphs = (enable != 0);
+    if (!enable && ctx->gexec) {
+        cudaStreamSynchronize(ctx->stream);
+        cudaGraphExecDestroy(ctx->gexec);
+        ctx->gexec = nullptr;
+        ctx->gkey.clear();
+    }
+    return ETRAJ_OK;
+}
+
+int etraj_set_autotune(etraj_ctx* ctx, int enable) {
+    if (!ctx) return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->autotune = (enable != 0);
+    if (!enable) ctx->tiles.clear();
+    return ETRAJ_OK;
+}
+
+int etraj_bulk_tile(etraj_ctx* ctx, int dimension, int phase, int target, int multi, int* threads,
+                    int* blocks_per_sm, int* refill_min) {
+    if (!ctx) return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    const int key = (multi ? 1000 : 0) + dimension * 100 + phase * 10 + target;
+    auto it = ctx->tiles.find(key);
+    const BulkTile t = (it != ctx->tiles.end()) ? it->second : kTileDefault;
+    if (threads) *threads = t.threads;
+    if (blocks_per_sm) *blocks_per_sm = t.blocks_per_sm;
+    if (refill_min) *refill_min = t.refill_min;
+    return (it != ctx->tiles.end()) ? ETRAJ_OK : ETRAJ_ERR_NOT_FOUND;
 }
 
 int etraj_stage_times(etraj_ctx* ctx, double* ms, int n) {

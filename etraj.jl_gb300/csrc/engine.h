@@ -158,6 +158,9 @@ struct BulkParams {
     float Z, Ip, sc, a1, b1, a2, b2, a3, b3, a2b2;
 };
 int launch_field_table(const DJob& J, double T0, double h, int n_int, float4* tab, cudaStream_t s);
+// *out = min(*count, cap) (the autotuner's sample of the electrons)
+int launch_clamp_count(const unsigned long long* count, unsigned long long cap, unsigned long long* out,
+                       cudaStream_t s);
 // FP32 collection of the bulk integrator's final states.  With inst (n_inst
 // instances of one grid J.grid) the keys are instance * J.grid + bin and the
 // "not deposited" key is n_inst * J.grid.

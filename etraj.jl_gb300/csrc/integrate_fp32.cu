@@ -706,6 +706,20 @@ int launch_collect_bulk(const DJob& J, InitSoA soa, const double* t, const int64
     return 1;
 }
 
+namespace {
+__global__ void k_clamp_count(const unsigned long long* __restrict__ count, unsigned long long cap,
+                              unsigned long long* __restrict__ out) {
+    const unsigned long long c = *count;
+    *out = c < cap ? c : cap;
+}
+}  // namespace
+
+int launch_clamp_count(const unsigned long long* count, unsigned long long cap, unsigned long long* out,
+                       cudaStream_t s) {
+    k_clamp_count<<<1, 1, 0, s>>>(count, cap, out);
+    return 1;
+}
+
 int launch_field_table(const DJob& J, double T0, double h, int n_int, float4* tab, cudaStream_t s) {
     k_field_table<<<(n_int + 127) / 128, 128, 0, s>>>(J, T0, h, n_int, tab);
     return 1;

@@ -189,6 +189,21 @@ class Engine:
                                              abi.i32ptr(status), abi.i32ptr(steps)))
         return fin, status, steps
 
+    def set_graphs(self, enable):
+        self._check(self.lib.etraj_set_graphs(self.ctx, 1 if enable else 0))
+
+    def set_autotune(self, enable):
+        self._check(self.lib.etraj_set_autotune(self.ctx, 1 if enable else 0))
+
+    def bulk_tile(self, dimension, phase, target, multi=False):
+        """(threads, blocks_per_sm, refill_min, tuned) of a bulk-integrator variant."""
+        t, b, r = C.c_int32(), C.c_int32(), C.c_int32()
+        st = self.lib.etraj_bulk_tile(self.ctx, dimension, phase, target, 1 if multi else 0, C.byref(t),
+                                      C.byref(b), C.byref(r))
+        if st not in (abi.OK, abi.ERR_NOT_FOUND):
+            self._check(st)
+        return t.value, b.value, r.value, st == abi.OK
+
     def run_batch(self, jobs, want_spectrum=True, want_amplitude=False, weights=None):
         """Run up to 64 FP32-bulk jobs (same dimension, phase, rtol, target and grid)
         as one batch; returns [(result, spectrum, amplitude)] and, with `weights`,

@@ -256,6 +256,27 @@ int etraj_server_wait(etraj_server* srv, uint64_t ticket, etraj_result* out, dou
 int etraj_server_stats(etraj_server* srv, int64_t* running, int64_t* queued, size_t* hbm_in_use);
 const char* etraj_server_last_error(const etraj_server* srv);
 
+/* ---- CUDA graphs ------------------------------------------------------------------
+ * No counterpart in the reference.  With etraj_set_graphs(ctx, 1) the kernel
+ * sequence of a job (prologue to deposit) is captured into a CUDA graph and
+ * replayed for the following jobs whose launch parameters are identical
+ * (same job, same buffers, same bulk launch shape), e.g. repeated runs of one
+ * configuration; any other job is captured anew.  Off by default. */
+int etraj_set_graphs(etraj_ctx* ctx, int enable);
+
+/* ---- autotuner --------------------------------------------------------------------
+ * No counterpart in the reference.  The FP32-bulk integrator's launch shape
+ * (threads per block, blocks per SM, free lanes a warp waits for before it
+ * refills) is tuned once per context and kernel variant on the first 2^18
+ * electrons of the first job with enough work, by timing 8 candidates; results
+ * never depend on it.  etraj_set_autotune(ctx, 0) switches tuning off and
+ * returns to the fixed shape 256 x 2 x 4.  etraj_bulk_tile reports the shape
+ * in use for a variant (ETRAJ_ERR_NOT_FOUND: not tuned yet, fixed shape
+ * reported). */
+int etraj_set_autotune(etraj_ctx* ctx, int enable);
+int etraj_bulk_tile(etraj_ctx* ctx, int dimension, int phase, int target, int multi, int* threads,
+                    int* blocks_per_sm, int* refill_min);
+
 /* ---- diagnostics ----------------------------------------------------------------
  * Device time (ms) of the stages of the last etraj_run on this context: sampling,
  * compaction, field table, integrator, collection, deposit.  Writes up to n

@@ -116,3 +116,21 @@ def test_bulk_deterministic(eng):
     _, s1, a1 = eng.run(job, want_amplitude=True)
     _, s2, a2 = eng.run(job, want_amplitude=True)
     assert np.array_equal(s1, s2) and np.array_equal(a1, a2)
+
+
+def test_autotuned_shape_changes_no_result():
+    """The autotuner picks the bulk integrator's launch shape from timings; one
+    electron per lane and the deterministic deposit make results independent of it."""
+    job = bulk(job_of(method="SPANE", dim=2, phase="SCTS", target="Ar", laser="cos2", ellip=1.0, mc=True,
+                      nt=700, nkd=400, nkz=1, pnum=(200, 200), pmax=2.0))
+    tuned = et.Engine(device=0)
+    fixed = et.Engine(device=0)
+    fixed.set_autotune(False)
+    r1, s1, a1 = tuned.run(job, want_amplitude=True)
+    assert tuned.bulk_tile(2, abi.PHASE_SCTS, abi.TARGET_SAE)[3]  # 2.8e5 candidates: tuned on this run
+    r2, s2, a2 = fixed.run(job, want_amplitude=True)
+    assert fixed.bulk_tile(2, abi.PHASE_SCTS, abi.TARGET_SAE) == (256, 2, 4, False)
+    assert r1.num_effective_traj == r2.num_effective_traj and r1.ion_prob == r2.ion_prob
+    assert np.array_equal(s1, s2) and np.array_equal(a1, a2)
+    tuned.close()
+    fixed.close()
