@@ -370,7 +370,7 @@ struct PinnedBlock {
 
 // Launch shape of the bulk integrator.
 struct BulkTile {
-    int threads, blocks_per_sm, refill_min;
+    int threads, blocks_per_sm, refill_min, occ;
 };
 
 }  // namespace
@@ -570,6 +570,7 @@ void prepare_bulk(const DJob& J, double tmin, BulkParams& B) {
     B.threads = 256;
     B.blocks_per_sm = 2;
     B.refill_min = 4;
+    B.occ = 2;
     const DTarget& T_ = J.target;
     B.Z = (float)T_.Z;
     B.Ip = (float)T_.Ip;
@@ -589,9 +590,10 @@ void prepare_bulk(const DJob& J, double tmin, BulkParams& B) {
 // depend on the launch shape (one electron per lane, deterministic deposit).
 cudaEvent_t get_event(etraj_ctx* ctx);
 
-constexpr BulkTile kTileCandidates[] = {{256, 2, 4}, {256, 2, 8}, {256, 2, 2}, {256, 2, 16},
-                                        {128, 4, 4}, {128, 4, 8}, {128, 3, 4}, {64, 8, 4}};
-constexpr BulkTile kTileDefault = {256, 2, 4};
+constexpr BulkTile kTileCandidates[] = {{256, 2, 4, 2}, {256, 2, 8, 2}, {256, 2, 2, 2}, {256, 2, 16, 2},
+                                        {128, 4, 4, 2}, {128, 4, 8, 2}, {128, 3, 4, 2}, {64, 8, 4, 2},
+                                        {256, 3, 4, 3}, {256, 3, 8, 3}, {128, 6, 4, 3}, {128, 6, 8, 3}};
+constexpr BulkTile kTileDefault = {256, 2, 4, 2};
 
 // Stage events: inside a stream capture they become event-record nodes of the graph.
 void rec(etraj_ctx* ctx, cudaEvent_t e, cudaStream_t s) {
@@ -605,6 +607,7 @@ void apply_tile(BulkParams& B, const BulkTile& t) {
     B.threads = t.threads;
     B.blocks_per_sm = t.blocks_per_sm;
     B.refill_min = t.refill_min;
+    B.occ = t.occ;
     const size_t tb = (size_t)B.n_int * 2 * sizeof(float4);
     B.table_in_smem = (B.n_inst == 0 && tb <= (size_t)96 * 1024 && tb * (size_t)t.blocks_per_sm <= (size_t)200 * 1024)
                           ? 1 : 0;
@@ -808,7 +811,7 @@ int enqueue_kernels_maybe_graph(etraj_ctx* ctx, const etraj_job* job, const Host
     std::memcpy(k, &P, sizeof P);
     k += sizeof P;
     const BulkTile t = ctx->tiles.count(tile_k) ? ctx->tiles[tile_k] : kTileDefault;
-    const int extra[3] = {job->precision, t.threads * 1000 + t.blocks_per_sm, t.refill_min};
+    const int extra[3] = {job->precision, t.threads * 1000 + t.blocks_per_sm * 10 + t.occ, t.refill_min};
     std::memcpy(k, extra, sizeof extra);
     k += sizeof extra;
     std::memcpy(k, &n_int, sizeof n_int);

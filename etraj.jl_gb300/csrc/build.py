@@ -30,7 +30,7 @@ UNITS = {
     "integrate_fp32.cu": ["--fmad=true"],
     "sampler_fp32.cu": ["--fmad=true"],
 }
-HEADERS = ["engine.h", "physics.cuh", "detmath.h"]
+HEADERS = sorted(f for f in os.listdir(HERE) if f.endswith((".h", ".cuh")))
 
 
 def nvcc():

@@ -198,8 +198,10 @@ __device__ __forceinline__ float small_int_to_float(int k) {
 // over the instances' ranges, held in shared memory) and reads that instance's
 // table and clock there, so one warp may integrate electrons of several
 // instances at once: the work stealing spans all of them.
-template <int DIM, int PHASE, int TGT, bool MULTI>
-__global__ void __launch_bounds__(256, 2)
+// OCC: resident 256-thread blocks per SM the build is held to (2: <= 128
+// registers per thread, 16 warps per SM; 3: <= 85 registers, 24 warps).
+template <int DIM, int PHASE, int TGT, bool MULTI, int OCC>
+__global__ void __launch_bounds__(256, OCC)
 k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double* __restrict__ tsamp,
                  const int64_t* __restrict__ idx, const unsigned long long* __restrict__ count,
                  unsigned long long* __restrict__ queue, TrajOut out) {
@@ -669,7 +671,7 @@ int launch_bulk_t(const BulkParams& P, InitSoA soa, const double* t, const int64
                   const unsigned long long* count, unsigned long long* queue, TrajOut out, int sm_count,
                   cudaStream_t s) {
     const size_t smem = (!MULTI && P.table_in_smem) ? (size_t)P.n_int * 2 * sizeof(float4) : 0;
-    auto kern = k_integrate_bulk<DIM, PHASE, TGT, MULTI>;
+    auto kern = (P.occ == 3) ? k_integrate_bulk<DIM, PHASE, TGT, MULTI, 3> : k_integrate_bulk<DIM, PHASE, TGT, MULTI, 2>;
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     // persistent grid, but no more blocks than the job can keep busy (at least ~4
     // electrons per lane): a block holds its SM's registers until its last warp

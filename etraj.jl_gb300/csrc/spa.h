@@ -43,6 +43,15 @@
 #error "spa.h: define SPA_LASER_T, SPA_WIN and SPA_AW before including"
 #endif
 
+/* The heavy pieces are real functions on the device: inlined at every call
+ * site they made the sampler's compilation take minutes.  With contraction
+ * off the results do not depend on inlining. */
+#ifdef __CUDACC__
+#define SPA_HEAVY static __host__ __device__ __noinline__
+#else
+#define SPA_HEAVY static
+#endif
+
 typedef struct {
     double key; /* Re t of w[] (NaN: empty) */
     double w[4];
@@ -50,7 +59,7 @@ typedef struct {
 
 DM_FN void spa_win_init(spa_win* W) { W->key = dm_u2d(0x7ff8000000000000ull); }
 
-DM_FN void spa_A(const SPA_LASER_T* L, spa_win* W, dm_cplx t, dm_cplx* ax, dm_cplx* ay) {
+SPA_HEAVY void spa_A(const SPA_LASER_T* L, spa_win* W, dm_cplx t, dm_cplx* ax, dm_cplx* ay) {
     if (!(W->key == t.re)) {
         SPA_WIN(L, t.re, W->w);
         W->key = t.re;
@@ -88,7 +97,7 @@ DM_FN double spa_dspe(const SPA_LASER_T* L, spa_win* W, double tr, double x, dou
 
 /* t_i of the saddle point from the initial guess x0; returns 0 when the
  * solve does not converge or t_i <= 0 (solve_spe, SPASampler.jl:241-249). */
-DM_FN double spa_solve_ti(const SPA_LASER_T* L, spa_win* W, double tr, double kd, double kz, double Ip,
+SPA_HEAVY double spa_solve_ti(const SPA_LASER_T* L, spa_win* W, double tr, double kd, double kz, double Ip,
                           double x0) {
     const double ftol = 1e-8, eta = 1e-4;
     double x = x0;
@@ -196,7 +205,7 @@ DM_FN double spa_norm(dm_cplx z) { return (z.im == 0.0) ? fabs(z.re) : dm_hypot(
  * Kronrod extension of the 7-point Gauss rule, Kronrod 1965).  g1 receives
  * the rule of the second integrand of SPA_INT_IM_AXY (same arithmetic as a
  * separate pass; may be NULL otherwise). */
-DM_FN spa_seg spa_evalrule2(int kind, const spa_quad_par* P, dm_cplx a, dm_cplx b, spa_seg* g1) {
+SPA_HEAVY spa_seg spa_evalrule2(int kind, const spa_quad_par* P, dm_cplx a, dm_cplx b, spa_seg* g1) {
     const double x[8] = {-0.991455371120812639206854697526329, -0.949107912342758524526189684047851,
                          -0.864864423359769072789712788640926, -0.741531185599394439863864773280788,
                          -0.586087235467691130294144845693013, -0.405845151377397166906606412076961,
@@ -286,7 +295,7 @@ DM_FN void spa_heap_down(spa_seg* h, int n, int i) {
 /* integral of `kind` whose first Kronrod pass over the whole segment is
  * `first`; *ok = 0 when the estimate is not finite or the interval budget
  * runs out before the tolerance is met */
-DM_FN dm_cplx spa_quadgk_from(int kind, const spa_quad_par* P, spa_seg first, int* ok) {
+SPA_HEAVY dm_cplx spa_quadgk_from(int kind, const spa_quad_par* P, spa_seg first, int* ok) {
     const double rtol = 1.4901161193847656e-08; /* sqrt(eps(Float64)) */
     spa_seg h[SPA_MAX_SEGS];
     h[0] = first;
@@ -343,7 +352,7 @@ DM_FN void spa_exit(const spa_quad_par* P, double ti, double* x0, double* y0, in
 
 /* jac(kd, kz) (SPASampler.jl:280-292): |d(px,py)/d(tr,kd)| by central
  * differences of four saddle-point solves (a failed solve enters as t_i = 0). */
-DM_FN double spa_jac(const SPA_LASER_T* L, spa_win* W, double tr, double kd, double kz, double Ip,
+SPA_HEAVY double spa_jac(const SPA_LASER_T* L, spa_win* W, double tr, double kd, double kz, double Ip,
                      double omega_over_F, double omega) {
     const double dtr = 0.01, dkd = 0.01;
 #define SPA_GUESS(k) (dm_asinh(omega_over_F * sqrt(((k) * (k) + kz * kz) + 2.0 * Ip)) / omega)
