@@ -282,25 +282,36 @@ def main():
             dist.barrier()
 
     # ---- device-resident timing (no spectrum copy) ------------------------------------
+    # Jobs go through the asynchronous entry points with up to 4 in flight, so the
+    # host set-up of one job overlaps the kernels of the one before; events on the
+    # library's stream bracket the timed sequence, and each job's own device time
+    # (its start/done events inside the library) gives the latency percentiles.
     for _ in range(args.warmup):
         eng.run(job, want_spectrum=False)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
+    t_start, t_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     lat, effs, launches, steps_total = [], [], 0, 0
     sync_all()
     with ClockSampler(local) as clk:
         t_wall = time.perf_counter()
+        t_start.record(stream)
+        inflight = []
         for i in range(args.steps):
-            ev[i][0].record(stream)
-            r, _, _ = eng.run(job, want_spectrum=False)
-            ev[i][1].record(stream)
-            effs.append(r.num_effective_traj)
-            launches += r.num_kernel_launches
-            steps_total += r.num_steps
+            res = abi.Result()
+            inflight.append((eng.submit(job, res), res))
+            if len(inflight) == 4 or i == args.steps - 1:
+                if i == args.steps - 1:
+                    t_end.record(stream)
+                while inflight and (len(inflight) == 4 or i == args.steps - 1):
+                    tk, r = inflight.pop(0)
+                    eng.wait(tk, r)
+                    lat.append(r.elapsed_ms)
+                    effs.append(r.num_effective_traj)
+                    launches += r.num_kernel_launches
+                    steps_total += r.num_steps
         sync_all()
         t_wall = time.perf_counter() - t_wall
-    ms = [a.elapsed_time(b) for a, b in ev]
-    t_max = torch.tensor([sum(ms)], device=dev)
+    ms = lat
+    t_max = torch.tensor([t_start.elapsed_time(t_end)], device=dev)
     if world > 1:
         dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
     eff_total = torch.tensor([float(sum(effs))], device=dev)
@@ -336,7 +347,7 @@ def main():
         achieved = flops / (kern_ms / 1e3) / 1e12 if (kern_ms and headline) else None
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": statistics.mean(ms), "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": t_max.item() / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 stages + f64 collection/deposit",
             "data": "synthetic",
             "config": {"workload": workload_text, "effective_trajectories_per_step": statistics.mean(effs),

@@ -125,6 +125,8 @@ SIGNATURES = [
     ("etraj_set_graphs", C.c_int, [C.c_void_p, C.c_int]),
     ("etraj_set_autotune", C.c_int, [C.c_void_p, C.c_int]),
     ("etraj_bulk_tile", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, _I32P, _I32P, _I32P]),
+    ("etraj_set_bulk_tile", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                      C.c_int]),
     ("etraj_stage_times", C.c_int, [C.c_void_p, _DP, C.c_int]),
     ("etraj_deposit_noalloc", C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                         C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

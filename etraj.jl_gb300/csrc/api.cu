@@ -545,6 +545,40 @@ int alloc_outputs(etraj_ctx* ctx, const DJob& J, int64_t max_n, bool with_state,
     return ETRAJ_OK;
 }
 
+// Smallest radius beyond which every exp(-b r) term of the SAE potential and
+// force is below 2^-26 Z: |a| (1 + b r) e^{-b r} (potential and force
+// brackets), |a2| r e^{-b2 r} (potential) and |a2 b2| (r^2 + sc) e^{-b2 r}
+// (force, relative to Z / r^2).  Each is decreasing beyond its maximum, so the
+// first radius past all maxima where all hold is returned (1e30: never).
+float sae_far_radius(const DTarget& T) {
+    if (T.kind != ETRAJ_TARGET_SAE) return 1e30f;
+    const double eps = std::ldexp(1.0, -26) * T.Z;
+    const double a[3] = {T.a1, T.a2, T.a3}, b[3] = {T.b1, T.b2, T.b3};
+    double rmin = 0.0;
+    for (int i = 0; i < 3; ++i) {
+        if (a[i] == 0.0) continue;
+        if (!(b[i] > 0.0)) return 1e30f;
+        rmin = std::max(rmin, 2.0 / b[i]);
+    }
+    auto ok = [&](double r) {
+        for (int i = 0; i < 3; ++i) {
+            if (a[i] == 0.0) continue;
+            const double e = std::exp(-b[i] * r);
+            if (std::fabs(a[i]) * (1.0 + b[i] * r) * e >= eps) return false;
+            if (i == 1 && std::fabs(a[i]) * r * e >= eps) return false;
+            if (i == 1 && std::fabs(a[i] * b[i]) * (r * r + T.sc) * e >= eps) return false;
+        }
+        return true;
+    };
+    double r = rmin;
+    while (!ok(r)) {
+        r *= 1.01;
+        r += 0.01;
+        if (r > 1e6) return 1e30f;
+    }
+    return (float)(r * 1.01);
+}
+
 // Bulk-integrator parameters: field table spanning [tmin, t_final] with
 // spacing T_min/512 (T_min the shortest laser period).
 void prepare_bulk(const DJob& J, double tmin, BulkParams& B) {
@@ -558,6 +592,7 @@ void prepare_bulk(const DJob& J, double tmin, BulkParams& B) {
     B.T0 = tmin - h;
     B.n_int = (int)std::ceil((J.t_final - B.T0) / h) + 2;
     B.inv_h_d = 1.0 / h;
+    B.max_iters = kBulkMaxIters;
     B.h = (float)h;
     B.inv_h = (float)(1.0 / h);
     B.t_final = J.t_final;
@@ -579,16 +614,39 @@ void prepare_bulk(const DJob& J, double tmin, BulkParams& B) {
     B.a2 = (float)T_.a2; B.b2 = (float)T_.b2;
     B.a3 = (float)T_.a3; B.b3 = (float)T_.b3;
     B.a2b2 = (float)(T_.a2 * T_.b2);
+    B.r_far = sae_far_radius(T_);
 }
 
 // ---- autotuner of the bulk integrator's launch shape ----------------------------------
-// Candidates: threads per block x blocks per SM (128 registers per thread fix
-// 16 warps per SM) x the number of free lanes a warp waits for before it
-// refills.  Each variant (dimension, phase, target, single/multi-instance) is
-// tuned once per context, on the first 2^18 electrons of its first job with
-// enough work, by timing every candidate twice with events; results do not
-// depend on the launch shape (one electron per lane, deterministic deposit).
+// Candidates: threads per block x blocks per SM x the register budget of the
+// build (<= 128 registers: 16 warps per SM; <= 85: 24 warps) x the number of
+// free lanes a warp waits for before it refills.  Each variant (dimension,
+// phase, target, single/multi-instance) is tuned once per device and process,
+// on the first 2^18 electrons of its first job with enough work, each electron
+// capped at kTuneMaxIters steps (a job's slowest trajectory would otherwise set
+// the time of every candidate), by timing every candidate twice with events.
+// The choice is kept process-wide, so the contexts of a server tune a variant
+// once between them.  Results do not depend on the launch shape (one electron
+// per lane, deterministic deposit).
 cudaEvent_t get_event(etraj_ctx* ctx);
+constexpr int kTuneMaxIters = 4096;
+
+std::mutex g_tile_mu;                             // guards g_tiles; held across a tuning run
+std::map<std::pair<int, int>, BulkTile> g_tiles;  // (device, variant) -> launch shape
+
+// The context's launch shape for a variant: its own choice, else the process-wide one.
+bool find_tile(etraj_ctx* ctx, int key, BulkTile* t) {
+    auto it = ctx->tiles.find(key);
+    if (it == ctx->tiles.end()) {
+        if (!ctx->autotune) return false;
+        std::lock_guard<std::mutex> lk(g_tile_mu);
+        auto g = g_tiles.find({ctx->device, key});
+        if (g == g_tiles.end()) return false;
+        it = ctx->tiles.emplace(key, g->second).first;
+    }
+    if (t) *t = it->second;
+    return true;
+}
 
 constexpr BulkTile kTileCandidates[] = {{256, 2, 4, 2}, {256, 2, 8, 2}, {256, 2, 2, 2}, {256, 2, 16, 2},
                                         {128, 4, 4, 2}, {128, 4, 8, 2}, {128, 3, 4, 2}, {64, 8, 4, 2},
@@ -618,8 +676,19 @@ int tuned_bulk_launch(etraj_ctx* ctx, BulkParams& B, const InitSoA& soa, const d
                       int* launches, cudaEvent_t* ev) {
     cudaStream_t s = ctx->stream;
     const int key = tile_key(B);
-    auto it = ctx->tiles.find(key);
-    if (it == ctx->tiles.end() && ctx->autotune && B.max_n >= ((int64_t)1 << 18)) {
+    BulkTile chosen = kTileDefault;
+    bool have = find_tile(ctx, key, &chosen);
+    std::unique_lock<std::mutex> tune_lk(g_tile_mu, std::defer_lock);
+    if (!have && ctx->autotune && B.max_n >= ((int64_t)1 << 18)) {
+        tune_lk.lock();  // one tuning run at a time; another context may have finished it meanwhile
+        auto g = g_tiles.find({ctx->device, key});
+        if (g != g_tiles.end()) {
+            chosen = g->second;
+            have = true;
+            ctx->tiles[key] = chosen;
+        }
+    }
+    if (!have && ctx->autotune && B.max_n >= ((int64_t)1 << 18)) {
         unsigned long long* sub = nullptr;
         ETRAJ_TRY(ensure_t(ctx, "tune.count", 1, &sub));
         *launches += launch_clamp_count(count, 1ull << 18, sub, s);
@@ -629,6 +698,7 @@ int tuned_bulk_launch(etraj_ctx* ctx, BulkParams& B, const InitSoA& soa, const d
         for (int rep = 0; rep < 2; ++rep) {
             for (int c = 0; c < nc; ++c) {
                 BulkParams Bc = B;
+                Bc.max_iters = kTuneMaxIters;
                 apply_tile(Bc, kTileCandidates[c]);
                 cudaMemsetAsync(work, 0, sizeof(unsigned long long), s);
                 cudaEventRecord(evs[(size_t)(4 * c + 2 * rep)], s);
@@ -651,9 +721,12 @@ int tuned_bulk_launch(etraj_ctx* ctx, BulkParams& B, const InitSoA& soa, const d
             }
         }
         for (auto& ev_ : evs) ctx->event_pool.push_back(ev_);
-        it = ctx->tiles.emplace(key, bt).first;
+        ctx->tiles[key] = bt;
+        g_tiles[{ctx->device, key}] = bt;
+        chosen = bt;
     }
-    apply_tile(B, it != ctx->tiles.end() ? it->second : kTileDefault);
+    if (tune_lk.owns_lock()) tune_lk.unlock();
+    apply_tile(B, chosen);
     cudaMemsetAsync(work, 0, sizeof(unsigned long long), s);
     if (ev) rec(ctx, ev[0], s);
     *launches += launch_integrate_bulk(B, soa, t, idx, count, work, out, ctx->sm_count, s);
@@ -706,7 +779,7 @@ int get_pinned(etraj_ctx* ctx, size_t bytes, PinnedBlock* out) {
 
 void put_pinned(etraj_ctx* ctx, void* p, size_t bytes) {
     if (!p) return;
-    if (ctx->pinned_pool.size() < 8) ctx->pinned_pool.push_back(PinnedBlock{p, bytes});
+    if (ctx->pinned_pool.size() < 64) ctx->pinned_pool.push_back(PinnedBlock{p, bytes});
     else cudaFreeHost(p);
 }
 
@@ -798,7 +871,7 @@ int enqueue_kernels_maybe_graph(etraj_ctx* ctx, const etraj_job* job, const Host
         B.max_n = J.n_total;
         n_int = (size_t)B.n_int;
         tile_k = tile_key(B);
-        if (ctx->autotune && !ctx->tiles.count(tile_k) && B.max_n >= ((int64_t)1 << 18)) use_graph = false;
+        if (ctx->autotune && !find_tile(ctx, tile_k, nullptr) && B.max_n >= ((int64_t)1 << 18)) use_graph = false;
         float4* tab = nullptr;  // allocate the field table outside the capture
         ETRAJ_TRY(ensure_t(ctx, "field_table", n_int * 2, &tab));
     }
@@ -810,7 +883,8 @@ int enqueue_kernels_maybe_graph(etraj_ctx* ctx, const etraj_job* job, const Host
     k += sizeof J;
     std::memcpy(k, &P, sizeof P);
     k += sizeof P;
-    const BulkTile t = ctx->tiles.count(tile_k) ? ctx->tiles[tile_k] : kTileDefault;
+    BulkTile t = kTileDefault;
+    find_tile(ctx, tile_k, &t);
     const int extra[3] = {job->precision, t.threads * 1000 + t.blocks_per_sm * 10 + t.occ, t.refill_min};
     std::memcpy(k, extra, sizeof extra);
     k += sizeof extra;
@@ -1743,12 +1817,25 @@ int etraj_bulk_tile(etraj_ctx* ctx, int dimension, int phase, int target, int mu
     if (!ctx) return ETRAJ_ERR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> lk(ctx->mu);
     const int key = (multi ? 1000 : 0) + dimension * 100 + phase * 10 + target;
-    auto it = ctx->tiles.find(key);
-    const BulkTile t = (it != ctx->tiles.end()) ? it->second : kTileDefault;
+    BulkTile t = kTileDefault;
+    const bool found = find_tile(ctx, key, &t);
     if (threads) *threads = t.threads;
     if (blocks_per_sm) *blocks_per_sm = t.blocks_per_sm;
     if (refill_min) *refill_min = t.refill_min;
-    return (it != ctx->tiles.end()) ? ETRAJ_OK : ETRAJ_ERR_NOT_FOUND;
+    return found ? ETRAJ_OK : ETRAJ_ERR_NOT_FOUND;
+}
+
+int etraj_set_bulk_tile(etraj_ctx* ctx, int dimension, int phase, int target, int multi, int threads,
+                        int blocks_per_sm, int refill_min) {
+    if (!ctx) return ETRAJ_ERR_INVALID_ARGUMENT;
+    const int warps = (threads / 32) * blocks_per_sm;
+    if ((threads != 64 && threads != 128 && threads != 256) || blocks_per_sm < 1 || warps > 24 ||
+        refill_min < 1 || refill_min > 32)
+        return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    const int key = (multi ? 1000 : 0) + dimension * 100 + phase * 10 + target;
+    ctx->tiles[key] = BulkTile{threads, blocks_per_sm, refill_min, warps > 16 ? 3 : 2};
+    return ETRAJ_OK;
 }
 
 int etraj_stage_times(etraj_ctx* ctx, double* ms, int n) {

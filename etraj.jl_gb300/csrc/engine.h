@@ -157,7 +157,10 @@ struct BulkParams {
     int nf;             // t_final = T0 + h (nf + ff)
     float ff;
     float Z, Ip, sc, a1, b1, a2, b2, a3, b3, a2b2;
+    float r_far;        // SAE: radius beyond which the exp(-b r) terms are dropped
+    int max_iters;      // steps before an electron is given up (status 1)
 };
+constexpr int kBulkMaxIters = 1000000;  // OrdinaryDiffEq's default maxiters
 int launch_field_table(const DJob& J, double T0, double h, int n_int, float4* tab, cudaStream_t s);
 // *out = min(*count, cap) (the autotuner's sample of the electrons)
 int launch_clamp_count(const unsigned long long* count, unsigned long long cap, unsigned long long* out,

@@ -100,7 +100,6 @@ __constant__ float cBTA[7] = {(float)bta(0), (float)bta(1), (float)bta(2), (floa
 
 constexpr float ABSTOL = 1e-6f, BETA1 = 0.14f, BETA2 = 0.08f, QMIN_INV = 5.0f, QMAX_INV = 0.1f,
                 INV_GAMMA = 1.0f / 0.9f, LOG2_QOLDINIT = -13.287712379549449f;  // log2(1e-4)
-constexpr int MAXITERS = 1000000;
 constexpr float kDthMin = 2.4e-7f;  // smallest step (in table intervals) the FP32 clock resolves
 
 __device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
@@ -151,11 +150,29 @@ __device__ __forceinline__ void accel(const BulkParams& P, const float4* __restr
     } else {
         const float r = r2 * rsqrt_nr(fmaxf(r2, 1e-30f));
         const float ris = rsqrt_nr(r2 + P.sc);
-        const float e1 = __expf(-P.b1 * r), e2 = __expf(-P.b2 * r), e3 = __expf(-P.b3 * r);
-        const float br = fmaf(P.a3 * fmaf(P.b3, r, 1.0f), e3, fmaf(P.a1 * fmaf(P.b1, r, 1.0f), e1, P.Z));
-        coef = -fmaf(ris * ris * ris, br, P.a2b2 * ris * e2);
+        // Beyond r_far (host: every exp(-b r) term below 2^-26 of the sum it
+        // joins) each lane takes its exponentials as exactly 0.  fmaf(x, 0, y) is
+        // y, so when all active lanes are that far the short form below gives
+        // the same bits as the full one: a lane's result never depends on which
+        // electrons share its warp.
+        const bool far = r > P.r_far;
+        float br, num;
+        if (__all_sync(__activemask(), far)) {
+            br = P.Z;
+            coef = -((ris * ris * ris) * br);
+            num = P.Z;
+        } else {
+            float e1 = 0.0f, e2 = 0.0f, e3 = 0.0f;
+            if (!far) {
+                e1 = __expf(-P.b1 * r);
+                e2 = __expf(-P.b2 * r);
+                e3 = __expf(-P.b3 * r);
+            }
+            br = fmaf(P.a3 * fmaf(P.b3, r, 1.0f), e3, fmaf(P.a1 * fmaf(P.b1, r, 1.0f), e1, P.Z));
+            coef = -fmaf(ris * ris * ris, br, P.a2b2 * ris * e2);
+            num = fmaf(P.a3, e3, fmaf(P.a2 * r, e2, fmaf(P.a1, e1, P.Z)));
+        }
         if (PHASE != ETRAJ_PHASE_CTMC) {
-            const float num = fmaf(P.a3, e3, fmaf(P.a2 * r, e2, fmaf(P.a1, e1, P.Z)));
             // the 2D SCTS reference divides by r^2+sc, not its square root (SAEAtom.jl:316)
             V = (DIM == 2 && PHASE == ETRAJ_PHASE_SCTS) ? num * (ris * ris) : num * ris;
         }
@@ -370,7 +387,7 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
             if (last) dth = remaining;
             int status = 0;
             if (!(dth == dth)) status = 4;
-            else if (iter > MAXITERS) status = 1;
+            else if (iter > P.max_iters) status = 1;
             else if (dth < kDthMin && !last) status = 2;
             if (status == 0) {
                 const float dt = dth * hh, dt2 = dt * dt;

@@ -204,6 +204,11 @@ class Engine:
             self._check(st)
         return t.value, b.value, r.value, st == abi.OK
 
+    def set_bulk_tile(self, dimension, phase, target, threads, blocks_per_sm, refill_min, multi=False):
+        """Pin a bulk-integrator variant's launch shape on this engine."""
+        self._check(self.lib.etraj_set_bulk_tile(self.ctx, dimension, phase, target, 1 if multi else 0,
+                                                 threads, blocks_per_sm, refill_min))
+
     def run_batch(self, jobs, want_spectrum=True, want_amplitude=False, weights=None):
         """Run up to 64 FP32-bulk jobs (same dimension, phase, rtol, target and grid)
         as one batch; returns [(result, spectrum, amplitude)] and, with `weights`,

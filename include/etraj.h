@@ -267,15 +267,22 @@ int etraj_set_graphs(etraj_ctx* ctx, int enable);
 /* ---- autotuner --------------------------------------------------------------------
  * No counterpart in the reference.  The FP32-bulk integrator's launch shape
  * (threads per block, blocks per SM, free lanes a warp waits for before it
- * refills) is tuned once per context and kernel variant on the first 2^18
- * electrons of the first job with enough work, by timing 8 candidates; results
- * never depend on it.  etraj_set_autotune(ctx, 0) switches tuning off and
- * returns to the fixed shape 256 x 2 x 4.  etraj_bulk_tile reports the shape
- * in use for a variant (ETRAJ_ERR_NOT_FOUND: not tuned yet, fixed shape
- * reported). */
+ * refills, and with it the register budget of the build: <= 128 registers per
+ * thread up to 16 warps per SM, <= 85 up to 24) is tuned once per device,
+ * process and kernel variant on the first 2^18 electrons of the first job with
+ * enough work (each capped at 4096 steps), by timing 12 candidates; every
+ * context of the process then uses that choice.  Results never depend on the
+ * shape.  etraj_set_autotune(ctx, 0) switches tuning off for the context and
+ * returns it to the fixed shape 256 x 2 x 4.  etraj_bulk_tile reports the
+ * shape in use for a variant (ETRAJ_ERR_NOT_FOUND: not tuned yet, fixed shape
+ * reported).  etraj_set_bulk_tile pins a variant's shape on one context
+ * (threads 64, 128 or 256; at most 24 warps per SM; refill_min 1..32);
+ * ETRAJ_ERR_INVALID_ARGUMENT for any other. */
 int etraj_set_autotune(etraj_ctx* ctx, int enable);
 int etraj_bulk_tile(etraj_ctx* ctx, int dimension, int phase, int target, int multi, int* threads,
                     int* blocks_per_sm, int* refill_min);
+int etraj_set_bulk_tile(etraj_ctx* ctx, int dimension, int phase, int target, int multi, int threads,
+                        int blocks_per_sm, int refill_min);
 
 /* ---- diagnostics ----------------------------------------------------------------
  * Device time (ms) of the stages of the last etraj_run on this context: sampling,

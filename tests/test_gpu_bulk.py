@@ -134,3 +134,39 @@ def test_autotuned_shape_changes_no_result():
     assert np.array_equal(s1, s2) and np.array_equal(a1, a2)
     tuned.close()
     fixed.close()
+
+
+TILES = [(256, 2, 4), (256, 2, 16), (128, 4, 1), (64, 8, 32), (256, 3, 4), (128, 6, 8), (64, 12, 2), (64, 1, 4)]
+
+
+@pytest.mark.parametrize("dim,pname", [(2, "SCTS"), (3, "QTMC")])
+def test_every_launch_shape_gives_the_same_bits(dim, pname):
+    """Launch shapes of both register budgets (16 and 24 warps per SM), tiny and
+    wide refill thresholds, and a one-block-per-SM launch: one electron per lane
+    and the warp-uniform far-field branch of the SAE force keep every bit."""
+    phase = {"SCTS": abi.PHASE_SCTS, "QTMC": abi.PHASE_QTMC}[pname]
+    job = bulk(job_of(method="SPANE", dim=dim, phase=pname, target="Ar", laser="cos2",
+                      ellip=1.0, mc=True, nt=300, nkd=200, nkz=1 if dim == 2 else 4,
+                      pnum=(120, 120) if dim == 2 else (48, 48, 16), pmax=2.0))
+    eng = et.Engine(device=0)
+    ref = None
+    for th, bps, rf in TILES:
+        eng.set_bulk_tile(dim, phase, abi.TARGET_SAE, th, bps, rf)
+        assert eng.bulk_tile(dim, phase, abi.TARGET_SAE)[:3] == (th, bps, rf)
+        out = eng.run(job, want_amplitude=phase != abi.PHASE_CTMC)
+        if ref is None:
+            ref = out
+            assert out[0].num_effective_traj > 0
+            continue
+        assert out[0].num_effective_traj == ref[0].num_effective_traj and out[0].ion_prob == ref[0].ion_prob
+        assert out[0].num_steps == ref[0].num_steps
+        assert np.array_equal(out[1], ref[1]) and np.array_equal(out[2], ref[2])
+    eng.close()
+
+
+def test_set_bulk_tile_rejects_bad_shapes():
+    eng = et.Engine(device=0)
+    for th, bps, rf in [(96, 2, 4), (256, 4, 4), (128, 0, 4), (128, 2, 0), (128, 2, 33)]:
+        with pytest.raises(et.EtrajError):
+            eng.set_bulk_tile(2, abi.PHASE_SCTS, abi.TARGET_SAE, th, bps, rf)
+    eng.close()
