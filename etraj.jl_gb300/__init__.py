@@ -8,12 +8,14 @@ from .abi import load_library
 from .lasers import (Laser, MonochromaticLaser, Cos4Laser, Cos2Laser, GaussianLaser,
                      BichromaticLaser)
 from .targets import (Target, SAEAtomBase, HydrogenLikeAtom, SAEAtom, get_atom,
-                      get_available_atoms, hartree_asymp_coeff)
+                      get_available_atoms, hartree_asymp_coeff, MoleculeBase, GenericMolecule,
+                      LoadMolecule, get_mol, get_available_mols)
 from .simulation import (perform_traj_simulation, make_job, rate_prefix_bits, Engine, Server,
                          EtrajError, default_engine)
 
 __all__ = ["load_library", "Laser", "MonochromaticLaser", "Cos4Laser", "Cos2Laser",
            "GaussianLaser", "BichromaticLaser", "Target", "SAEAtomBase", "HydrogenLikeAtom",
-           "SAEAtom", "get_atom", "get_available_atoms", "hartree_asymp_coeff",
+           "SAEAtom", "get_atom", "get_available_atoms", "hartree_asymp_coeff", "MoleculeBase",
+           "GenericMolecule", "LoadMolecule", "get_mol", "get_available_mols",
            "perform_traj_simulation", "make_job", "rate_prefix_bits", "Engine", "Server",
            "EtrajError", "default_engine"]

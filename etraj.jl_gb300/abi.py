@@ -21,8 +21,9 @@ ERR_NOT_READY = 6
 ERR_NOT_FOUND = 7
 
 LASER_COS4, LASER_COS2, LASER_GAUSSIAN, LASER_BICHROMATIC = 0, 1, 2, 3
-TARGET_HYDROGEN_LIKE, TARGET_SAE = 0, 1
-SAMPLER_ADK, SAMPLER_SPANE, SAMPLER_SPA = 0, 1, 2
+TARGET_HYDROGEN_LIKE, TARGET_SAE, TARGET_MOLECULE = 0, 1, 2
+MOL_MAX_L = 6
+SAMPLER_ADK, SAMPLER_SPANE, SAMPLER_SPA, SAMPLER_WFAT = 0, 1, 2, 3
 PREFIX_PRE, PREFIX_PRECC, PREFIX_JAC = 1, 2, 4
 PHASE_CTMC, PHASE_QTMC, PHASE_SCTS = 0, 1, 2
 PRECISION_FP64, PRECISION_FP32_BULK = 0, 1
@@ -46,7 +47,12 @@ class Target(C.Structure):
                 ("quan_ax_theta", C.c_double), ("quan_ax_phi", C.c_double),
                 ("a1", C.c_double), ("b1", C.c_double), ("a2", C.c_double),
                 ("b2", C.c_double), ("a3", C.c_double), ("b3", C.c_double),
-                ("soft_core", C.c_double)]
+                ("soft_core", C.c_double),
+                ("mol_rot", C.c_double * 3), ("mol_Ip_traj", C.c_double),
+                ("asymp_lmax", C.c_int32), ("wfat_nxi_max", C.c_int32), ("wfat_m_max", C.c_int32),
+                ("wfat_lmax", C.c_int32),
+                ("asymp_coeff_lm", C.POINTER(C.c_double)), ("wfat_intdata", C.POINTER(C.c_double)),
+                ("wfat_mu", C.c_double * 3)]
 
 
 class Job(C.Structure):
@@ -84,6 +90,9 @@ class Job(C.Structure):
     def copy(self):
         j = Job()
         C.pointer(j)[0] = self
+        keep = getattr(self, "_keep", None)
+        if keep is not None:
+            j._keep = keep  # arrays the target's pointers refer to
         return j
 
 

@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "mol_check.h"
 
 using namespace etraj;
 
@@ -128,6 +129,7 @@ double u53_host(uint32_t a, uint32_t b) {
 struct HostJob {
     DJob J;
     std::vector<double> t, kd, kz;
+    std::vector<double> mol_clm, mol_wint;  // molecular target: copies of the caller's tables
 };
 
 int validate_job(const etraj_job* job, std::string& err) {
@@ -140,7 +142,7 @@ int validate_job(const etraj_job* job, std::string& err) {
     if (job->dimension != 2 && job->dimension != 3)
         return fail("[TrajectorySimulationJob] `dimension` must be either 2 or 3.");
     if (job->init_cond_method != ETRAJ_SAMPLER_ADK && job->init_cond_method != ETRAJ_SAMPLER_SPANE &&
-        job->init_cond_method != ETRAJ_SAMPLER_SPA)
+        job->init_cond_method != ETRAJ_SAMPLER_SPA && job->init_cond_method != ETRAJ_SAMPLER_WFAT)
         return fail("[ElectronSamplers] Undefined initial condition method.");
     if (job->traj_phase_method < 0 || job->traj_phase_method > 2)
         return fail("[ADKSampler] Undefined phase method.");
@@ -182,14 +184,25 @@ int validate_job(const etraj_job* job, std::string& err) {
     }
     if (grid >= (int64_t)0xFFFFFFFFll) return fail("momentum grid too large (>= 2^32 bins).");
     const etraj_target& T = job->target;
-    if (!(T.Ip > 0)) return fail("[SAEAtom] Ip should be positive.");
-    if (!(T.l >= 0 && T.l >= std::abs(T.m))) return fail("[SAEAtom] Invalid (l,m).");
-    if (T.l > kMaxL) {
-        err = "angular quantum number l > 4 is not supported.";
-        return ETRAJ_ERR_UNSUPPORTED;
+    const char* mmsg = nullptr;
+    const int mst = etraj_mol_check(job, &mmsg);
+    if (mst > 0) {
+        err = mmsg;
+        return mst;
     }
-    if (!(T.asymp_coeff > 0)) return fail("[SAEAtom] asymp_coeff should be either `:hartree` or a positive number.");
-    if (T.kind == ETRAJ_TARGET_SAE) {
+    if (mst < 0) {
+        if (!(T.Ip > 0)) return fail("[SAEAtom] Ip should be positive.");
+        if (!(T.l >= 0 && T.l >= std::abs(T.m))) return fail("[SAEAtom] Invalid (l,m).");
+        if (T.l > kMaxL) {
+            err = "angular quantum number l > 4 is not supported.";
+            return ETRAJ_ERR_UNSUPPORTED;
+        }
+        if (!(T.asymp_coeff > 0))
+            return fail("[SAEAtom] asymp_coeff should be either `:hartree` or a positive number.");
+    }
+    if (T.kind == ETRAJ_TARGET_MOLECULE) {
+        // trajectories: Coulomb tail with soft core 1.0 (GenericMolecule.jl:444-445)
+    } else if (T.kind == ETRAJ_TARGET_SAE) {
         if (!(T.b1 >= 0 && T.b2 >= 0 && T.b3 >= 0)) return fail("[SAEAtom] b1,b2,b3 should be non-negative.");
         if (!(T.soft_core > 0)) return fail("[SAEAtom] soft_core should be positive.");
     } else if (T.kind == ETRAJ_TARGET_HYDROGEN_LIKE) {
@@ -268,6 +281,45 @@ void prepare_job(const etraj_job* job, HostJob& H) {
     J.l = T.l;
     J.m = T.m;
     J.C = T.asymp_coeff;
+    if (T.kind == ETRAJ_TARGET_MOLECULE) {
+        // GenericMolecule's trajectories are the hydrogen-like equations with
+        // Z = charge + 1, soft core 1.0 and the phase's Ip = IonPotential(mol)
+        // (GenericMolecule.jl:438-445); the sampler uses the orbital's Ip (J.Ip)
+        J.target.kind = ETRAJ_TARGET_HYDROGEN_LIKE;
+        J.target.Ip = T.mol_Ip_traj;
+        J.target.sc = 1.0;
+        J.target.skip_ok = 0;
+        J.l = 0;
+        J.m = 0;
+        J.C = 0.0;
+        DMol& M = J.mol;
+        M.on = 1;
+        M.wfat = (J.method == ETRAJ_SAMPLER_WFAT) ? 1 : 0;
+        for (int i = 0; i < 3; ++i) {
+            M.rot[i] = T.mol_rot[i];
+            M.mu[i] = T.wfat_mu[i];
+        }
+        const double kap = std::sqrt(2.0 * T.Ip);
+        if (M.wfat) {
+            M.nxi = T.wfat_nxi_max;
+            M.mmax = T.wfat_m_max;
+            M.wl = T.wfat_lmax;
+            const size_t n = (size_t)(M.nxi + 1) * (size_t)(2 * M.mmax + 1) * (size_t)(M.wl + 1) * (size_t)(2 * M.wl + 1);
+            H.mol_wint.assign(T.wfat_intdata, T.wfat_intdata + 2 * n);
+            M.stride = (M.nxi + 1) * (2 * M.mmax + 1) + (M.nxi + 1) * (M.mmax + 1);
+        } else {
+            const int L = T.asymp_lmax;
+            H.mol_clm.assign(T.asymp_coeff_lm, T.asymp_coeff_lm + 2 * (size_t)(L + 1) * (size_t)(2 * L + 1));
+            mol_terms_build(L, H.mol_clm.data(), &M.T);
+            for (int l = 0; l <= L; ++l)
+                for (int mp = -l; mp <= l; ++mp) {
+                    const dm_cplx P = mol_sph_prefactor(l, mp, kap);
+                    M.P[2 * (l * l + l + mp)] = P.re;
+                    M.P[2 * (l * l + l + mp) + 1] = P.im;
+                }
+            M.stride = std::max(2 * M.T.ncd, 2);
+        }
+    }
     J.q_theta = T.quan_ax_theta;
     J.q_phi = T.quan_ax_phi;
     J.kappa = std::sqrt(2.0 * J.Ip);
@@ -498,9 +550,19 @@ struct Pipeline {
         if (_st != ETRAJ_OK) return _st; \
     } while (0)
 
-int alloc_sampling(etraj_ctx* ctx, const HostJob& H, Pipeline& P) {
+int alloc_sampling(etraj_ctx* ctx, HostJob& H, Pipeline& P) {
     const DJob& J = H.J;
     const size_t n = (size_t)J.n_total;
+    if (J.mol.on) {
+        // the molecular tables; their addresses go into the device job
+        double *clm = nullptr, *wint = nullptr, *tab = nullptr;
+        if (!H.mol_clm.empty()) ETRAJ_TRY(ensure_t(ctx, "mol.clm", H.mol_clm.size(), &clm));
+        if (!H.mol_wint.empty()) ETRAJ_TRY(ensure_t(ctx, "mol.wint", H.mol_wint.size(), &wint));
+        ETRAJ_TRY(ensure_t(ctx, "mol.tab", (size_t)J.n_t * (size_t)J.mol.stride, &tab));
+        H.J.mol.clm = clm;
+        H.J.mol.wint = wint;
+        H.J.mol.tab = tab;
+    }
     ETRAJ_TRY(ensure_t(ctx, "t", H.t.size(), &P.t));
     ETRAJ_TRY(ensure_t(ctx, "kd", H.kd.size(), &P.kd));
     ETRAJ_TRY(ensure_t(ctx, "kz", H.kz.size(), &P.kz));
@@ -543,6 +605,19 @@ int alloc_outputs(etraj_ctx* ctx, const DJob& J, int64_t max_n, bool with_state,
     ETRAJ_TRY(ensure_t(ctx, "counters", 1, &P.counters));
     ETRAJ_TRY(ensure_t(ctx, "work", 4, &P.work));
     return ETRAJ_OK;
+}
+
+// Copies a job's host inputs (time and momentum samples, molecular tables) to the device.
+void upload_inputs(const HostJob& H, const Pipeline& P, cudaStream_t s) {
+    cudaMemcpyAsync(P.t, H.t.data(), H.t.size() * sizeof(double), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(P.kd, H.kd.data(), H.kd.size() * sizeof(double), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(P.kz, H.kz.data(), H.kz.size() * sizeof(double), cudaMemcpyHostToDevice, s);
+    if (!H.mol_clm.empty())
+        cudaMemcpyAsync((void*)H.J.mol.clm, H.mol_clm.data(), H.mol_clm.size() * sizeof(double),
+                        cudaMemcpyHostToDevice, s);
+    if (!H.mol_wint.empty())
+        cudaMemcpyAsync((void*)H.J.mol.wint, H.mol_wint.data(), H.mol_wint.size() * sizeof(double),
+                        cudaMemcpyHostToDevice, s);
 }
 
 // Smallest radius beyond which every exp(-b r) term of the SAE potential and
@@ -837,7 +912,8 @@ int enqueue_kernels(etraj_ctx* ctx, const etraj_job* job, const HostJob& H, cons
     int launches = 0;
     rec(ctx, ctx->stage_ev[0], s);
     launches += launch_batch_prepare(J, P.t, P.batches, s);
-    if (job->precision == ETRAJ_PRECISION_FP32_BULK && J.method != ETRAJ_SAMPLER_SPA && J.cutoff >= kSample32MinCutoff)
+    if (job->precision == ETRAJ_PRECISION_FP32_BULK && J.method != ETRAJ_SAMPLER_SPA && !J.mol.on &&
+        J.cutoff >= kSample32MinCutoff)
         launches += launch_sample32_range(J, 0, J.n_t, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s);
     else
         launches += launch_sample_range(J, 0, J.n_t, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s);
@@ -969,9 +1045,7 @@ int enqueue_job(etraj_ctx* ctx, const etraj_job* job, JobRec& r) {
         r.ev_done = ctx->ev1;
     }
     cudaStream_t s = ctx->stream;
-    cudaMemcpyAsync(P.t, H.t.data(), H.t.size() * sizeof(double), cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(P.kd, H.kd.data(), H.kd.size() * sizeof(double), cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(P.kz, H.kz.data(), H.kz.size() * sizeof(double), cudaMemcpyHostToDevice, s);
+    upload_inputs(H, P, s);
     cudaEventRecord(r.ev_start, s);
     int launches = 0;
     ETRAJ_TRY(enqueue_kernels_maybe_graph(ctx, job, H, P, &launches));
@@ -1050,6 +1124,9 @@ int run_batch(etraj_ctx* ctx, const etraj_job* jobs, int n, etraj_result* res, c
         const int st = validate_job(&jobs[i], err);
         if (st != ETRAJ_OK) return set_err(ctx, st, "job " + std::to_string(i) + ": " + err);
         const etraj_job& ji = jobs[i];
+        if (ji.target.kind == ETRAJ_TARGET_MOLECULE)
+            return set_err(ctx, ETRAJ_ERR_UNSUPPORTED,
+                           "etraj_run_batch: molecular targets are run one job at a time (etraj_run, etraj_submit)");
         bool same = ji.precision == ETRAJ_PRECISION_FP32_BULK && ji.dimension == j0.dimension &&
                     ji.traj_phase_method == j0.traj_phase_method && ji.traj_rtol == j0.traj_rtol &&
                     std::memcmp(&ji.target, &j0.target, sizeof ji.target) == 0;
@@ -1264,9 +1341,7 @@ int sample_range(etraj_ctx* ctx, const etraj_job* job, int64_t b0, int64_t nb, d
     Pipeline P;
     ETRAJ_TRY(alloc_sampling(ctx, H, P));
     cudaStream_t s = ctx->stream;
-    cudaMemcpyAsync(P.t, H.t.data(), H.t.size() * sizeof(double), cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(P.kd, H.kd.data(), H.kd.size() * sizeof(double), cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(P.kz, H.kz.data(), H.kz.size() * sizeof(double), cudaMemcpyHostToDevice, s);
+    upload_inputs(H, P, s);
     launch_batch_prepare(H.J, P.t, P.batches, s);
     launch_sample_range(H.J, b0, nb, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s);
     cudaError_t e = cudaGetLastError();

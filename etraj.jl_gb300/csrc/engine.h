@@ -12,6 +12,7 @@
 
 #include "../../include/etraj.h"
 #include "detmath.h"
+#include "mol.h"
 #include "sae_skip.h"
 
 namespace etraj {
@@ -56,6 +57,21 @@ struct DBatch {
 
 constexpr int kMaxL = 4;
 
+// Molecular targets (mol.h): the ionizing orbital's tables on the device.
+struct DMol {
+    int on;              // molecular target
+    int wfat;            // WFAT sampler (else the MO-ADK prefix of ADK/SPANE/SPA)
+    mol_terms T;         // MO-ADK: (l, m) pairs with C_lm != 0
+    int nxi, mmax, wl;   // WFAT: channels n_xi <= nxi, |m| <= mmax; integrals l <= wl
+    int stride;          // doubles per time sample in tab
+    double rot[3];       // MolRotation
+    double mu[3];        // WFAT orbital dipole
+    double P[2 * MOL_NLM];   // Y_{l m'} prefactors (complex)
+    const double* clm;   // C_lm (device copy)
+    const double* wint;  // WFAT integrals (device copy)
+    double* tab;         // per time sample: C D (MO-ADK) or |G|^2 and the W factors (WFAT)
+};
+
 struct DJob {
     // sampling
     int method, dim, mc, prefix, phase, rows, mono, l, m;
@@ -75,6 +91,7 @@ struct DJob {
     int64_t grid;
     DLaser laser;
     DTarget target;
+    DMol mol;
 };
 
 // Sampled electrons, candidate-indexed structure of arrays.

@@ -1,9 +1,10 @@
-// sampler.cu -- ADK, SPANE and SPA initial-condition sampling on the device.
+// sampler.cu -- ADK, SPANE, SPA and WFAT initial-condition sampling on the device.
 //
 // Reference: gen_electron_batch in src/ElectronSamplers/ADKSampler.jl:167-396,
-// SPANESampler.jl:163-404 and SPASampler.jl:150-431, with the helpers of
-// shared_methods.jl:4-47.  The SPA saddle-point solve and quadratures are in
-// spa.h, shared with the CPU oracle.
+// SPANESampler.jl:163-404, SPASampler.jl:150-431 and WFATSampler.jl:129-249,
+// with the helpers of shared_methods.jl:4-47.  The SPA saddle-point solve and
+// quadratures are in spa.h, the molecular prefactor and the WFAT rate in
+// mol.h, both shared with the CPU oracle.
 //
 // Layout: one thread per candidate (time sample b, transverse-momentum
 // sample i), candidates in the reference's loop order (kd outer, kz inner;
@@ -154,6 +155,32 @@ __global__ void k_batch_prepare(const __grid_constant__ DJob J, const double* __
     out[b] = B;
 }
 
+// Per-time-sample tables of a molecular target: one block per time sample,
+// threads over the table's entries (MO-ADK: C_lm D^l_{m' m}; WFAT: |G|^2 of
+// each channel and the time-sample factors of W).
+__global__ void __launch_bounds__(128) k_mol_prepare(const __grid_constant__ DJob J, const DBatch* __restrict__ batches) {
+    const DMol& M = J.mol;
+    for (int64_t b = blockIdx.x; b < J.n_t; b += gridDim.x) {
+        const DBatch& B = batches[b];
+        double a, be, g;
+        mol_euler(M.rot, B.Fx, B.Fy, B.F, &a, &be, &g);
+        double* out = M.tab + b * (int64_t)M.stride;
+        if (M.wfat) {
+            const int nch = (M.nxi + 1) * (2 * M.mmax + 1), na = (M.nxi + 1) * (M.mmax + 1);
+            for (int c = threadIdx.x; c < nch + na; c += blockDim.x) {
+                out[c] = (c < nch) ? mol_wfat_g2(c, M.nxi, M.mmax, M.wl, M.wint, M.mu, J.kappa, be, g)
+                                   : mol_wfat_A(c - nch, M.nxi, J.kappa, J.nstar, B.F);
+            }
+        } else {
+            for (int e = threadIdx.x; e < M.T.ncd; e += blockDim.x) {
+                const dm_cplx v = mol_cd_entry(&M.T, M.clm, e, a, be, g);
+                out[2 * e] = v.re;
+                out[2 * e + 1] = v.im;
+            }
+        }
+    }
+}
+
 // The k-sum of the solid harmonic (shared_methods.jl:21).
 __device__ dm_cplx sph_sum(int l, int m, dm_cplx x, dm_cplx y, dm_cplx z) {
     dm_cplx xp = dm_c(x.re - y.im, x.im + y.re);
@@ -174,11 +201,14 @@ __device__ dm_cplx sph_sum(int l, int m, dm_cplx x, dm_cplx y, dm_cplx z) {
 }
 
 // Sum over m' of C D^l_{m' m} Y_{l m'} (ADKSampler.jl:243-265).
-__device__ dm_cplx pre_numerator(const DJob& J, const DBatch& B, dm_cplx kx, dm_cplx ky, dm_cplx kz) {
+// Molecules: sum over (l, m, m') of C_lm D^l_{m' m} Y_{l m'} (mol.h), with
+// the time sample's C D table.
+__device__ dm_cplx pre_numerator(const DJob& J, const DBatch& B, int64_t b, dm_cplx kx, dm_cplx ky, dm_cplx kz) {
     dm_cplx ckx = dm_cconj(kx), cky = dm_cconj(ky), ckz = dm_cconj(kz);
     dm_cplx nkx = dm_cadd(dm_cadd(dm_cscale(ckx, 0.0), dm_cscale(cky, 0.0)), dm_cscale(ckz, 1.0));
     dm_cplx nky = dm_cadd(dm_cadd(dm_cscale(ckx, B.ny0), dm_cscale(cky, B.ny1)), dm_cscale(ckz, 0.0));
     dm_cplx nkz = dm_cadd(dm_cadd(dm_cscale(ckx, B.nz0), dm_cscale(cky, B.nz1)), dm_cscale(ckz, 0.0));
+    if (J.mol.on) return mol_numerator(&J.mol.T, J.mol.tab + b * (int64_t)J.mol.stride, J.mol.P, nkx, nky, nkz);
     dm_cplx acc = dm_c(0.0, 0.0);
     for (int mp = -J.l; mp <= J.l; ++mp) {
         int i = mp + J.l;
@@ -218,7 +248,21 @@ k_sample(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double* _
         }
         uint8_t keep = 0;
         double x0 = 0.0, y0 = 0.0, kx0 = 0.0, ky0 = 0.0, rate = 0.0, ph = 0.0;
-        if (!(fabs(kd0) < 1e-4)) {
+        if (J.method == ETRAJ_SAMPLER_WFAT) {
+            // WFATSampler.jl:173-240: ADK's exit point, the WFAT rate, CTMC rows
+            if (!(kd0 * kd0 + kz0 * kz0 < 1e-4 * 1e-4)) {
+                const double F = B.F;
+                kx0 = kd0 * (-B.sphi);
+                ky0 = kd0 * B.cphi;
+                const double r0 = (J.Ip + (kd0 * kd0 + kz0 * kz0) / 2.0) / F;
+                x0 = r0 * B.cphi;
+                y0 = r0 * B.sphi;
+                const double* tb = J.mol.tab + b * (int64_t)J.mol.stride;
+                const int nch = (J.mol.nxi + 1) * (2 * J.mol.mmax + 1);
+                rate = mol_wfat_rate(J.mol.nxi, J.mol.mmax, tb, tb + nch, J.kappa, F, kd0, kz0, J.dkdt);
+                keep = (!(rate != rate) && !(rate < J.cutoff)) ? 1 : 0;
+            }
+        } else if (!(fabs(kd0) < 1e-4)) {
             const double Ip = J.Ip, F = B.F;
             kx0 = kd0 * (-B.sphi);
             ky0 = kd0 * B.cphi;
@@ -259,7 +303,7 @@ k_sample(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double* _
                         kx = dm_c(kx0 + h * B.dFx, -(ti * B.Fx));
                         ky = dm_c(ky0 + h * B.dFy, -(ti * B.Fy));
                     }
-                    dm_cplx num = pre_numerator(J, B, kx, ky, kz);
+                    dm_cplx num = pre_numerator(J, B, b, kx, ky, kz);
                     double cpre = (J.prefix & ETRAJ_PREFIX_PRE) ? J.c : B.c_cc;
                     double den = (J.e_pre == 0.5) ? sqrt(X2) : dm_pow_pos(X2, J.e_pre);
                     dm_cplx pre = dm_cscale(num, cpre);
@@ -443,7 +487,7 @@ k_sample_spa(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const doubl
                     dm_cplx amp = dm_cscale(dm_cexp(iS), sqrt(J.dkdt));
                     if (J.prefix & (ETRAJ_PREFIX_PRE | ETRAJ_PREFIX_PRECC)) {
                         const dm_cplx kx = dm_c(px + Ax.re, Ax.im), ky = dm_c(py + Ay.re, Ay.im);
-                        const dm_cplx num = pre_numerator(J, B, kx, ky, dm_c(kz0, 0.0));
+                        const dm_cplx num = pre_numerator(J, B, b, kx, ky, dm_c(kz0, 0.0));
                         const double cpre = (J.prefix & ETRAJ_PREFIX_PRE) ? J.c : B.c_cc;
                         const dm_cplx kF = dm_caddr(dm_cadd(dm_cmul(kx, Fx), dm_cmul(ky, Fy)), kz0 * 0.0);
                         const dm_cplx den = spa_cpow(kF, (J.nstar + 1.0) / 2.0);
@@ -477,7 +521,10 @@ int launch_batch_prepare(const DJob& J, const double* t, DBatch* batches, cudaSt
     int threads = 64;  // few, FP64-heavy threads: spread them over every SM
     int blocks = (int)((J.n_t + threads - 1) / threads);
     k_batch_prepare<<<blocks, threads, 0, s>>>(J, t, batches);
-    return 1;
+    if (!J.mol.on) return 1;
+    const int64_t mb = J.n_t < ((int64_t)1 << 20) ? J.n_t : ((int64_t)1 << 20);
+    k_mol_prepare<<<(unsigned)(mb > 0 ? mb : 1), 128, 0, s>>>(J, batches);
+    return 2;
 }
 
 int launch_sample_range(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,

@@ -16,11 +16,14 @@ import numpy as np
 
 from . import abi
 from .lasers import Laser, MonochromaticLaser, BichromaticLaser
-from .targets import Target, SAEAtomBase
+from .targets import Target, SAEAtomBase, MoleculeBase
 
-_METHODS = {"ADK": abi.SAMPLER_ADK, "SPANE": abi.SAMPLER_SPANE, "SFAAE": abi.SAMPLER_SPANE,
-            "SPA": abi.SAMPLER_SPA, "SFA": abi.SAMPLER_SPA}
-_MOLECULAR = {"MOADK", "MOSPANE", "MOSFAAE", "MOSPA", "MOSFA", "WFAT"}
+# init_sampler's method names and aliases (ElectronSamplers.jl:11-24)
+_METHODS = {"ADK": abi.SAMPLER_ADK, "MOADK": abi.SAMPLER_ADK,
+            "SPANE": abi.SAMPLER_SPANE, "SFAAE": abi.SAMPLER_SPANE, "MOSPANE": abi.SAMPLER_SPANE,
+            "MOSFAAE": abi.SAMPLER_SPANE,
+            "SPA": abi.SAMPLER_SPA, "SFA": abi.SAMPLER_SPA, "MOSPA": abi.SAMPLER_SPA, "MOSFA": abi.SAMPLER_SPA,
+            "WFAT": abi.SAMPLER_WFAT}
 _PHASES = {"CTMC": abi.PHASE_CTMC, "QTMC": abi.PHASE_QTMC, "SCTS": abi.PHASE_SCTS}
 _PREFIX_BITS = {"Pre": abi.PREFIX_PRE, "PreCC": abi.PREFIX_PRECC, "Jac": abi.PREFIX_JAC}
 _PRECISIONS = {"fp64": abi.PRECISION_FP64, "fp32_bulk": abi.PRECISION_FP32_BULK}
@@ -61,18 +64,19 @@ def make_job(*, init_cond_method, laser, target, dimension, sample_t_intv, sampl
     """Checks the keywords as TrajectorySimulationJob (TrajectorySimulation.jl:164-298) and
     the sampler constructors do, and packs them into an etraj_job."""
     method = _sym(init_cond_method)
-    if method in _MOLECULAR:
-        raise NotImplementedError("[ElectronSamplers] molecular method `%s` is not part of this "
-                                  "engine (molecular targets are not built)." % method)
     if method not in _METHODS:
         raise ValueError("[ElectronSamplers] Undefined initial condition method [%s]." % method)
     if not isinstance(laser, Laser):
         raise TypeError("`laser` must be a Laser.")
-    if not isinstance(target, SAEAtomBase):
-        raise NotImplementedError("only atomic targets (HydrogenLikeAtom, SAEAtom) are supported.")
+    if not isinstance(target, (SAEAtomBase, MoleculeBase)):
+        raise TypeError("`target` must be an atom (HydrogenLikeAtom, SAEAtom) or a molecule (GenericMolecule).")
+    if method == "WFAT" and not isinstance(target, MoleculeBase):
+        raise TypeError("[WFATSampler] The WFAT sampler supports molecular targets only.")
     phase = _sym(traj_phase_method)
     if phase not in _PHASES:
         raise ValueError("[ADKSampler] Undefined phase method [%s]." % phase)
+    if method == "WFAT" and phase != "CTMC":
+        raise ValueError("[WFATSampler] Unsupported phase method [%s]." % phase)
     assert sample_t_intv[0] < sample_t_intv[1], \
         "[TrajectorySimulationJob] `sample_t_intv` must be a valid interval."
     assert traj_t_final > sample_t_intv[1], \
@@ -103,7 +107,11 @@ def make_job(*, init_cond_method, laser, target, dimension, sample_t_intv, sampl
     j.sample_cutoff_limit = float(sample_cutoff_limit)
     j.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
     j.laser = laser.to_c()
-    j.target = target.to_c()
+    if isinstance(target, MoleculeBase):
+        j.target, keep = target.to_c(orbit_ridx=mol_orbit_ridx, wfat=(method == "WFAT"))
+        j._keep = keep  # the arrays behind the target's pointers
+    else:
+        j.target = target.to_c()
     return j
 
 

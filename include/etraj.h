@@ -73,29 +73,50 @@ typedef struct etraj_laser {
     double delay;               /* BICHROMATIC: delay of mono[1] (BichromaticLaser.jl:73-85) */
 } etraj_laser;
 
-/* ---- targets: src/Targets/{HydrogenLikeAtom,SAEAtom}.jl --------------------- */
+/* ---- targets: src/Targets/{HydrogenLikeAtom,SAEAtom,GenericMolecule}.jl ---------- */
 typedef enum etraj_target_kind {
     ETRAJ_TARGET_HYDROGEN_LIKE = 0, /* HydrogenLikeAtom.jl:7 */
-    ETRAJ_TARGET_SAE = 1            /* SAEAtom.jl:7 */
+    ETRAJ_TARGET_SAE = 1,           /* SAEAtom.jl:7 */
+    ETRAJ_TARGET_MOLECULE = 2       /* GenericMolecule.jl:7 */
 } etraj_target_kind;
+
+/* Largest l of a molecule's asymptotic coefficients and WFAT integrals, and
+ * the largest WFAT channel indices n_xi and |m| (the database files hold 6). */
+#define ETRAJ_MOL_MAX_L 6
 
 typedef struct etraj_target {
     int32_t kind;
-    int32_t Z;              /* asymptotic nuclear charge (nucl_charge) */
-    int32_t l, m;
-    double Ip;              /* a.u. */
-    double asymp_coeff;     /* C_kl, already resolved (the :hartree default is SAEAtomBase_shared.jl:3-11) */
+    int32_t Z;              /* asymptotic nuclear charge (nucl_charge; molecule: charge + 1) */
+    int32_t l, m;           /* atoms only */
+    double Ip;              /* a.u.; molecule: IonPotential(mol, orbit_ridx), the ionizing orbital's */
+    double asymp_coeff;     /* atoms: C_kl, already resolved (the :hartree default is SAEAtomBase_shared.jl:3-11) */
     double quan_ax_theta;   /* rad */
     double quan_ax_phi;     /* rad */
-    double a1, b1, a2, b2, a3, b3; /* SAE potential parameters; ignored for hydrogen-like targets */
-    double soft_core;
+    double a1, b1, a2, b2, a3, b3; /* SAE potential parameters; ignored for other targets */
+    double soft_core;       /* atoms; a molecule's trajectories use 1.0 (GenericMolecule.jl:444-445) */
+    /* ETRAJ_TARGET_MOLECULE: the ionizing orbital's data as GenericMolecule
+     * holds it (GenericMolecule.jl:7-41), read from the molecule's data file by
+     * the caller.  The arrays are caller-owned and read only during the call
+     * that takes the job (etraj_run, etraj_submit, ...). */
+    double mol_rot[3];          /* MolRotation: Euler angles alpha, beta, gamma (z-y'-z''), rad */
+    double mol_Ip_traj;         /* IonPotential(mol), the Ip of the trajectories' phase (:438-443) */
+    int32_t asymp_lmax;         /* MolAsympCoeff: C_lm for l = 0..asymp_lmax (<= ETRAJ_MOL_MAX_L) */
+    int32_t wfat_nxi_max;       /* MolWFATMaxChannels: n_xi = 0..wfat_nxi_max */
+    int32_t wfat_m_max;         /* m = -wfat_m_max..wfat_m_max */
+    int32_t wfat_lmax;          /* the integrals' l = 0..wfat_lmax */
+    const double* asymp_coeff_lm;  /* (asymp_lmax+1) x (2 asymp_lmax+1) complex (re, im pairs),
+                                      column-major: C[l+1, m+l+1] as in MolAsympCoeff; NULL: none */
+    const double* wfat_intdata;    /* (nxi+1) x (2 m_max+1) x (lmax+1) x (2 lmax+1) complex, column-major,
+                                      as MolWFATData's IntData; NULL: none */
+    double wfat_mu[3];             /* MolWFATData's orbital dipole mu */
 } etraj_target;
 
 /* ---- job: the keyword arguments of perform_traj_simulation ---------------- */
 typedef enum etraj_sampler_kind {
     ETRAJ_SAMPLER_ADK = 0,   /* :ADK   ADKSampler.jl */
     ETRAJ_SAMPLER_SPANE = 1, /* :SPANE SPANESampler.jl */
-    ETRAJ_SAMPLER_SPA = 2    /* :SPA   SPASampler.jl */
+    ETRAJ_SAMPLER_SPA = 2,   /* :SPA   SPASampler.jl */
+    ETRAJ_SAMPLER_WFAT = 3   /* :WFAT  WFATSampler.jl (molecular targets, CTMC) */
 } etraj_sampler_kind;
 
 /* rate_prefix bit mask (ADKSampler.jl:49-77): :Exp = 0, :Full = PRECC|JAC */

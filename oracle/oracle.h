@@ -61,6 +61,8 @@ void oracle_laser_eval_complex(const etraj_laser* laser, int64_t n, const double
                                double* Fy);
 void oracle_target_eval(const etraj_target* target, int64_t n, const double* xyz, double* V,
                         double* F);
+/* G_{nxi m}(theta, chi) of a molecular target's WFAT data; out = (re, im). */
+void oracle_mol_wfat_G(const etraj_target* T, int nxi, int m, double theta, double chi, double* out);
 double oracle_hartree_asymp_coeff(int Z, double Ip, int l);
 /* exp(-b r) skip of the SAE terms: the per-target exactness check and a
  * process-wide switch (default on) used to show the skip changes nothing */

@@ -10,6 +10,7 @@
 #include "oracle.h"
 #include "../etraj.jl_gb300/csrc/detmath.h"
 #include "../etraj.jl_gb300/csrc/sae_skip.h"
+#include "../etraj.jl_gb300/csrc/mol_check.h"
 
 typedef struct {
     int kind;

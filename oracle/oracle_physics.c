@@ -314,6 +314,16 @@ int oracle_sae_skip_exact(const etraj_target* in) {
 
 void o_target_prepare(const etraj_target* in, o_target* T) {
     memset(T, 0, sizeof *T);
+    if (in->kind == ETRAJ_TARGET_MOLECULE) {
+        /* GenericMolecule's trajectories: -Z (r^2+1)^(-1/2) with Z = charge + 1
+         * and the phase's Ip = IonPotential(mol) (GenericMolecule.jl:438-445) --
+         * the hydrogen-like equations with soft core 1.0 */
+        T->kind = ETRAJ_TARGET_HYDROGEN_LIKE;
+        T->Z = (double)in->Z;
+        T->Ip = in->mol_Ip_traj;
+        T->sc = 1.0;
+        return;
+    }
     T->kind = in->kind;
     T->Z = (double)in->Z;
     T->Ip = in->Ip;

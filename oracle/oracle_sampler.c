@@ -8,6 +8,8 @@
  *   src/ElectronSamplers/SPASampler.jl:19-431 (with the shared spa.h)
  *   src/ElectronSamplers/shared_methods.jl:4-47 (random points, solid
  *     harmonics, FF->MF Euler angles, field-frame axes)
+ *   src/ElectronSamplers/WFATSampler.jl:129-249 and the molecular branches of
+ *     the ADK, SPANE and SPA prefactors (the shared mol.h)
  *
  * Monte-Carlo draws: the reference uses Julia's unseeded global RNG
  * (shared_methods.jl:4-12, ADKSampler.jl:141).  Here every draw comes from a
@@ -165,6 +167,27 @@ int o_sampler_init(const etraj_job* job, o_sampler* S) {
     S->cc_base = dm_pow_pos(2.0, (3.0 * n) / 2.0 + 1.0) * dm_pow_pos(S->kappa, 5.0 * n + 0.5);
     S->e_pre = (n + 1.0) / 4.0;
     for (int mp = -S->l; mp <= S->l; ++mp) S->Plm[mp + S->l] = o_sph_prefactor(S->l, mp, S->kappa);
+    if (T->kind == ETRAJ_TARGET_MOLECULE) {
+        S->mol = 1;
+        S->wfat = (S->method == ETRAJ_SAMPLER_WFAT);
+        for (int i = 0; i < 3; ++i) S->mol_rot[i] = T->mol_rot[i];
+        if (S->wfat) {
+            S->nxi = T->wfat_nxi_max;
+            S->mmax = T->wfat_m_max;
+            S->wl = T->wfat_lmax;
+            S->wint = T->wfat_intdata;
+            for (int i = 0; i < 3; ++i) S->mu[i] = T->wfat_mu[i];
+        } else {
+            S->clm = T->asymp_coeff_lm;
+            mol_terms_build(T->asymp_lmax, S->clm, &S->T);
+            for (int l = 0; l <= T->asymp_lmax; ++l)
+                for (int mp = -l; mp <= l; ++mp) {
+                    const dm_cplx P = mol_sph_prefactor(l, mp, S->kappa);
+                    S->Pmol[2 * (l * l + l + mp)] = P.re;
+                    S->Pmol[2 * (l * l + l + mp) + 1] = P.im;
+                }
+        }
+    }
 
     S->n_t = job->sample_t_num;
     S->t = (double*)malloc(sizeof(double) * (size_t)S->n_t);
@@ -251,6 +274,23 @@ void o_batch_prepare(const o_sampler* S, int64_t b, o_batch* B) {
     dm_sincos(t1, &st1, &ct1);
     double t2 = dm_atan2(M[0][2] * ct1 + M[1][2] * st1, M[2][2]);
     double t3 = dm_atan2(M[1][0] * ct1 - M[0][0] * st1, M[1][1] * ct1 - M[0][1] * st1);
+    if (S->mol) {
+        /* molecular frame RotZYZ(MolRotation) instead of the quantization axis */
+        double a, b_, g;
+        mol_euler(S->mol_rot, B->Fx, B->Fy, B->F, &a, &b_, &g);
+        if (S->wfat) {
+            const int nch = (S->nxi + 1) * (2 * S->mmax + 1), na = (S->nxi + 1) * (S->mmax + 1);
+            for (int c = 0; c < nch; ++c) B->g2[c] = mol_wfat_g2(c, S->nxi, S->mmax, S->wl, S->wint, S->mu, S->kappa, b_, g);
+            for (int e = 0; e < na; ++e) B->A[e] = mol_wfat_A(e, S->nxi, S->kappa, S->n, B->F);
+        } else {
+            for (int e = 0; e < S->T.ncd; ++e) {
+                const dm_cplx v = mol_cd_entry(&S->T, S->clm, e, a, b_, g);
+                B->cd[2 * e] = v.re;
+                B->cd[2 * e + 1] = v.im;
+            }
+        }
+        return;
+    }
     /* D^l_{m' m}(a,b,g) = e^{-i m' a} d^l_{m' m}(b) e^{-i m g} for m' = -l..l */
     for (int mp = -S->l; mp <= S->l; ++mp) {
         double s1, c1, s3, c3;
@@ -269,6 +309,7 @@ static dm_cplx o_pre_numerator(const o_sampler* S, const o_batch* B, dm_cplx kx,
     dm_cplx nkx = dm_cadd(dm_cadd(dm_cscale(ckx, 0.0), dm_cscale(cky, 0.0)), dm_cscale(ckz, 1.0));
     dm_cplx nky = dm_cadd(dm_cadd(dm_cscale(ckx, B->ny[0]), dm_cscale(cky, B->ny[1])), dm_cscale(ckz, B->ny[2]));
     dm_cplx nkz = dm_cadd(dm_cadd(dm_cscale(ckx, B->nz[0]), dm_cscale(cky, B->nz[1])), dm_cscale(ckz, B->nz[2]));
+    if (S->mol) return mol_numerator(&S->T, B->cd, S->Pmol, nkx, nky, nkz);
     dm_cplx acc = dm_c(0.0, 0.0);
     for (int mp = -S->l; mp <= S->l; ++mp) {
         dm_cplx Y = dm_cmul(S->Plm[mp + S->l], o_sph_sum(S->l, mp, nkx, nky, nkz));
@@ -415,6 +456,30 @@ int o_candidate_spa(const o_sampler* S, const o_batch* B, double kd0, double kz0
     return 1;
 }
 
+/* One WFAT candidate (WFATSampler.jl:173-198 for the grid, :200-240 for
+ * Monte-Carlo): ADK's exit point and momentum, the WFAT rate, CTMC rows. */
+int o_candidate_wfat(const o_sampler* S, const o_batch* B, double kd0, double kz0, double* row) {
+    if (kd0 * kd0 + kz0 * kz0 < 1e-4 * 1e-4) return 0;
+    const double F = B->F;
+    const double kx0 = kd0 * (-B->sphi);
+    const double ky0 = kd0 * B->cphi;
+    const double r0 = (S->Ip + (kd0 * kd0 + kz0 * kz0) / 2.0) / F;
+    const double x0 = r0 * B->cphi;
+    const double y0 = r0 * B->sphi;
+    const double rate = mol_wfat_rate(S->nxi, S->mmax, B->g2, B->A, S->kappa, F, kd0, kz0, S->dkdt);
+    if (dm_isnan(rate) || rate < S->cutoff) return 0;
+    int k = 0;
+    row[k++] = x0;
+    row[k++] = y0;
+    if (S->dim == 3) row[k++] = 0.0;
+    row[k++] = kx0;
+    row[k++] = ky0;
+    if (S->dim == 3) row[k++] = kz0;
+    row[k++] = B->tr;
+    row[k++] = rate;
+    return 1;
+}
+
 /* (kd0, kz0) of Monte-Carlo candidate i of batch b (shared_methods.jl:4-12,
  * ADKSampler.jl:350-363). */
 void o_mc_point(const o_sampler* S, int64_t b, int64_t i, double* kd0, double* kz0) {
@@ -433,7 +498,7 @@ void o_mc_point(const o_sampler* S, int64_t b, int64_t i, double* kd0, double* k
 }
 
 int64_t o_sample_batch(const o_sampler* S, int64_t b, double* init, int64_t capacity) {
-    o_batch B;
+    static __thread o_batch B;  /* about 8 KB with the molecular tables: off the stack */
     o_batch_prepare(S, b, &B);
     int64_t count = 0;
     double row[9];
@@ -447,7 +512,9 @@ int64_t o_sample_batch(const o_sampler* S, int64_t b, double* init, int64_t capa
         } else {
             o_mc_point(S, b, i, &kd0, &kz0);
         }
-        if (spa ? o_candidate_spa(S, &B, kd0, kz0, row) : o_candidate(S, &B, kd0, kz0, row)) {
+        const int kept = spa ? o_candidate_spa(S, &B, kd0, kz0, row)
+                             : S->wfat ? o_candidate_wfat(S, &B, kd0, kz0, row) : o_candidate(S, &B, kd0, kz0, row);
+        if (kept) {
             if (count < capacity) memcpy(init + count * S->rows, row, sizeof(double) * (size_t)S->rows);
             ++count;
         }
@@ -531,4 +598,13 @@ int oracle_sample_all(const etraj_job* job, double* init, int64_t capacity, int6
     *count = total;
     o_sampler_free(&S);
     return 0;
+}
+
+/* G_{nxi m}(theta, chi) of a molecular target's WFAT data (mol.h), for the
+ * structure-factor pins (GenericMolecule.jl:236-259); out = (re, im). */
+void oracle_mol_wfat_G(const etraj_target* T, int nxi, int m, double theta, double chi, double* out) {
+    const dm_cplx G = mol_wfat_G(nxi, m, T->wfat_nxi_max, T->wfat_m_max, T->wfat_lmax, T->wfat_intdata, T->wfat_mu,
+                                 sqrt(2.0 * T->Ip), theta, chi);
+    out[0] = G.re;
+    out[1] = G.im;
 }

@@ -3,6 +3,7 @@
 #define ETRAJ_ORACLE_SAMPLER_H
 
 #include "oracle_internal.h"
+#include "../etraj.jl_gb300/csrc/mol.h"
 
 typedef struct {
     int method, dim, mc, prefix, phase, rows, mono;
@@ -16,12 +17,23 @@ typedef struct {
     double *t, *kd, *kz;
     double mc_kd_max, mc_kz_max, dkdt;
     double spa_omega; /* the SPA initial guess' angular frequency (SPASampler.jl:160-166) */
+    /* molecular targets (mol.h layouts) */
+    int mol, wfat;
+    mol_terms T;                  /* MO-ADK: (l, m) pairs with C_lm != 0 */
+    double mol_rot[3];
+    const double* clm;            /* C_lm (caller's array) */
+    double Pmol[2 * MOL_NLM];     /* Y_{l m'} prefactors */
+    int nxi, mmax, wl;            /* WFAT channel and integral sizes */
+    const double* wint;           /* WFAT integrals (caller's array) */
+    double mu[3];
 } o_sampler;
 
 typedef struct {
     double tr, Fx, Fy, dFx, dFy, F, phi, sphi, cphi, gamma, c_cc, W;
     double ny[3], nz[3];
     dm_cplx D[9];
+    double cd[2 * MOL_NCD];       /* MO-ADK: C_lm D^l_{m' m} */
+    double g2[MOL_NCH], A[MOL_NA]; /* WFAT: |G|^2 per channel, time-sample factors of W */
 } o_batch;
 
 void o_philox4x32(uint32_t c[4], uint64_t seed);
@@ -32,6 +44,7 @@ void o_sampler_free(o_sampler* S);
 void o_batch_prepare(const o_sampler* S, int64_t b, o_batch* B);
 int o_candidate(const o_sampler* S, const o_batch* B, double kd0, double kz0, double* row);
 int o_candidate_spa(const o_sampler* S, const o_batch* B, double kd0, double kz0, double* row);
+int o_candidate_wfat(const o_sampler* S, const o_batch* B, double kd0, double kz0, double* row);
 void o_mc_point(const o_sampler* S, int64_t b, int64_t i, double* kd0, double* kz0);
 int64_t o_sample_batch(const o_sampler* S, int64_t b, double* init, int64_t capacity);
 

@@ -206,7 +206,7 @@ int oracle_validate(const etraj_job* job, char* msg, int len) {
     if (job->dimension != 2 && job->dimension != 3)
         return o_fail(msg, len, "[TrajectorySimulationJob] `dimension` must be either 2 or 3.");
     if (job->init_cond_method != ETRAJ_SAMPLER_ADK && job->init_cond_method != ETRAJ_SAMPLER_SPANE &&
-        job->init_cond_method != ETRAJ_SAMPLER_SPA)
+        job->init_cond_method != ETRAJ_SAMPLER_SPA && job->init_cond_method != ETRAJ_SAMPLER_WFAT)
         return o_fail(msg, len, "[ElectronSamplers] Undefined initial condition method.");
     if (job->traj_phase_method < 0 || job->traj_phase_method > 2)
         return o_fail(msg, len, "[ADKSampler] Undefined phase method.");
@@ -240,11 +240,21 @@ int oracle_validate(const etraj_job* job, char* msg, int len) {
             return o_fail(msg, len, "[TrajectorySimulationJob] `final_p_max` must be positive.");
     }
     const etraj_target* T = &job->target;
-    if (!(T->Ip > 0)) return o_fail(msg, len, "[SAEAtom] Ip should be positive.");
-    if (!(T->l >= 0 && T->l >= abs(T->m))) return o_fail(msg, len, "[SAEAtom] Invalid (l,m).");
-    if (T->l > 4) return ETRAJ_ERR_UNSUPPORTED;
-    if (!(T->asymp_coeff > 0)) return o_fail(msg, len, "[SAEAtom] asymp_coeff should be either `:hartree` or a positive number.");
-    if (T->kind == ETRAJ_TARGET_SAE) {
+    const char* mmsg = 0;
+    int mst = etraj_mol_check(job, &mmsg);
+    if (mst > 0) {
+        o_fail(msg, len, mmsg);
+        return mst;
+    }
+    if (mst == 0) {
+        /* molecular target: checked above */
+    } else if (!(T->Ip > 0)) return o_fail(msg, len, "[SAEAtom] Ip should be positive.");
+    else if (!(T->l >= 0 && T->l >= abs(T->m))) return o_fail(msg, len, "[SAEAtom] Invalid (l,m).");
+    else if (T->l > 4) return ETRAJ_ERR_UNSUPPORTED;
+    else if (!(T->asymp_coeff > 0)) return o_fail(msg, len, "[SAEAtom] asymp_coeff should be either `:hartree` or a positive number.");
+    if (T->kind == ETRAJ_TARGET_MOLECULE) {
+        /* trajectories: Coulomb tail with soft core 1.0 (GenericMolecule.jl:444-445) */
+    } else if (T->kind == ETRAJ_TARGET_SAE) {
         if (!(T->b1 >= 0 && T->b2 >= 0 && T->b3 >= 0)) return o_fail(msg, len, "[SAEAtom] b1,b2,b3 should be non-negative.");
         if (!(T->soft_core > 0)) return o_fail(msg, len, "[SAEAtom] soft_core should be positive.");
     } else if (T->kind == ETRAJ_TARGET_HYDROGEN_LIKE) {

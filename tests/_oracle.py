@@ -46,6 +46,7 @@ def lib():
             "oracle_laser_eval_complex": (None, [C.POINTER(abi.Laser), C.c_int64, _DP, _DP, _DP, _DP, _DP, _DP]),
             "oracle_target_eval": (None, [C.POINTER(abi.Target), C.c_int64, _DP, _DP, _DP]),
             "oracle_hartree_asymp_coeff": (C.c_double, [C.c_int, C.c_double, C.c_int]),
+            "oracle_mol_wfat_G": (None, [C.POINTER(abi.Target), C.c_int, C.c_int, C.c_double, C.c_double, _DP]),
             "oracle_rhs": (None, [_JP, C.c_double, _DP, _DP]),
             "oracle_sae_skip_exact": (C.c_int, [C.c_void_p]),
             "oracle_set_sae_skip": (None, [C.c_int]),
@@ -214,3 +215,9 @@ def tsit5_tableau():
     bt = np.zeros(7)
     lib().oracle_tsit5_tableau(_p(c), _p(a), _p(bt))
     return c, a.reshape(7, 6), bt
+
+
+def mol_wfat_G(target, nxi, m, theta, chi):
+    out = np.zeros(2)
+    lib().oracle_mol_wfat_G(C.byref(target), nxi, m, theta, chi, _p(out))
+    return complex(out[0], out[1])

@@ -107,7 +107,7 @@ def test_python_mirror_rejects_what_the_reference_rejects():
         et.make_job(**{**kw, "final_p_num": (50, 50, 50)})
     with pytest.raises(ValueError):
         et.make_job(**{**kw, "traj_phase_method": "XYZ"})
-    with pytest.raises(NotImplementedError):
+    with pytest.raises(TypeError):  # WFATSampler takes molecular targets only (WFATSampler.jl:4)
         et.make_job(**{**kw, "init_cond_method": "WFAT"})
     with pytest.raises(AssertionError):
         et.Cos4Laser(peak_int=1e14, cyc_num=2, ellip=0.0)

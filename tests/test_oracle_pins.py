@@ -16,6 +16,7 @@ import pytest
 
 import _oracle as O
 import etraj_gb300 as et
+from _mol import hydrogen
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 with open(os.path.join(GOLDEN, "sampler_survivors.json")) as f:
@@ -23,21 +24,27 @@ with open(os.path.join(GOLDEN, "sampler_survivors.json")) as f:
 with open(os.path.join(GOLDEN, "physics_pins.json")) as f:
     PINS = json.load(f)
 
-BUILT_METHODS = {"ADK", "SPANE", "SPA"}
+BUILT_METHODS = {"ADK", "SPANE", "SPA", "WFAT"}
 
 
 def survivor_job(modifiers):
+    """The sampler of an `init_sampler(; merge(params, ...)...)` test case; the
+    molecule is get_mol("Hydrogen") (rotated by rot_β=π/2, rot_γ=π/2 for mol_rot)."""
     p = dict(SURV["common"])
     for m in modifiers:
         p.update(SURV["modifiers"][m])
-    if "mol" in modifiers or "mol_rot" in modifiers or p["init_cond_method"] == "WFAT":
-        return None
     L = p.pop("laser")
     p.pop("target")
     laser = et.Cos4Laser(peak_int=L["peak_int"], wave_len=L["wave_len"], cyc_num=L["cyc_num"],
                          ellip=L["ellip"])
+    if "mol_rot" in modifiers:
+        target = hydrogen(rot_β=math.pi / 2, rot_γ=math.pi / 2)
+    elif "mol" in modifiers:
+        target = hydrogen()
+    else:
+        target = et.get_atom("H")
     dim = p["dimension"]
-    return et.make_job(laser=laser, target=et.get_atom("H"), traj_t_final=200.0,
+    return et.make_job(laser=laser, target=target, traj_t_final=200.0,
                        final_p_max=(2.0,) * dim, final_p_num=(10,) * dim, **p)
 
 
@@ -48,8 +55,6 @@ def _case_id(c):
 @pytest.mark.parametrize("case", SURV["cases"], ids=[_case_id(c) for c in SURV["cases"]])
 def test_sampler_survivor_counts(case):
     job = survivor_job(case["modifiers"])
-    if job is None:
-        pytest.skip("molecular targets (get_mol, WFAT) are outside the built path")
     if O.validate(job)[0] == 2:
         pytest.skip("sampler not built yet")
     r = O.sample_batch(job, SURV["batch_id"])
