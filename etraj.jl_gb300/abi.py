@@ -136,6 +136,10 @@ SIGNATURES = [
     ("etraj_bulk_tile", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, _I32P, _I32P, _I32P]),
     ("etraj_set_bulk_tile", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                       C.c_int]),
+    ("etraj_set_straggler_repack", C.c_int, [C.c_void_p, C.c_int]),
+    ("etraj_set_keep_final_states", C.c_int, [C.c_void_p, C.c_int]),
+    ("etraj_dump_final_states", C.c_int, [C.c_void_p, C.c_uint64, _DP, _DP, _I32P]),
+    ("etraj_dump_step_counts", C.c_int, [C.c_void_p, C.c_uint64, _I32P]),
     ("etraj_stage_times", C.c_int, [C.c_void_p, _DP, C.c_int]),
     ("etraj_deposit_noalloc", C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                         C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -401,6 +401,7 @@ struct DevBuf {
 // buffers (synchronous etraj_run) or in a pinned staging block that is copied
 // out when the job completes (asynchronous submit and the server).
 struct JobRec {
+    uint64_t ticket = 0;         // 0: etraj_run's job
     int status = ETRAJ_OK;       // enqueue status; an error completes the job at once
     std::string error;
     etraj_result res{};          // the caller's output pointers; scalars filled at completion
@@ -444,6 +445,12 @@ struct etraj_ctx {
     bool stage_valid = false;
     uint64_t next_ticket = 1;
     std::map<uint64_t, JobRec> jobs;       // asynchronous tickets of this context
+    // per-survivor final states of the last job, kept with etraj_set_keep_final_states
+    bool keep_states = false;
+    bool dump_valid = false;
+    uint64_t dump_ticket = 0;
+    TrajOut dump_out{};
+    const unsigned long long* dump_count = nullptr;
     std::vector<PinnedBlock> pinned_pool;  // staging blocks for reuse
     std::vector<cudaEvent_t> event_pool;
     // CUDA-graph replay of the per-job kernel sequence (opt-in): the graph of
@@ -455,6 +462,7 @@ struct etraj_ctx {
     int glaunches = 0;
     // bulk-integrator launch shapes chosen by the autotuner, per kernel variant
     bool autotune = true;
+    bool repack = true;  // the bulk integrator's rounds with parking of long-running electrons
     std::map<int, BulkTile> tiles;
     // sizing without allocating: ensure() only adds up the growth
     bool dry = false;
@@ -585,6 +593,7 @@ int alloc_sampling(etraj_ctx* ctx, HostJob& H, Pipeline& P) {
 
 int alloc_outputs(etraj_ctx* ctx, const DJob& J, int64_t max_n, bool with_state, Pipeline& P) {
     const size_t n = (size_t)(max_n > 0 ? max_n : 1);
+    if (!ctx->dry) ctx->dump_valid = false;  // the buffers now belong to a new job
     ETRAJ_TRY(ensure_t(ctx, "out.key", n, &P.out.key));
     ETRAJ_TRY(ensure_t(ctx, "out.c_re", n, &P.out.c_re));
     ETRAJ_TRY(ensure_t(ctx, "out.c_im", n, &P.out.c_im));
@@ -594,7 +603,13 @@ int alloc_outputs(etraj_ctx* ctx, const DJob& J, int64_t max_n, bool with_state,
     ETRAJ_TRY(ensure_t(ctx, "out.steps", n, &P.out.steps));
     if (with_state) ETRAJ_TRY(ensure_t(ctx, "out.final_state", n * (size_t)J.n_state, &P.out.final_state));
     else P.out.final_state = nullptr;
-    P.out.p_inf = nullptr;
+    if (ctx->keep_states) {
+        ETRAJ_TRY(ensure_t(ctx, "out.p_inf", 3 * n, &P.out.p_inf));
+        ETRAJ_TRY(ensure_t(ctx, "out.fphase", n, &P.out.fphase));
+    } else {
+        P.out.p_inf = nullptr;
+        P.out.fphase = nullptr;
+    }
     void* dep = nullptr;
     ETRAJ_TRY(ensure(ctx, "deposit", deposit_scratch_bytes(max_n), &dep));
     deposit_scratch_carve(dep, max_n, &P.dep);
@@ -603,7 +618,7 @@ int alloc_outputs(etraj_ctx* ctx, const DJob& J, int64_t max_n, bool with_state,
     ETRAJ_TRY(ensure_t(ctx, "mspec", (size_t)J.grid, &P.mspec));
     ETRAJ_TRY(ensure_t(ctx, "sums", 2, &P.sums));
     ETRAJ_TRY(ensure_t(ctx, "counters", 1, &P.counters));
-    ETRAJ_TRY(ensure_t(ctx, "work", 4, &P.work));
+    ETRAJ_TRY(ensure_t(ctx, "work", kBulkCounters, &P.work));
     return ETRAJ_OK;
 }
 
@@ -775,7 +790,6 @@ int tuned_bulk_launch(etraj_ctx* ctx, BulkParams& B, const InitSoA& soa, const d
                 BulkParams Bc = B;
                 Bc.max_iters = kTuneMaxIters;
                 apply_tile(Bc, kTileCandidates[c]);
-                cudaMemsetAsync(work, 0, sizeof(unsigned long long), s);
                 cudaEventRecord(evs[(size_t)(4 * c + 2 * rep)], s);
                 *launches += launch_integrate_bulk(Bc, soa, t, idx, sub, work, out, ctx->sm_count, s);
                 cudaEventRecord(evs[(size_t)(4 * c + 2 * rep + 1)], s);
@@ -802,10 +816,25 @@ int tuned_bulk_launch(etraj_ctx* ctx, BulkParams& B, const InitSoA& soa, const d
     }
     if (tune_lk.owns_lock()) tune_lk.unlock();
     apply_tile(B, chosen);
-    cudaMemsetAsync(work, 0, sizeof(unsigned long long), s);
     if (ev) rec(ctx, ev[0], s);
     *launches += launch_integrate_bulk(B, soa, t, idx, count, work, out, ctx->sm_count, s);
     if (ev) rec(ctx, ev[1], s);
+    return ETRAJ_OK;
+}
+
+// The park buffer of the bulk integrator's rounds: two halves of max_n/16 +
+// 4096 entries (at most 2^20) of kParkWords words.  An electron that finds
+// the buffer full finishes in its current round, so the size only bounds how
+// much the later rounds can repack.
+int attach_park(etraj_ctx* ctx, BulkParams& B) {
+    B.park_buf = nullptr;
+    B.park_cap = 0;
+    if (!ctx->repack) return ETRAJ_OK;
+    const int cap = (int)std::min<int64_t>(B.max_n / 16 + 4096, (int64_t)1 << 20);
+    uint32_t* buf = nullptr;
+    ETRAJ_TRY(ensure_t(ctx, "park", (size_t)2 * (size_t)cap * kParkWords, &buf));
+    B.park_buf = buf;
+    B.park_cap = cap;
     return ETRAJ_OK;
 }
 
@@ -826,6 +855,7 @@ int launch_integrate(etraj_ctx* ctx, const DJob& J, const InitSoA& soa, const do
     float4* tab = nullptr;
     ETRAJ_TRY(ensure_t(ctx, "field_table", (size_t)B.n_int * 2, &tab));
     B.table = tab;
+    ETRAJ_TRY(attach_park(ctx, B));
     *launches += launch_field_table(J, B.T0, (double)1.0 / B.inv_h_d, B.n_int, tab, s);
     ETRAJ_TRY(tuned_bulk_launch(ctx, B, soa, t, idx, count, work, out, launches, ev));
     *launches += launch_collect_bulk(J, soa, t, idx, count, out, max_n, ctx->sm_count, s);
@@ -900,6 +930,8 @@ size_t plan_growth(etraj_ctx* ctx, const etraj_job* job) {
         prepare_bulk(H.J, H.t.front(), B);
         float4* tab = nullptr;
         ensure_t(ctx, "field_table", (size_t)B.n_int * 2, &tab);
+        B.max_n = H.J.n_total;
+        attach_park(ctx, B);
     }
     ctx->dry = false;
     return ctx->dry_bytes;
@@ -948,8 +980,9 @@ int enqueue_kernels_maybe_graph(etraj_ctx* ctx, const etraj_job* job, const Host
         n_int = (size_t)B.n_int;
         tile_k = tile_key(B);
         if (ctx->autotune && !find_tile(ctx, tile_k, nullptr) && B.max_n >= ((int64_t)1 << 18)) use_graph = false;
-        float4* tab = nullptr;  // allocate the field table outside the capture
+        float4* tab = nullptr;  // allocate the field table and the park buffer outside the capture
         ETRAJ_TRY(ensure_t(ctx, "field_table", n_int * 2, &tab));
+        ETRAJ_TRY(attach_park(ctx, B));
     }
     if (!use_graph) return enqueue_kernels(ctx, job, H, P, launches);
     void* tab_ptr = ctx->bufs.count("field_table") ? ctx->bufs["field_table"].p : nullptr;
@@ -961,7 +994,8 @@ int enqueue_kernels_maybe_graph(etraj_ctx* ctx, const etraj_job* job, const Host
     k += sizeof P;
     BulkTile t = kTileDefault;
     find_tile(ctx, tile_k, &t);
-    const int extra[3] = {job->precision, t.threads * 1000 + t.blocks_per_sm * 10 + t.occ, t.refill_min};
+    const int extra[3] = {job->precision, t.threads * 1000 + t.blocks_per_sm * 10 + t.occ,
+                          t.refill_min * 2 + (ctx->repack ? 1 : 0)};
     std::memcpy(k, extra, sizeof extra);
     k += sizeof extra;
     std::memcpy(k, &n_int, sizeof n_int);
@@ -1062,6 +1096,10 @@ int enqueue_job(etraj_ctx* ctx, const etraj_job* job, JobRec& r) {
     r.launches = launches;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_err(ctx, e, "kernel launch");
+    ctx->dump_valid = ctx->keep_states;
+    ctx->dump_ticket = r.ticket;
+    ctx->dump_out = P.out;
+    ctx->dump_count = P.count;
     return ETRAJ_OK;
 }
 
@@ -1245,6 +1283,7 @@ int run_batch(etraj_ctx* ctx, const etraj_job* jobs, int n, etraj_result* res, c
     M.max_n = N;
     M.inst = d_inst;
     M.n_inst = n;
+    ETRAJ_TRY(attach_park(ctx, M));
     ETRAJ_TRY(tuned_bulk_launch(ctx, M, P.soa, P.t, P.idx, P.count, P.work, P.out, &launches, ctx->stage_ev + 3));
     launches += launch_collect_bulk(H[0].J, P.soa, P.t, P.idx, P.count, P.out, N, ctx->sm_count, s, d_inst, n);
     cudaEventRecord(ctx->stage_ev[5], s);
@@ -1555,6 +1594,7 @@ int etraj_submit(etraj_ctx* ctx, const etraj_job* job, etraj_result* out, uint64
     cudaSetDevice(ctx->device);
     const uint64_t tk = ctx->next_ticket++;
     JobRec& r = ctx->jobs[tk];
+    r.ticket = tk;
     r.res = *out;
     r.staged = true;
     r.status = enqueue_job(ctx, job, r);
@@ -1910,6 +1950,64 @@ int etraj_set_bulk_tile(etraj_ctx* ctx, int dimension, int phase, int target, in
     std::lock_guard<std::mutex> lk(ctx->mu);
     const int key = (multi ? 1000 : 0) + dimension * 100 + phase * 10 + target;
     ctx->tiles[key] = BulkTile{threads, blocks_per_sm, refill_min, warps > 16 ? 3 : 2};
+    return ETRAJ_OK;
+}
+
+int etraj_set_straggler_repack(etraj_ctx* ctx, int enable) {
+    if (!ctx) return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->repack = (enable != 0);
+    return ETRAJ_OK;
+}
+
+int etraj_set_keep_final_states(etraj_ctx* ctx, int enable) {
+    if (!ctx) return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    ctx->keep_states = (enable != 0);
+    return ETRAJ_OK;
+}
+
+namespace {
+// Number of survivors of the kept job, after it has finished (ticket 0: the last job).
+int dump_prepare(etraj_ctx* ctx, uint64_t ticket, int64_t* n) {
+    if (!ctx->dump_valid || (ticket != 0 && ticket != ctx->dump_ticket))
+        return set_err(ctx, ETRAJ_ERR_NOT_FOUND,
+                       "final states are kept only for the context's last job, and only when "
+                       "etraj_set_keep_final_states was on when it was enqueued");
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    unsigned long long c = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&c, ctx->dump_count, sizeof c, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "final states");
+    *n = (int64_t)c;
+    return ETRAJ_OK;
+}
+}  // namespace
+
+int etraj_dump_final_states(etraj_ctx* ctx, uint64_t ticket, double* p_inf, double* phase, int32_t* status) {
+    if (!ctx) return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    int64_t n = 0;
+    ETRAJ_TRY(dump_prepare(ctx, ticket, &n));
+    if (n == 0) return ETRAJ_OK;
+    const TrajOut& o = ctx->dump_out;
+    cudaError_t e = cudaSuccess;
+    if (p_inf && e == cudaSuccess) e = cudaMemcpy(p_inf, o.p_inf, (size_t)n * 3 * 8, cudaMemcpyDeviceToHost);
+    if (phase && e == cudaSuccess) e = cudaMemcpy(phase, o.fphase, (size_t)n * 8, cudaMemcpyDeviceToHost);
+    if (status && e == cudaSuccess) e = cudaMemcpy(status, o.status, (size_t)n * 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "final states");
+    return ETRAJ_OK;
+}
+
+int etraj_dump_step_counts(etraj_ctx* ctx, uint64_t ticket, int32_t* steps) {
+    if (!ctx || !steps) return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    int64_t n = 0;
+    ETRAJ_TRY(dump_prepare(ctx, ticket, &n));
+    if (n == 0) return ETRAJ_OK;
+    cudaError_t e = cudaMemcpy(steps, ctx->dump_out.steps, (size_t)n * 4, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "step counts");
     return ETRAJ_OK;
 }
 

@@ -111,6 +111,7 @@ struct TrajOut {
     int32_t* steps;      // step attempts
     double* final_state; // optional: n_state doubles per survivor (row-major)
     double* p_inf;       // optional: 3 doubles per survivor
+    double* fphase;      // optional: final phase per survivor (0 for CTMC)
 };
 
 struct Counters {
@@ -176,7 +177,24 @@ struct BulkParams {
     float Z, Ip, sc, a1, b1, a2, b2, a3, b3, a2b2;
     float r_far;        // SAE: radius beyond which the exp(-b r) terms are dropped
     int max_iters;      // steps before an electron is given up (status 1)
+    // Rounds: the integrator runs as kBulkRounds launches.  In round r an
+    // electron that has taken kParkBudget[r] steps in the round writes its
+    // whole state to the park buffer and frees its lane; round r+1 resumes the
+    // parked electrons packed densely (blocks without parked work exit at
+    // once).  park_buf == nullptr: one launch, no parking.
+    uint32_t* park_buf;   // 2 halves x park_cap entries x kParkWords words (word-major)
+    int park_cap;         // entries per half
+    // set per round by the launcher
+    int park_budget;      // steps per electron in this round (0: no limit)
+    const uint32_t* park_in;                    // rounds >= 1: resume from here
+    const unsigned long long* park_in_count;
+    uint32_t* park_out;                         // all rounds but the last: park into here
+    unsigned long long* park_out_count;
 };
+constexpr int kParkWords = 33;   // words of one parked electron (3D with phase)
+constexpr int kBulkRounds = 4;
+constexpr int kParkBudget[kBulkRounds] = {1024, 16384, 262144, 0};
+constexpr int kBulkCounters = 2 * kBulkRounds;  // work counter and park count per round
 constexpr int kBulkMaxIters = 1000000;  // OrdinaryDiffEq's default maxiters
 int launch_field_table(const DJob& J, double T0, double h, int n_int, float4* tab, cudaStream_t s);
 // *out = min(*count, cap) (the autotuner's sample of the electrons)

@@ -41,6 +41,8 @@
 //
 // Roofline: FP32 issue bound, MUFU for rsqrt/exp2/log2; no tensor cores.
 
+#include <climits>
+
 #include "physics.cuh"
 
 namespace etraj {
@@ -226,6 +228,11 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
     constexpr int N = 2 * DIM + (HASPH ? 1 : 0);
     extern __shared__ float4 s_tab[];
     __shared__ BulkInst s_inst[MULTI ? kMaxInstances : 1];
+    // a resume round launches a full grid; blocks past the parked electrons exit
+    // at once, so a job's later rounds hold only the SMs their electrons need
+    if (P.park_in && (unsigned long long)blockIdx.x * blockDim.x >=
+                         min(*P.park_in_count, (unsigned long long)P.park_cap))
+        return;
     const float4* tab = P.table;
     if (MULTI) {
         for (int i = threadIdx.x; i < P.n_inst; i += blockDim.x) s_inst[i] = P.inst[i];
@@ -239,13 +246,14 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
-    const unsigned long long n_traj = *count;
+    const bool resume = (P.park_in != nullptr);
+    const unsigned long long n_traj = resume ? min(*P.park_in_count, (unsigned long long)P.park_cap) : *count;
 
     // state (hi, lo): x[DIM], p[DIM], phase
     float xh[DIM], xl[DIM], ph[DIM], pl[DIM], fh = 0.0f, flo = 0.0f;
     float K1[DIM], kph1 = 0.0f;  // FSAL derivatives
     float mK1 = 0.0f, mph1 = 0.0f;  // and their term magnitudes
-    int tn = 0, iter = 0, attempts = 0;
+    int tn = 0, iter = 0, attempts = 0, rs = 0;  // rs: step attempts in this round
     float tfr = 0.0f, dth = 0.0f, dthp = 0.0f, dthmax = 0.0f, lqold = LOG2_QOLDINIT, q11 = 1.0f;
     bool accept = false, active = false, need = true;
     unsigned long long s = 0;
@@ -262,7 +270,42 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
             if (need) {
                 need = false;
                 s = base + __popc(needm & lt_mask);
-                if (s < n_traj) {
+                rs = 0;
+                if (s < n_traj && resume) {
+                    // a parked electron: its whole state, in the order the parking wrote it
+                    const uint32_t* b = P.park_in + s;
+                    const size_t cs = (size_t)P.park_cap;
+                    int k = 0;
+                    auto gf = [&]() { return __uint_as_float(b[cs * (size_t)(k++)]); };
+                    auto gi = [&]() { return (int)b[cs * (size_t)(k++)]; };
+                    const unsigned long long lo = (unsigned)gi(), hi = (unsigned)gi();
+                    s = lo | (hi << 32);
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d) {
+                        xh[d] = gf();
+                        xl[d] = gf();
+                        ph[d] = gf();
+                        pl[d] = gf();
+                        K1[d] = gf();
+                    }
+                    fh = gf();
+                    flo = gf();
+                    kph1 = gf();
+                    mK1 = gf();
+                    mph1 = gf();
+                    tn = gi();
+                    iter = gi();
+                    attempts = gi();
+                    tfr = gf();
+                    dth = gf();
+                    dthp = gf();
+                    dthmax = gf();
+                    lqold = gf();
+                    q11 = gf();
+                    accept = gi() != 0;
+                    my = gi();
+                    active = true;
+                } else if (s < n_traj) {
                     // load the electron and pick the first step (Hairer's starting step)
                     const int64_t g = idx ? idx[s] : (int64_t)s;
                     double u0x[DIM], u0p[DIM];
@@ -368,6 +411,56 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
             }
         }
         if (__ballot_sync(FULL, active) == 0u) break;
+        if (P.park_out) {
+            // park the electrons that used up this round's step budget
+            const bool want = active && rs >= P.park_budget;
+            const unsigned pm = __ballot_sync(FULL, want);
+            if (pm) {
+                const int leader = __ffs(pm) - 1;
+                unsigned long long base = 0ull;
+                if (lane == leader) base = atomicAdd(P.park_out_count, (unsigned long long)__popc(pm));
+                base = __shfl_sync(FULL, base, leader);
+                const unsigned long long e = base + __popc(pm & lt_mask);
+                if (want && e < (unsigned long long)P.park_cap) {
+                    uint32_t* b = P.park_out + e;
+                    const size_t cs = (size_t)P.park_cap;
+                    int k = 0;
+                    auto pf = [&](float v) { b[cs * (size_t)(k++)] = __float_as_uint(v); };
+                    auto pi = [&](int v) { b[cs * (size_t)(k++)] = (uint32_t)v; };
+                    pi((int)(uint32_t)s);
+                    pi((int)(uint32_t)(s >> 32));
+#pragma unroll
+                    for (int d = 0; d < DIM; ++d) {
+                        pf(xh[d]);
+                        pf(xl[d]);
+                        pf(ph[d]);
+                        pf(pl[d]);
+                        pf(K1[d]);
+                    }
+                    pf(fh);
+                    pf(flo);
+                    pf(kph1);
+                    pf(mK1);
+                    pf(mph1);
+                    pi(tn);
+                    pi(iter);
+                    pi(attempts);
+                    pf(tfr);
+                    pf(dth);
+                    pf(dthp);
+                    pf(dthmax);
+                    pf(lqold);
+                    pf(q11);
+                    pi(accept ? 1 : 0);
+                    pi(my);
+                    active = false;
+                    need = true;  // the lane takes the next queued electron
+                } else if (want) {
+                    rs = INT_MIN;  // park buffer full: finish the electron in this round
+                }
+                if (__ballot_sync(FULL, active) == 0u) continue;
+            }
+        }
         if (active) {
             // ---- one Tsit5 step attempt (lanes without work idle; every lane returns to
             //      the ballots above, so the *_sync calls always see the full warp) -----------
@@ -465,6 +558,7 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
                 const float ms = acc * (1.0f / N);
                 const float lh = 0.5f * __log2f(ms);  // log2 EEst
                 ++attempts;
+                ++rs;
                 float q;
                 if (ms == 0.0f) {
                     q = QMAX_INV;
@@ -566,6 +660,7 @@ k_collect_bulk(const __grid_constant__ DJob J, InitSoA soa, const double* __rest
         uint32_t key = sentinel;
         double cre = 0.0, cim = 0.0, wion = 0.0, wunc = 0.0;
         float pin[3] = {0.0f, 0.0f, 0.0f};
+        double phase_out = 0.0;
         bool ionized = false;
         if (st == 0) {
             const double* f = out.final_state + s * N;
@@ -604,6 +699,7 @@ k_collect_bulk(const __grid_constant__ DJob J, InitSoA soa, const double* __rest
                 const int toff = (n_inst > 0) ? s_toff[my] : 0;
                 phase = (phase + J.target.Ip * tsamp[toff + soa.batch[g]]) - (double)corr;
             }
+            phase_out = phase;
             if (E >= 0.0f) {
                 ionized = true;
                 wion = prob;
@@ -662,6 +758,7 @@ k_collect_bulk(const __grid_constant__ DJob J, InitSoA soa, const double* __rest
             out.p_inf[3 * s + 1] = pin[1];
             out.p_inf[3 * s + 2] = pin[2];
         }
+        if (out.fphase) out.fphase[s] = phase_out;
         out.status[s] = st | (ionized ? 0x100 : 0);
     }
 }
@@ -698,8 +795,20 @@ int launch_bulk_t(const BulkParams& P, InitSoA soa, const double* t, const int64
     const int64_t want = (P.max_n + lanes_per_block - 1) / lanes_per_block;
     const int64_t cap = (int64_t)sm_count * P.blocks_per_sm;
     const int blocks = (int)(want < 1 ? 1 : (want < cap ? want : cap));
-    kern<<<blocks, P.threads, smem, s>>>(P, soa, t, idx, count, queue, out);
-    return 1;
+    // queue[2r]: the work counter of round r; queue[2r+1]: electrons parked in round r
+    const int rounds = P.park_buf ? kBulkRounds : 1;
+    cudaMemsetAsync(queue, 0, sizeof(unsigned long long) * 2 * rounds, s);
+    for (int r = 0; r < rounds; ++r) {
+        BulkParams Q = P;
+        const size_t half = (size_t)P.park_cap * kParkWords;
+        Q.park_budget = kParkBudget[r];
+        Q.park_in = (r > 0) ? P.park_buf + (size_t)((r - 1) & 1) * half : nullptr;
+        Q.park_in_count = (r > 0) ? queue + 2 * (r - 1) + 1 : nullptr;
+        Q.park_out = (P.park_buf && r + 1 < rounds) ? P.park_buf + (size_t)(r & 1) * half : nullptr;
+        Q.park_out_count = queue + 2 * r + 1;
+        kern<<<(r == 0) ? blocks : (int)cap, P.threads, smem, s>>>(Q, soa, t, idx, count, queue + 2 * r, out);
+    }
+    return rounds;
 }
 
 }  // namespace

@@ -238,6 +238,7 @@ __device__ __forceinline__ bool collect(const DJob& J, int status, const double*
     uint32_t key = (uint32_t)J.grid;
     double cre = 0.0, cim = 0.0, wion = 0.0, wunc = 0.0;
     double pin[3] = {0.0, 0.0, 0.0};
+    double phase_out = 0.0;
     bool ionized = false;
     if (status == 0) {
         double x, y, z, px, py, pz, K;
@@ -262,6 +263,7 @@ __device__ __forceinline__ bool collect(const DJob& J, int status, const double*
             double rp = (DIM == 2) ? (x * px + y * py) : ((x * py + y * py) + z * pz);
             phase = phase - (Z * sqrtb) * (dm_log(g) + dm_asinh(rp / (g * sqrtb)));
         }
+        phase_out = phase;
         if (E >= 0.0) {
             ionized = true;
             wion = prob;
@@ -314,6 +316,7 @@ __device__ __forceinline__ bool collect(const DJob& J, int status, const double*
         out.p_inf[3 * s + 1] = pin[1];
         out.p_inf[3 * s + 2] = pin[2];
     }
+    if (out.fphase) out.fphase[s] = phase_out;
     return ionized;
 }
 

@@ -212,6 +212,29 @@ class Engine:
             self._check(st)
         return t.value, b.value, r.value, st == abi.OK
 
+    def set_straggler_repack(self, enable):
+        """Bulk path: run the integrator in rounds that repack long-running electrons."""
+        self._check(self.lib.etraj_set_straggler_repack(self.ctx, 1 if enable else 0))
+
+    def keep_final_states(self, enable=True):
+        """Keep per-survivor final states of the following jobs (dump_final_states)."""
+        self._check(self.lib.etraj_set_keep_final_states(self.ctx, 1 if enable else 0))
+
+    def dump_final_states(self, n, ticket=0):
+        """(p_inf (n, 3), phase (n,), status (n,)) of the last job's n survivors;
+        status = retcode | 0x100 when ionized."""
+        p = np.zeros((n, 3))
+        ph = np.zeros(n)
+        st = np.zeros(n, dtype=np.int32)
+        self._check(self.lib.etraj_dump_final_states(self.ctx, ticket, abi.dptr(p), abi.dptr(ph),
+                                                     st.ctypes.data_as(C.POINTER(C.c_int32))))
+        return p, ph, st
+
+    def dump_step_counts(self, n, ticket=0):
+        steps = np.zeros(n, dtype=np.int32)
+        self._check(self.lib.etraj_dump_step_counts(self.ctx, ticket, steps.ctypes.data_as(C.POINTER(C.c_int32))))
+        return steps
+
     def set_bulk_tile(self, dimension, phase, target, threads, blocks_per_sm, refill_min, multi=False):
         """Pin a bulk-integrator variant's launch shape on this engine."""
         self._check(self.lib.etraj_set_bulk_tile(self.ctx, dimension, phase, target, 1 if multi else 0,

@@ -305,6 +305,37 @@ int etraj_bulk_tile(etraj_ctx* ctx, int dimension, int phase, int target, int mu
 int etraj_set_bulk_tile(etraj_ctx* ctx, int dimension, int phase, int target, int multi, int threads,
                         int blocks_per_sm, int refill_min);
 
+/* ---- rounds of the bulk integrator ------------------------------------------------------
+ * No counterpart in the reference.  A few electrons of a job can need up to
+ * maxiters (10^6) steps while the rest finish in ~100.  Left in place, each
+ * keeps its whole thread block -- and that block's share of an SM -- resident
+ * for seconds, so concurrent jobs (the serving loop) cannot get onto the GPU.
+ * With repacking on (the default) the bulk integrator runs in rounds: an
+ * electron that has taken 1024 steps in round 0 (then 16384, 262144 in the
+ * next rounds) writes its integrator state to a device buffer and frees its
+ * lane, and the next round resumes the parked electrons in as few blocks as
+ * they fill.  Each electron's arithmetic does not depend on where it runs, so
+ * results are the same bits either way. */
+int etraj_set_straggler_repack(etraj_ctx* ctx, int enable);
+
+
+/* ---- per-trajectory final states ---------------------------------------------------
+ * For parity checks against the reference's per-trajectory results: with
+ * etraj_set_keep_final_states(ctx, 1) on when a job is enqueued (etraj_run or
+ * etraj_submit), the context keeps, per surviving electron in the order of the
+ * reference's concatenated `init` columns, the asymptotic momentum p_inf
+ * (p_inf_vec of TrajectorySimulation.jl:383-384 / :478-479; zeros when not
+ * ionized), the final phase (after the SCTS correction of :362-369 / :457-464;
+ * 0 for CTMC) and the status: the ODE retcode (0 Success, 1 MaxIters,
+ * 2 DtLessThanMin, 3 Unstable, 4 DtNaN) with bit 0x100 set when E_inf >= 0.
+ * etraj_dump_final_states copies them (n = num_effective_traj rows; any pointer
+ * may be NULL) for `ticket` (0: the last job) once the job has finished; the
+ * data is kept until the context's next job.  ETRAJ_ERR_NOT_FOUND otherwise.
+ * etraj_dump_step_counts gives each survivor's Tsit5 step attempts. */
+int etraj_set_keep_final_states(etraj_ctx* ctx, int enable);
+int etraj_dump_final_states(etraj_ctx* ctx, uint64_t ticket, double* p_inf, double* phase, int32_t* status);
+int etraj_dump_step_counts(etraj_ctx* ctx, uint64_t ticket, int32_t* steps);
+
 /* ---- diagnostics ----------------------------------------------------------------
  * Device time (ms) of the stages of the last etraj_run on this context: sampling,
  * compaction, field table, integrator, collection, deposit.  Writes up to n

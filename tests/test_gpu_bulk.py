@@ -170,3 +170,35 @@ def test_set_bulk_tile_rejects_bad_shapes():
         with pytest.raises(et.EtrajError):
             eng.set_bulk_tile(2, abi.PHASE_SCTS, abi.TARGET_SAE, th, bps, rf)
     eng.close()
+
+
+
+def test_rounds_with_parking_keep_every_bit():
+    """The integrator's rounds park electrons past a step budget and resume them
+    in other lanes, warps and launches; results stay the same bits (a long pulse
+    at a long wavelength gives electrons past every budget)."""
+    T = 2 * np.pi * 1600.0 / 45.563352525
+    L = et.Cos2Laser(peak_int=1e14, wave_len=1600.0, cyc_num=6, ellip=0.3)
+    job = et.make_job(init_cond_method="ADK", laser=L, target=et.get_atom("Ar"), dimension=2,
+                      sample_t_intv=(-1.5 * T, 1.5 * T), sample_t_num=400, traj_t_final=5 * T,
+                      final_p_max=(2.0, 2.0), final_p_num=(120, 120), sample_monte_carlo=True, mc_kt_num=500,
+                      mc_kd_max=1.0, traj_phase_method="SCTS", seed=7, precision="fp32_bulk")
+    on = et.Engine(device=0)
+    off = et.Engine(device=0)
+    off.set_straggler_repack(False)
+    for e in (on, off):
+        e.keep_final_states(True)
+    r1, s1, a1 = on.run(job, want_amplitude=True)
+    r2, s2, a2 = off.run(job, want_amplitude=True)
+    n = r1.num_effective_traj
+    assert n == r2.num_effective_traj > 0
+    assert r1.num_steps == r2.num_steps and r1.ion_prob == r2.ion_prob and r1.num_failed_traj == r2.num_failed_traj
+    assert np.array_equal(s1, s2) and np.array_equal(a1, a2)
+    p1, f1, t1 = on.dump_final_states(n)
+    p2, f2, t2 = off.dump_final_states(n)
+    assert np.array_equal(p1, p2) and np.array_equal(f1, f2) and np.array_equal(t1, t2)
+    st = on.dump_step_counts(n)
+    assert np.array_equal(st, off.dump_step_counts(n))
+    assert (st > 1024).sum() > 0 and (st > 16384).sum() > 0  # electrons went through later rounds
+    on.close()
+    off.close()

@@ -265,3 +265,80 @@ def test_gpu_config1_full_size(eng):
     assert rel_l2(spec, rspec) <= 1e-10
     assert same_bits(spec, rspec)
     assert res.ion_prob == rsc["ion_prob"]
+
+
+# ---- per-trajectory final states (etraj_dump_final_states) -------------------------------
+
+@pytest.mark.parametrize("phase", ["QTMC", "SCTS"])
+def test_gpu_dump_final_states_match_oracle(eng, phase):
+    """Per survivor, in the reference's column order: p_inf, status and step
+    counts bit for bit; the QTMC phase is the ODE's last component, the SCTS
+    phase reproduces the oracle's deposited amplitude sqrt(w) e^{i phase}."""
+    job = job_of(method="ADK", dim=3, phase=phase, target="Ar", nt=16, nkd=9, nkz=5, laser="cos2", ellip=0.5)
+    eng.keep_final_states(True)
+    try:
+        res, _, _ = eng.run(job)
+        n = res.num_effective_traj
+        p, ph, st = eng.dump_final_states(n)
+        steps = eng.dump_step_counts(n)
+    finally:
+        eng.keep_final_states(False)
+    init = O.sample_all(job)
+    fin, rst, rsteps = O.integrate(job, init)
+    _, _, sc, rp, _ = O.collect(job, init, fin, rst, rsteps)
+    assert n == init.shape[0] > 0
+    assert np.array_equal(st & 0xFF, rst) and np.array_equal(steps, rsteps)
+    assert int(np.count_nonzero(st & 0x100)) == res.num_ionized_traj == int(sc["num_ionized"])
+    ion = (st & 0x100) != 0
+    assert same_bits(p[ion], rp[ion])
+    ok = rst == 0
+    if phase == "QTMC":
+        assert same_bits(ph[ok], fin[ok, -1])
+    else:
+        key, cre, cim = O.contributions(job, init, fin, rst)
+        dep = key < job.grid_size
+        w = np.sqrt(init[dep, 7])
+        np.testing.assert_allclose(w * np.cos(ph[dep]), cre[dep], rtol=1e-12, atol=1e-14 * w.max())
+        np.testing.assert_allclose(w * np.sin(ph[dep]), cim[dep], rtol=1e-12, atol=1e-14 * w.max())
+
+
+def test_gpu_dump_final_states_bookkeeping(eng):
+    job = job_of(method="ADK", dim=2, nt=8, nkd=11)
+    eng.run(job)  # not kept
+    with pytest.raises(et.EtrajError) as e:
+        eng.dump_final_states(1)
+    assert e.value.status == abi.ERR_NOT_FOUND
+    eng.keep_final_states(True)
+    try:
+        r1 = abi.Result()
+        t1 = eng.submit(job, r1)
+        eng.wait(t1, r1)
+        p1, _, s1 = eng.dump_final_states(r1.num_effective_traj, ticket=t1)
+        p0, _, s0 = eng.dump_final_states(r1.num_effective_traj)  # ticket 0: the last job
+        assert same_bits(p1, p0) and np.array_equal(s1, s0)
+        eng.run(job_of(method="ADK", dim=2, nt=8, nkd=11, seed=4))
+        with pytest.raises(et.EtrajError):  # overwritten by the next job
+            eng.dump_final_states(r1.num_effective_traj, ticket=t1)
+    finally:
+        eng.keep_final_states(False)
+
+
+def test_gpu_dump_final_states_bulk_path(eng):
+    """The bulk path's per-survivor asymptotic momenta track FP64's."""
+    job = job_of(method="SPANE", dim=2, phase="SCTS", target="Ar", laser="cos2", ellip=1.0, mc=True, nt=200,
+                 nkd=100, nkz=1)
+    eng.keep_final_states(True)
+    try:
+        r64, _, _ = eng.run(job)
+        p64, _, s64 = eng.dump_final_states(r64.num_effective_traj)
+        b = job.copy()
+        b.precision = abi.PRECISION_FP32_BULK
+        r32, _, _ = eng.run(b)
+        p32, _, s32 = eng.dump_final_states(r32.num_effective_traj)
+    finally:
+        eng.keep_final_states(False)
+    assert r32.num_effective_traj == r64.num_effective_traj
+    both = ((s64 & 0x100) != 0) & ((s32 & 0x100) != 0)
+    assert both.sum() > 0.95 * ((s64 & 0x100) != 0).sum()
+    d = np.linalg.norm(p32[both] - p64[both], axis=1) / np.linalg.norm(p64[both], axis=1)
+    assert np.median(d) < 1e-3
