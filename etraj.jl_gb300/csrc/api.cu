@@ -622,6 +622,17 @@ int alloc_outputs(etraj_ctx* ctx, const DJob& J, int64_t max_n, bool with_state,
     return ETRAJ_OK;
 }
 
+// The candidate kernel of a job: the bulk path samples in FP32 (ADK and SPANE
+// while every kept rate stays in FP32's normal range, and SPA), molecular
+// targets and the FP64 path in FP64.
+int launch_sampler(int precision, const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
+                   const DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count, cudaStream_t s) {
+    const bool fp32 = precision == ETRAJ_PRECISION_FP32_BULK && !J.mol.on &&
+                      (J.method == ETRAJ_SAMPLER_SPA || J.cutoff >= kSample32MinCutoff);
+    return fp32 ? launch_sample32_range(J, b0, nb, kd, kz, batches, soa, flag, sm_count, s)
+                : launch_sample_range(J, b0, nb, kd, kz, batches, soa, flag, sm_count, s);
+}
+
 // Copies a job's host inputs (time and momentum samples, molecular tables) to the device.
 void upload_inputs(const HostJob& H, const Pipeline& P, cudaStream_t s) {
     cudaMemcpyAsync(P.t, H.t.data(), H.t.size() * sizeof(double), cudaMemcpyHostToDevice, s);
@@ -944,11 +955,7 @@ int enqueue_kernels(etraj_ctx* ctx, const etraj_job* job, const HostJob& H, cons
     int launches = 0;
     rec(ctx, ctx->stage_ev[0], s);
     launches += launch_batch_prepare(J, P.t, P.batches, s);
-    if (job->precision == ETRAJ_PRECISION_FP32_BULK && J.method != ETRAJ_SAMPLER_SPA && !J.mol.on &&
-        J.cutoff >= kSample32MinCutoff)
-        launches += launch_sample32_range(J, 0, J.n_t, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s);
-    else
-        launches += launch_sample_range(J, 0, J.n_t, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s);
+    launches += launch_sampler(job->precision, J, 0, J.n_t, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s);
     rec(ctx, ctx->stage_ev[1], s);
     launches += launch_compact(P.flag, J.n_total, P.idx, P.block_sums, compact_blocks(J.n_total) + 1, P.count, s);
     rec(ctx, ctx->stage_ev[2], s);
@@ -1263,12 +1270,8 @@ int run_batch(etraj_ctx* ctx, const etraj_job* jobs, int n, etraj_result* res, c
         const int64_t c = coff[i];
         so.x += c; so.y += c; so.kx += c; so.ky += c; so.kz += c; so.rate += c; so.batch += c;
         if (so.phase) so.phase += c;
-        if (J.method != ETRAJ_SAMPLER_SPA && J.cutoff >= kSample32MinCutoff)
-            launches += launch_sample32_range(J, 0, J.n_t, P.kd + koff[i], P.kz + zoff[i], bat, so, P.flag + c,
-                                              ctx->sm_count, s);
-        else
-            launches += launch_sample_range(J, 0, J.n_t, P.kd + koff[i], P.kz + zoff[i], bat, so, P.flag + c,
-                                            ctx->sm_count, s);
+        launches += launch_sampler(ETRAJ_PRECISION_FP32_BULK, J, 0, J.n_t, P.kd + koff[i], P.kz + zoff[i], bat, so,
+                                   P.flag + c, ctx->sm_count, s);
     }
     cudaEventRecord(ctx->stage_ev[1], s);
     launches += launch_compact(P.flag, N, P.idx, P.block_sums, compact_blocks(N) + 1, P.count, s);
@@ -1382,7 +1385,7 @@ int sample_range(etraj_ctx* ctx, const etraj_job* job, int64_t b0, int64_t nb, d
     cudaStream_t s = ctx->stream;
     upload_inputs(H, P, s);
     launch_batch_prepare(H.J, P.t, P.batches, s);
-    launch_sample_range(H.J, b0, nb, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s);
+    launch_sampler(job->precision, H.J, b0, nb, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_err(ctx, e, "sample launch");
     return gather_rows(ctx, H, P, b0 * H.J.n_cand, nb * H.J.n_cand, init, capacity, count);

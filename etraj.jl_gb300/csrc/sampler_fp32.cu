@@ -13,7 +13,7 @@
 // distance of the cutoff may be kept by one path and dropped by the other.  Output layout is the
 // FP64 kernel's (candidate-indexed SoA of doubles and a keep flag).
 
-#include "engine.h"
+#include "physics.cuh"
 
 namespace etraj {
 namespace {
@@ -72,6 +72,483 @@ __device__ cf sph_sum(int l, int m, cf x, cf y, cf z) {
         acc = cadd(acc, tt);
     }
     return acc;
+}
+
+// ---- FP32 SPA candidate (SPASampler.jl:150-431) -------------------------------------
+// Every complex time the SPA candidate evaluates, except the four solves of its
+// finite-difference Jacobian, has Re t = t_r: the saddle-point iterates
+// t_r + i t_i and the quadrature paths from t_r to t_r + i t_i.  The laser's
+// phases at t_r (up to ~1e3 rad) are therefore reduced once in FP64, and
+// A(t_r + i tau), F(t_r + i tau) follow in FP32 from cosh/sinh of the
+// imaginary parts.  The solve and the quadratures are the algorithms of spa.h
+// (NLsolve's trust-region dogleg with a central-difference derivative;
+// QuadGK's adaptive Gauss-Kronrod (7,15) with an interval heap) at FP32's
+// tolerances: ftol 1e-5 on the saddle-point residual, derivative step
+// cbrt(eps(Float32)), quadrature rtol sqrt(eps(Float32)), which is the
+// tolerance QuadGK picks for Float32 integrands.
+enum { Q_IM_AX = 0, Q_IM_AY = 1, Q_ACTION = 2, Q_IM_AXY = 3 };
+constexpr int kSegs32 = 48;  // interval budget of one quadrature
+
+struct SpaMono32 {
+    float cth, sth, cu, su;   // cos, sin of the carrier and envelope phases at t_r
+    float om, w2n, cN;        // carrier and envelope angular frequencies, envelope factor
+    float preA, preF;         // A0 (F0) times the tanh windows (Cos) or the Gaussian at t_r
+    float gt, gi, inv_s2;     // Gaussian: t_r - t_shift, 1/(2 sigma^2), 1/sigma^2
+    float ellip, cphi, sphi;
+    int kind, azi0;
+};
+struct SpaBase32 {
+    int n;
+    SpaMono32 m[2];
+};
+
+__device__ void spa32_base(const DLaser& L, double tr, SpaBase32& S) {
+    S.n = L.nmono;
+    for (int k = 0; k < L.nmono; ++k) {
+        const DMono& M = L.m[k];
+        SpaMono32& m = S.m[k];
+        const double tt = ((k == 0) ? tr : tr - L.delay) - M.t_shift;
+        double th = M.omega * tt + M.cep;
+        th = th - 6.283185307179586 * rint(th * 0.15915494309189535);
+        double sn, cs;
+        sincos(th, &sn, &cs);
+        m.cth = (float)cs;
+        m.sth = (float)sn;
+        m.om = (float)M.omega;
+        m.kind = M.kind;
+        m.azi0 = M.azi_zero;
+        m.ellip = (float)M.ellip;
+        m.cphi = (float)M.cphi;
+        m.sphi = (float)M.sphi;
+        if (M.kind == ETRAJ_LASER_GAUSSIAN) {
+            m.gt = (float)tt;
+            m.gi = (float)M.inv_2s2;
+            m.inv_s2 = (float)M.inv_s2;
+            const double g0 = exp(-(tt * tt) * M.inv_2s2) * M.A0;
+            m.preA = (float)g0;
+            m.preF = (float)g0;
+            m.cu = m.su = m.w2n = m.cN = 0.0f;
+        } else {
+            double su, cu;
+            sincos(M.w2n * tt, &su, &cu);
+            m.cu = (float)cu;
+            m.su = (float)su;
+            m.w2n = (float)M.w2n;
+            m.cN = (float)M.cN;
+            double w1, w2;
+            window(M, tt, w1, w2);
+            m.preA = (float)((M.A0 * w1) * w2);
+            m.preF = (float)((M.F0 * w1) * w2);
+            m.gt = m.gi = m.inv_s2 = 0.0f;
+        }
+    }
+}
+
+// A (and F when fx != nullptr) at t_r + i tau
+__device__ void spa32_AF(const SpaBase32& S, float tau, cf& ax, cf& ay, cf* fx, cf* fy) {
+    ax = ay = cmk(0.0f, 0.0f);
+    if (fx) *fx = *fy = cmk(0.0f, 0.0f);
+    for (int k = 0; k < S.n; ++k) {
+        const SpaMono32& m = S.m[k];
+        const float ch = coshf(m.om * tau), sh = sinhf(m.om * tau);
+        const cf sth = cmk(m.sth * ch, m.cth * sh), cth = cmk(m.cth * ch, -(m.sth * sh));
+        cf preA, preF, cx, cy;
+        if (m.kind == ETRAJ_LASER_GAUSSIAN) {
+            float sa, ca;
+            sincosf(-2.0f * m.gt * tau * m.gi, &sa, &ca);
+            const float e = expf(tau * tau * m.gi);
+            preA = cmk(m.preA * e * ca, m.preA * e * sa);
+            preF = preA;
+            const cf a = cmk(m.gt * m.inv_s2, tau * m.inv_s2);
+            cx = cadd(cmul(a, cth), cscale(sth, m.om));
+            cy = cadd(cmul(a, sth), cscale(cth, -m.om));
+        } else {
+            const float chu = coshf(m.w2n * tau), shu = sinhf(m.w2n * tau);
+            const cf c = cmk(m.cu * chu, -(m.su * shu)), sv = cmk(m.su * chu, m.cu * shu);
+            const cf c2 = cmul(c, c);
+            const bool c4 = (m.kind == ETRAJ_LASER_COS4);
+            preA = cscale(c4 ? cmul(c2, c2) : c2, m.preA);
+            preF = cscale(c4 ? cmul(c2, c) : c, m.preF);
+            const cf b = cscale(sv, m.cN);
+            cx = cadd(cmul(c, sth), cmul(b, cth));
+            cy = cadd(cmul(cmk(-c.re, -c.im), cth), cmul(b, sth));
+        }
+        if (m.azi0) {
+            ax = cadd(ax, cmul(preA, cth));
+            ay = cadd(ay, cscale(cmul(preA, sth), m.ellip));
+            if (fx) {
+                *fx = cadd(*fx, cmul(preF, cx));
+                *fy = cadd(*fy, cscale(cmul(preF, cy), m.ellip));
+            }
+        } else {
+            const cf se = cscale(sth, m.ellip);
+            ax = cadd(ax, cmul(preA, cadd(cscale(cth, m.cphi), cscale(se, m.sphi))));
+            ay = cadd(ay, cmul(preA, cadd(cscale(cth, -m.sphi), cscale(se, m.cphi))));
+            if (fx) {
+                const cf cye = cscale(cy, m.ellip);
+                *fx = cadd(*fx, cmul(preF, cadd(cscale(cx, m.cphi), cscale(cye, m.sphi))));
+                *fy = cadd(*fy, cmul(preF, cadd(cscale(cx, -m.sphi), cscale(cye, m.cphi))));
+            }
+        }
+    }
+}
+
+// px_, py_ of SPASampler.jl:230-231
+__device__ __forceinline__ void spa32_pxy(float kd, cf Ax, cf Ay, float& px, float& py) {
+    const float den = sqrtf(fmaf(Ax.im, Ax.im, Ay.im * Ay.im));
+    px = (kd * Ay.im) / den - Ax.re;
+    py = (-kd * Ax.im) / den - Ay.re;
+}
+
+// saddle_point_equation (SPASampler.jl:233-239) at t_r + i x
+__device__ float spa32_spe(const SpaBase32& S, float x, float kd, float kz, float Ip) {
+    cf Ax, Ay;
+    spa32_AF(S, x, Ax, Ay, nullptr, nullptr);
+    float px, py;
+    spa32_pxy(kd, Ax, Ay, px, py);
+    const float ur = px + Ax.re, ui = Ax.im, vr = py + Ay.re, vi = Ay.im;
+    const float u2 = fmaf(ur, ur, -ui * ui), v2 = fmaf(vr, vr, -vi * vi);
+    return fmaf(0.5f, fmaf(kz, kz, u2 + v2), Ip);
+}
+
+__device__ float spa32_dspe(const SpaBase32& S, float x, float kd, float kz, float Ip) {
+    const float e = 4.9215667e-3f * fmaxf(fabsf(x), 1.0f);  // cbrt(eps(Float32))
+    return (spa32_spe(S, x + e, kd, kz, Ip) - spa32_spe(S, x - e, kd, kz, Ip)) / (2.0f * e);
+}
+
+// t_i of the saddle point (0: not converged or t_i <= 0); spa_solve_ti in FP32
+__device__ __noinline__ float spa32_solve(const SpaBase32& S, float kd, float kz, float Ip, float x0) {
+    const float ftol = 1e-5f, eta = 1e-4f;
+    float x = x0;
+    float r = spa32_spe(S, x, kd, kz, Ip);
+    float J = spa32_dspe(S, x, kd, kz, Ip);
+    if (!isfinite(r) || !isfinite(x)) return 0.0f;
+    bool converged = (fabsf(r) <= ftol);
+    float d = fabsf(J);
+    if (d == 0.0f) d = 1.0f;
+    float delta = fabsf(d * x);
+    if (delta == 0.0f) delta = 1.0f;
+    for (int it = 0; it < 200 && !converged; ++it) {
+        if (J == 0.0f) return 0.0f;
+        float p;
+        const float pn = -(r / J);
+        if (fabsf(d * pn) <= delta) {
+            p = pn;
+        } else {
+            const float g = (J * r) / (d * d);
+            const float wg = fabsf(d * g), Jg = J * g;
+            const float pc = ((-(wg * wg)) / (Jg * Jg)) * g;
+            if (fabsf(d * pc) >= delta) {
+                p = g * (-delta / wg);
+            } else {
+                const float df = pn - pc;
+                const float b = 2.0f * ((d * pc) * (d * df));
+                const float a = (d * df) * (d * df);
+                const float wc = fabsf(d * pc);
+                const float tau = (-b + sqrtf(b * b - (4.0f * a) * (wc * wc - delta * delta))) / (2.0f * a);
+                p = pc + tau * df;
+            }
+        }
+        const float xold = x;
+        x = x + p;
+        const float fn = spa32_spe(S, x, kd, kz, Ip);
+        const float rp = J * p + r;
+        const float rho = (r * r - fn * fn) / (r * r - rp * rp);
+        if (rho > eta) {
+            r = fn;
+            J = spa32_dspe(S, x, kd, kz, Ip);
+            d = fmaxf(0.1f * d, fabsf(J));
+            converged = (fabsf(x - xold) <= 0.0f) || (fabsf(r) <= ftol);
+        } else {
+            x = x - p;
+        }
+        if (rho < 0.1f) delta = 0.5f * delta;
+        else if (rho >= 0.9f) delta = 2.0f * fabsf(d * p);
+        else if (rho >= 0.5f) delta = fmaxf(delta, 2.0f * fabsf(d * p));
+        if (isnan(x) || isnan(fn)) break;
+    }
+    return (converged && x > 0.0f) ? x : 0.0f;
+}
+
+// integrands over tau at t = t_r + i tau: Im A_x, Im A_y (kind 3: both), or the
+// action's ((p_x+A_x)^2 + (p_y+A_y)^2 + k_z^2)/2 + I_p (kind 2)
+struct SpaQ32 {
+    const SpaBase32* S;
+    float px, py, kz, Ip;
+};
+__device__ __forceinline__ cf spa32_f(int kind, const SpaQ32& Q, float tau, float& v1) {
+    cf Ax, Ay;
+    spa32_AF(*Q.S, tau, Ax, Ay, nullptr, nullptr);
+    if (kind != Q_ACTION) {
+        v1 = Ay.im;
+        return cmk(kind == Q_IM_AY ? Ay.im : Ax.im, 0.0f);
+    }
+    v1 = 0.0f;
+    const cf u = cmk(Q.px + Ax.re, Ax.im), v = cmk(Q.py + Ay.re, Ay.im);
+    const cf sq = cadd(cmul(u, u), cmul(v, v));
+    return cmk(fmaf(0.5f, sq.re + Q.kz * Q.kz, Q.Ip), 0.5f * sq.im);
+}
+
+struct Seg32 {
+    float a, b, E;
+    cf I;
+};
+
+__device__ __forceinline__ float cabsf(cf z) { return (z.im == 0.0f) ? fabsf(z.re) : hypotf(z.re, z.im); }
+
+// Gauss-Kronrod (7, 15) on [a, b]; g1: the second integrand of kind 3
+__device__ __noinline__ Seg32 spa32_rule(int kind, const SpaQ32& Q, float a, float b, Seg32* g1) {
+    const float x[8] = {-0.991455371120812639f, -0.949107912342758525f, -0.864864423359769073f,
+                        -0.741531185599394440f, -0.586087235467691130f, -0.405845151377397167f,
+                        -0.207784955007898468f, 0.0f};
+    const float w[8] = {0.022935322010529225f, 0.063092092629978553f, 0.104790010322250184f,
+                        0.140653259715525919f, 0.169004726639267903f, 0.190350578064785410f,
+                        0.204432940075298892f, 0.209482141084727828f};
+    const float gw[4] = {0.129484966168869693f, 0.279705391489276668f, 0.381830050505118945f,
+                         0.417959183673469388f};
+    const float h = 0.5f * (b - a), c = 0.5f * (a + b);
+    cf Ig = cmk(0.0f, 0.0f), Ik = Ig;
+    float Jg = 0.0f, Jk = 0.0f;
+    for (int i = 0; i < 8; ++i) {
+        float u1 = 0.0f, u2 = 0.0f;
+        cf f;
+        float fh;
+        if (i < 7) {
+            const cf p = spa32_f(kind, Q, fmaf(h, x[i], c), u1);
+            const cf q = spa32_f(kind, Q, fmaf(-h, x[i], c), u2);
+            f = cadd(p, q);
+            fh = u1 + u2;
+        } else {
+            f = spa32_f(kind, Q, c, u1);
+            fh = u1;
+        }
+        Ik = cadd(Ik, cscale(f, w[i]));
+        Jk = fmaf(fh, w[i], Jk);
+        if (i & 1) {  // the Gauss nodes are the odd Kronrod nodes, the centre (i = 7) included
+            Ig = cadd(Ig, cscale(f, gw[i >> 1]));
+            Jg = fmaf(fh, gw[i >> 1], Jg);
+        }
+    }
+    Seg32 sg;
+    sg.a = a;
+    sg.b = b;
+    sg.I = cscale(Ik, h);
+    sg.E = cabsf(cadd(sg.I, cscale(Ig, -h)));
+    if (g1) {
+        g1->a = a;
+        g1->b = b;
+        g1->I = cmk(Jk * h, 0.0f);
+        g1->E = fabsf(Jk * h - Jg * h);
+    }
+    return sg;
+}
+
+__device__ __noinline__ cf spa32_quad_from(int kind, const SpaQ32& Q, Seg32 first, bool& ok) {
+    const float rtol = 3.4526698e-4f;  // sqrt(eps(Float32))
+    Seg32 hp[kSegs32];
+    hp[0] = first;
+    cf I = first.I;
+    float E = first.E;
+    ok = isfinite(E);
+    if (!ok || E <= rtol * cabsf(I)) return I;
+    int n = 1;
+    while (rtol * cabsf(I) < E) {
+        if (n + 1 > kSegs32) {
+            ok = false;
+            break;
+        }
+        const Seg32 sg = hp[0];
+        hp[0] = hp[n - 1];
+        --n;
+        {  // sift down
+            int i = 0;
+            const Seg32 xx = hp[0];
+            for (;;) {
+                const int l = 2 * i + 1;
+                if (l >= n) break;
+                const int rr = l + 1;
+                const int j = (rr >= n || hp[rr].E < hp[l].E) ? l : rr;
+                if (!(xx.E < hp[j].E)) break;
+                hp[i] = hp[j];
+                i = j;
+            }
+            if (n > 0) hp[i] = xx;
+        }
+        const float mid = 0.5f * (sg.a + sg.b);
+        const Seg32 s1 = spa32_rule(kind, Q, sg.a, mid, nullptr);
+        const Seg32 s2 = spa32_rule(kind, Q, mid, sg.b, nullptr);
+        if (!isfinite(s1.E) || !isfinite(s2.E)) {
+            ok = false;
+            return I;
+        }
+        I = cadd(cadd(cadd(I, cscale(sg.I, -1.0f)), s1.I), s2.I);
+        E = ((E - sg.E) + s1.E) + s2.E;
+        for (int t = 0; t < 2; ++t) {  // sift up
+            int i = n;
+            const Seg32 xx = t ? s2 : s1;
+            while (i > 0) {
+                const int pp = (i - 1) / 2;
+                if (!(hp[pp].E < xx.E)) break;
+                hp[i] = hp[pp];
+                i = pp;
+            }
+            hp[i] = xx;
+            ++n;
+        }
+    }
+    I = hp[0].I;
+    for (int i = 1; i < n; ++i) I = cadd(I, hp[i].I);
+    return I;
+}
+
+// jac(kd, kz) of SPASampler.jl:280-292 from four saddle-point solves
+__device__ __noinline__ float spa32_jac(const DLaser& L, double tr, const SpaBase32& S0, float kd, float kz, float Ip,
+                                        float wF, float w) {
+    const float dtr = 0.01f, dkd = 0.01f;
+    SpaBase32 Sp, Sm;
+    spa32_base(L, tr + 0.01, Sp);
+    spa32_base(L, tr - 0.01, Sm);
+    auto guess = [&](float k) { return asinhf(wF * sqrtf(fmaf(k, k, kz * kz) + 2.0f * Ip)) / w; };
+    const float ti_tp = spa32_solve(Sp, kd, kz, Ip, guess(kd));
+    const float ti_tm = spa32_solve(Sm, kd, kz, Ip, guess(kd));
+    const float ti_kp = spa32_solve(S0, kd + dkd, kz, Ip, guess(kd + dkd));
+    const float ti_km = spa32_solve(S0, kd - dkd, kz, Ip, guess(kd - dkd));
+    cf ax, ay;
+    float pxa, pya, pxb, pyb;
+    spa32_AF(Sp, ti_tp, ax, ay, nullptr, nullptr);
+    spa32_pxy(kd, ax, ay, pxa, pya);
+    spa32_AF(Sm, ti_tm, ax, ay, nullptr, nullptr);
+    spa32_pxy(kd, ax, ay, pxb, pyb);
+    const float dpxdtr = pxa - pxb, dpydtr = pya - pyb;
+    spa32_AF(S0, ti_kp, ax, ay, nullptr, nullptr);
+    spa32_pxy(kd + dkd, ax, ay, pxa, pya);
+    spa32_AF(S0, ti_km, ax, ay, nullptr, nullptr);
+    spa32_pxy(kd - dkd, ax, ay, pxb, pyb);
+    const float dpxdkd = pxa - pxb, dpydkd = pya - pyb;
+    return fabsf(dpxdtr * dpydkd - dpxdkd * dpydtr) / ((4.0f * dtr) * dkd);
+}
+
+// sum over m' of C D^l_{m' m} Y_{l m'} of conj(k) in the field frame (ADKSampler.jl:243-265)
+__device__ cf num32(const DJob& J, const FBatch& B, cf kx, cf ky, float kz0) {
+    const cf nkx = cmk(kz0, 0.0f);
+    const cf nky = cadd(cscale(cconj(kx), B.ny0), cscale(cconj(ky), B.ny1));
+    const cf nkz = cadd(cscale(cconj(kx), B.nz0), cscale(cconj(ky), B.nz1));
+    cf num = cmk(0.0f, 0.0f);
+    for (int mp = -J.l; mp <= J.l; ++mp) {
+        const int ii = mp + J.l;
+        const cf Y = cmul(cmk(J.fPlm[2 * ii], J.fPlm[2 * ii + 1]), sph_sum(J.l, mp, nkx, nky, nkz));
+        num = cadd(num, cmul(cmk(B.CD[2 * ii], B.CD[2 * ii + 1]), Y));
+    }
+    return num;
+}
+
+__global__ void __launch_bounds__(128)
+k_sample_spa32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double* __restrict__ kdv,
+               const double* __restrict__ kzv, const DBatch* __restrict__ batches, InitSoA soa,
+               uint8_t* __restrict__ flag) {
+    const int64_t total = nb * J.n_cand;
+    const float Ip = (float)J.Ip, kd_max = (float)J.mc_kd_max, kz_max = (float)J.mc_kz_max;
+    const float w = (float)J.spa_omega, e_half = (float)((J.nstar + 1.0) / 2.0);
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t bl = q / J.n_cand, i = q - bl * J.n_cand, b = b0 + bl;
+        const DBatch& DB = batches[b];
+        const FBatch& B = DB.f;
+        float kd0, kz0;
+        if (!J.mc) {
+            kd0 = (float)kdv[i / J.n_kz];
+            kz0 = (float)kzv[i % J.n_kz];
+        } else {
+            uint32_t c[4] = {(uint32_t)i, (uint32_t)((uint64_t)i >> 32), (uint32_t)b, 0x4B445A00u};
+            philox4x32(c, J.seed);
+            const float ua = (float)(c[0] >> 8) * 5.9604644775390625e-8f;
+            const float ub = (float)(c[2] >> 8) * 5.9604644775390625e-8f;
+            kd0 = ((ua - 0.5f) * 2.0f) * kd_max;
+            if (J.dim == 3) {
+                kz0 = ((ub - 0.5f) * 2.0f) * kz_max;
+                if (J.mc_kd_max == 0.0) kd0 = 0.0f;
+                else if (J.mc_kz_max == 0.0) kz0 = 0.0f;
+            } else {
+                kz0 = 0.0f;
+            }
+        }
+        uint8_t keep = 0;
+        double x0 = 0.0, y0 = 0.0, kx0 = 0.0, ky0 = 0.0, rate = 0.0, ph = 0.0;
+        // the batch is skipped when F(t_r) <= 1e-3 (SPASampler.jl:167-169)
+        if (!(fabsf(kd0) < 1e-4f) && DB.F > 1e-3) {
+            SpaBase32 S;
+            spa32_base(J.laser, DB.tr, S);
+            const float wF = w / B.F;
+            const float guess = asinhf(wF * sqrtf(fmaf(kd0, kd0, kz0 * kz0) + 2.0f * Ip)) / w;
+            const float ti = spa32_solve(S, kd0, kz0, Ip, guess);
+            if (ti != 0.0f) {
+                cf Ax, Ay, Fx, Fy;
+                spa32_AF(S, ti, Ax, Ay, &Fx, &Fy);
+                float px, py;
+                spa32_pxy(kd0, Ax, Ay, px, py);
+                SpaQ32 Q{&S, px, py, kz0, Ip};
+                Seg32 sy;
+                const Seg32 sx = spa32_rule(Q_IM_AXY, Q, 0.0f, ti, &sy);
+                bool okx, oky, oks;
+                const float xe = spa32_quad_from(Q_IM_AX, Q, sx, okx).re;
+                const float ye = spa32_quad_from(Q_IM_AY, Q, sy, oky).re;
+                // S_tun = -int_{t_s}^{t_r} f dt = i int_0^{t_i} f(t_r + i tau) dtau
+                const cf Qs = spa32_quad_from(Q_ACTION, Q, spa32_rule(Q_ACTION, Q, 0.0f, ti, nullptr), oks);
+                if (okx && oky && oks) {
+                    cf A0x, A0y;
+                    spa32_AF(S, 0.0f, A0x, A0y, nullptr, nullptr);
+                    x0 = xe;
+                    y0 = ye;
+                    kx0 = (double)(px + A0x.re);
+                    ky0 = (double)(py + A0y.re);
+                    // amplitude sqrt(dkdt) exp(i S_tun) [pre] [sqrt(jac)] = sqrt(dkdt) exp(-Q) [...]
+                    double ar = sqrt(J.dkdt) * exp(-(double)Qs.re), ai = 0.0;
+                    {
+                        double sn, cs;
+                        sincos(-(double)Qs.im, &sn, &cs);
+                        ai = ar * sn;
+                        ar = ar * cs;
+                    }
+                    if (J.prefix & (ETRAJ_PREFIX_PRE | ETRAJ_PREFIX_PRECC)) {
+                        const cf kx = cmk(px + Ax.re, Ax.im), ky = cmk(py + Ay.re, Ay.im);
+                        const cf num = num32(J, B, kx, ky, kz0);
+                        const float cpre = (J.prefix & ETRAJ_PREFIX_PRE) ? (float)J.c : B.c_cc;
+                        const cf kF = cadd(cmul(kx, Fx), cmul(ky, Fy));
+                        // (k_ts . F(t_s))^((n*+1)/2) as |z|^p cis(p arg z)
+                        const float mag = powf(hypotf(kF.re, kF.im), e_half);
+                        float sn, cs;
+                        sincosf(e_half * atan2f(kF.im, kF.re), &sn, &cs);
+                        const cf den = cmk(mag * cs, mag * sn);
+                        const float dd = fmaf(den.re, den.re, den.im * den.im);
+                        const cf nd = cscale(cmul(num, cconj(den)), cpre / dd);
+                        const double r2 = ar * nd.re - ai * nd.im, i2 = ar * nd.im + ai * nd.re;
+                        ar = r2;
+                        ai = i2;
+                    }
+                    if (J.prefix & ETRAJ_PREFIX_JAC) {
+                        const double sj = sqrt((double)spa32_jac(J.laser, DB.tr, S, kd0, kz0, Ip, wF, w));
+                        ar *= sj;
+                        ai *= sj;
+                    }
+                    rate = ar * ar + ai * ai;
+                    keep = (!(rate != rate) && !(rate < J.cutoff)) ? 1 : 0;
+                    if (keep && J.phase != ETRAJ_PHASE_CTMC) ph = atan2(ai, ar);
+                }
+            }
+        }
+        const int64_t g = b * J.n_cand + i;
+        flag[g] = keep;
+        if (keep) {
+            soa.x[g] = x0;
+            soa.y[g] = y0;
+            soa.kx[g] = kx0;
+            soa.ky[g] = ky0;
+            soa.kz[g] = kz0;
+            soa.rate[g] = rate;
+            if (soa.phase) soa.phase[g] = ph;
+            soa.batch[g] = (int32_t)b;
+        }
+    }
 }
 
 __global__ void __launch_bounds__(256)
@@ -194,6 +671,14 @@ k_sample32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double*
 int launch_sample32_range(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
                           const DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
                           cudaStream_t s) {
+    if (J.method == ETRAJ_SAMPLER_SPA) {
+        const int threads = 128;
+        const int64_t want = (nb * J.n_cand + threads - 1) / threads;
+        const int64_t cap = (int64_t)sm_count * 64;
+        const int blocks = (int)(want < cap ? (want > 0 ? want : 1) : cap);
+        k_sample_spa32<<<blocks, threads, 0, s>>>(J, b0, nb, kd, kz, batches, soa, flag);
+        return 1;
+    }
     const int threads = 256;
     const int64_t want = (nb * J.n_cand + threads - 1) / threads;
     const int64_t cap = (int64_t)sm_count * 32;

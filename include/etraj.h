@@ -213,7 +213,10 @@ int etraj_batch_info(const etraj_job* job, int64_t* batch_num, int64_t* batch_ma
 int etraj_sample_batch(etraj_ctx* ctx, const etraj_job* job, int64_t batch_id,
                        double* init, int64_t capacity, int64_t* count);
 
-/* The sampling stage of the whole job, batches concatenated in order. */
+/* The sampling stage of the whole job, batches concatenated in order.  Both
+ * entry points sample as the job's precision does: FP64 for
+ * ETRAJ_PRECISION_FP64, the bulk path's FP32 candidate kernels for
+ * ETRAJ_PRECISION_FP32_BULK (atomic targets). */
 int etraj_sample_all(etraj_ctx* ctx, const etraj_job* job,
                      double* init, int64_t capacity, int64_t* count);
 
