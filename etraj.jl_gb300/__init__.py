@@ -4,6 +4,7 @@ Host side of the drop-in for eTraj.jl's trajectory-simulation hot path: the
 reference's lasers, targets and `perform_traj_simulation` keywords, driving
 the sm_103a CUDA library behind include/etraj.h.
 """
+from . import h5write, jld2
 from .abi import load_library
 from .lasers import (Laser, MonochromaticLaser, Cos4Laser, Cos2Laser, GaussianLaser,
                      BichromaticLaser)

@@ -2,11 +2,10 @@
 
 Mirrors src/TrajectorySimulation.jl:103-161 (keywords, defaults and
 checks).  The batch loop at :154-157 becomes one etraj_run call on the GPU;
-there is no CPU path.  Output: the reference writes JLD2/HDF5 files; here the
-result is returned as a dict with the same keys as that file
-(px, py[, pz], momentum_spec, ion_prob, ion_prob_uncollected,
-num_effective_traj, params_text) and, when output_path is given, saved as a
-NumPy .npz archive.
+there is no CPU path.  Output: the result is returned as a dict with the keys
+of the reference's output file (px, py[, pz], momentum_spec, ion_prob,
+ion_prob_uncollected, num_effective_traj, params_text) and, when output_path
+is given, written as that JLD2 or HDF5 file (h5write.py) or a NumPy .npz.
 """
 import ctypes as C
 import math
@@ -374,14 +373,19 @@ def perform_traj_simulation(*, init_cond_method, laser, target, dimension, sampl
                             sample_t_num, traj_t_final, final_p_max, final_p_num,
                             ss_kd_max=0.0, ss_kd_num=0, ss_kz_max=0.0, ss_kz_num=0,
                             mc_kt_num=0, mc_kd_max=0.0, mc_kz_max=0.0,
-                            traj_phase_method="CTMC", traj_rtol=1e-6, output_fmt="npz",
+                            traj_phase_method="CTMC", traj_rtol=1e-6, output_fmt="jld2",
                             output_compress=True, output_path=None, sample_monte_carlo=False,
                             sample_cutoff_limit=1e-16, rate_prefix="Full", mol_orbit_ridx=0,
                             show_progress=False, precision="fp64", seed=0, engine=None):
     """Performs a semiclassical trajectory simulation (TrajectorySimulation.jl:103-161) on the GPU.
 
-    Returns a dict with the keys of the reference's output file.  Extra keywords:
-    `precision` ("fp64" or "fp32_bulk"), `seed` (Monte-Carlo stream), `engine`."""
+    Returns a dict with the keys of the reference's output file, and writes
+    that file when `output_path` is given: `output_fmt` :jld2 (the default) or
+    :h5 as write_output! does (h5write.py; uncompressed), or "npz".  As in the
+    reference (:199-215) an existing file is not overwritten (a time-stamped
+    name is used instead) and the extension is appended when missing.  Extra
+    keywords: `precision` ("fp64" or "fp32_bulk"), `seed` (Monte-Carlo
+    stream), `engine`."""
     job = make_job(init_cond_method=init_cond_method, laser=laser, target=target,
                    dimension=dimension, sample_t_intv=sample_t_intv, sample_t_num=sample_t_num,
                    traj_t_final=traj_t_final, final_p_max=final_p_max, final_p_num=final_p_num,
@@ -389,7 +393,12 @@ def perform_traj_simulation(*, init_cond_method, laser, target, dimension, sampl
                    ss_kz_num=ss_kz_num, mc_kt_num=mc_kt_num, mc_kd_max=mc_kd_max,
                    mc_kz_max=mc_kz_max, traj_phase_method=traj_phase_method, traj_rtol=traj_rtol,
                    sample_monte_carlo=sample_monte_carlo, sample_cutoff_limit=sample_cutoff_limit,
-                   rate_prefix=rate_prefix, precision=precision, seed=seed)
+                   rate_prefix=rate_prefix, mol_orbit_ridx=mol_orbit_ridx, precision=precision, seed=seed)
+    fmt = _sym(output_fmt)
+    if fmt == "hdf5":
+        fmt = "h5"
+    if fmt not in ("jld2", "h5", "npz"):
+        raise ValueError("[TrajectorySimulationJob] Unsupported output format `%s`." % output_fmt)
     eng = engine or default_engine()
     res, spec, amp = eng.run(job, want_spectrum=True,
                              want_amplitude=(_sym(traj_phase_method) != "CTMC"))
@@ -409,9 +418,28 @@ def perform_traj_simulation(*, init_cond_method, laser, target, dimension, sampl
     if amp is not None:
         out["amplitude"] = (amp[0::2] + 1j * amp[1::2]).reshape(shape, order="F")
     if output_path:
-        path = output_path if output_path.endswith(".npz") else output_path + ".npz"
-        np.savez_compressed(path, **{k: v for k, v in out.items()}) if output_compress \
-            else np.savez(path, **out)
+        import os
+        import time
+        path = output_path
+        if os.path.isfile(path) or os.path.isfile(path + "!"):
+            warnings.warn("[TrajectorySimulationJob] File `%s` already exists, saving under a time-stamped name." % path)
+            path = time.strftime("TrajectorySimulation-%Y%m%d.%H%M%S")
+        ext = "." + fmt
+        if not path.endswith(ext):
+            path += ext
+        if fmt == "npz":
+            (np.savez_compressed if output_compress else np.savez)(path, **out)
+        else:
+            # the names and order of write_output! (TrajectorySimulation.jl:508-543)
+            from . import h5write
+            items = [("params_text", out["params_text"]), ("px", out["px"]), ("py", out["py"])]
+            if dimension == 3:
+                items.append(("pz", out["pz"]))
+            items += [("momentum_spec", out["momentum_spec"]), ("ion_prob", float(out["ion_prob"])),
+                      ("ion_prob_uncollected", float(out["ion_prob_uncollected"])),
+                      ("num_effective_traj", int(out["num_effective_traj"]))]
+            h5write.write(path + "!", items, jld2=(fmt == "jld2"))
+            os.replace(path + "!", path)
         out["output_path"] = path
     return out
 

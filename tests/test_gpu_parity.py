@@ -239,6 +239,34 @@ def test_gpu_perform_traj_simulation_api(eng):
     assert np.allclose(np.abs(out["amplitude"]) ** 2, out["momentum_spec"])
 
 
+@pytest.mark.parametrize("fmt", [":jld2", ":h5"])
+def test_gpu_perform_traj_simulation_writes_the_reference_file(eng, tmp_path, fmt):
+    """write_output!'s datasets (TrajectorySimulation.jl:502-546), read back
+    with the package's JLD2/HDF5 reader; a 3D grid keeps Julia's axis order."""
+    T = period()
+    path = str(tmp_path / "run")
+    kw = dict(init_cond_method="ADK", laser=et.Cos4Laser(peak_int=1e14, wave_len=800.0, cyc_num=2, ellip=0.5),
+              target=et.get_atom("H"), dimension=3, sample_t_intv=(-T, T), sample_t_num=20, traj_t_final=3 * T,
+              final_p_max=(1.5, 1.2, 0.8), final_p_num=(40, 30, 6), ss_kd_max=1.0, ss_kd_num=15, ss_kz_max=1.0,
+              ss_kz_num=5, traj_phase_method="QTMC", engine=eng, output_fmt=fmt, output_path=path)
+    out = et.perform_traj_simulation(**kw)
+    ext = "." + fmt[1:]
+    assert out["output_path"] == path + ext
+    d = et.jld2.load(out["output_path"])
+    assert set(d) == {"params_text", "px", "py", "pz", "momentum_spec", "ion_prob", "ion_prob_uncollected",
+                      "num_effective_traj"}
+    assert np.array_equal(d["momentum_spec"], out["momentum_spec"]) and d["momentum_spec"].shape == (40, 30, 6)
+    assert np.array_equal(d["px"], out["px"]) and np.array_equal(d["pz"], out["pz"])
+    assert d["ion_prob"] == out["ion_prob"] and d["num_effective_traj"] == out["num_effective_traj"]
+    assert d["params_text"] == out["params_text"]
+    # an existing file is kept; the next run saves under another name
+    with pytest.warns(UserWarning):
+        out2 = et.perform_traj_simulation(**{**kw, "output_path": out["output_path"]})
+    assert out2["output_path"] != out["output_path"]
+    import os
+    os.remove(out2["output_path"])
+
+
 def test_gpu_budget_refusal():
     e = et.Engine(device=0, hbm_budget_bytes=1 << 20)
     job = job_of(method="ADK", dim=2, nt=400, nkd=200)
