@@ -177,11 +177,11 @@ struct BulkParams {
     float Z, Ip, sc, a1, b1, a2, b2, a3, b3, a2b2;
     float r_far;        // SAE: radius beyond which the exp(-b r) terms are dropped
     int max_iters;      // steps before an electron is given up (status 1)
-    // Rounds: the integrator runs as kBulkRounds launches.  In round r an
-    // electron that has taken kParkBudget[r] steps in the round writes its
-    // whole state to the park buffer and frees its lane; round r+1 resumes the
-    // parked electrons packed densely (blocks without parked work exit at
-    // once).  park_buf == nullptr: one launch, no parking.
+    // Rounds: the integrator runs as kBulkRounds launches.  In round r, once
+    // the round's queue is empty, an electron that has taken kParkBudget[r]
+    // steps in the round writes its whole state to the park buffer and frees
+    // its lane; round r+1 resumes the parked electrons packed densely (blocks
+    // without parked work exit at once).  park_buf == nullptr: one launch.
     uint32_t* park_buf;   // 2 halves x park_cap entries x kParkWords words (word-major)
     int park_cap;         // entries per half
     // set per round by the launcher

@@ -254,6 +254,7 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
     float K1[DIM], kph1 = 0.0f;  // FSAL derivatives
     float mK1 = 0.0f, mph1 = 0.0f;  // and their term magnitudes
     int tn = 0, iter = 0, attempts = 0, rs = 0;  // rs: step attempts in this round
+    bool drained = false;                         // the queue was found empty
     float tfr = 0.0f, dth = 0.0f, dthp = 0.0f, dthmax = 0.0f, lqold = LOG2_QOLDINIT, q11 = 1.0f;
     bool accept = false, active = false, need = true;
     unsigned long long s = 0;
@@ -267,6 +268,7 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
             unsigned long long base = 0ull;
             if (lane == leader) base = atomicAdd(queue, (unsigned long long)__popc(needm));
             base = __shfl_sync(FULL, base, leader);
+            drained = drained || (base + (unsigned long long)__popc(needm) > n_traj);
             if (need) {
                 need = false;
                 s = base + __popc(needm & lt_mask);
@@ -412,8 +414,16 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
         }
         if (__ballot_sync(FULL, active) == 0u) break;
         if (P.park_out) {
-            // park the electrons that used up this round's step budget
-            const bool want = active && rs >= P.park_budget;
+            // park the electrons that used up this round's step budget, once the
+            // queue is empty: while it holds work they keep their lanes, so they
+            // overlap the rest of the job instead of waiting for the next round
+            bool want = active && rs >= P.park_budget;
+            if (__any_sync(FULL, want) && !drained) {
+                unsigned long long q = 0ull;
+                if (lane == 0) q = atomicAdd(queue, 0ull);
+                drained = __shfl_sync(FULL, q, 0) >= n_traj;
+            }
+            want = want && drained;
             const unsigned pm = __ballot_sync(FULL, want);
             if (pm) {
                 const int leader = __ffs(pm) - 1;

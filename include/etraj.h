@@ -313,11 +313,12 @@ int etraj_set_bulk_tile(etraj_ctx* ctx, int dimension, int phase, int target, in
  * maxiters (10^6) steps while the rest finish in ~100.  Left in place, each
  * keeps its whole thread block -- and that block's share of an SM -- resident
  * for seconds, so concurrent jobs (the serving loop) cannot get onto the GPU.
- * With repacking on (the default) the bulk integrator runs in rounds: an
- * electron that has taken 1024 steps in round 0 (then 16384, 262144 in the
- * next rounds) writes its integrator state to a device buffer and frees its
- * lane, and the next round resumes the parked electrons in as few blocks as
- * they fill.  Each electron's arithmetic does not depend on where it runs, so
+ * With repacking on (the default) the bulk integrator of a job runs in
+ * rounds: once the queue is empty, an electron that has taken 1024 steps in
+ * round 0 (then 16384, 262144 in the next rounds) writes its integrator state
+ * to a device buffer and frees its lane, and the next round resumes the parked
+ * electrons in as few blocks as they fill.  Batches (etraj_run_batch) run as
+ * one launch.  Each electron's arithmetic does not depend on where it runs, so
  * results are the same bits either way. */
 int etraj_set_straggler_repack(etraj_ctx* ctx, int enable);
 
