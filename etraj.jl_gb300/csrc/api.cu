@@ -564,12 +564,15 @@ int alloc_sampling(etraj_ctx* ctx, HostJob& H, Pipeline& P) {
     if (J.mol.on) {
         // the molecular tables; their addresses go into the device job
         double *clm = nullptr, *wint = nullptr, *tab = nullptr;
+        float* tabf = nullptr;
         if (!H.mol_clm.empty()) ETRAJ_TRY(ensure_t(ctx, "mol.clm", H.mol_clm.size(), &clm));
         if (!H.mol_wint.empty()) ETRAJ_TRY(ensure_t(ctx, "mol.wint", H.mol_wint.size(), &wint));
         ETRAJ_TRY(ensure_t(ctx, "mol.tab", (size_t)J.n_t * (size_t)J.mol.stride, &tab));
+        ETRAJ_TRY(ensure_t(ctx, "mol.tabf", (size_t)J.n_t * (size_t)J.mol.stride, &tabf));
         H.J.mol.clm = clm;
         H.J.mol.wint = wint;
         H.J.mol.tab = tab;
+        H.J.mol.tabf = tabf;
     }
     ETRAJ_TRY(ensure_t(ctx, "t", H.t.size(), &P.t));
     ETRAJ_TRY(ensure_t(ctx, "kd", H.kd.size(), &P.kd));
@@ -622,13 +625,13 @@ int alloc_outputs(etraj_ctx* ctx, const DJob& J, int64_t max_n, bool with_state,
     return ETRAJ_OK;
 }
 
-// The candidate kernel of a job: the bulk path samples in FP32 (ADK and SPANE
-// while every kept rate stays in FP32's normal range, and SPA), molecular
-// targets and the FP64 path in FP64.
+// The candidate kernel of a job: the bulk path samples in FP32 (ADK, SPANE and
+// WFAT, atoms and molecules, while every kept rate stays in FP32's normal
+// range; SPA for atoms), the FP64 path and molecular SPA in FP64.
 int launch_sampler(int precision, const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
                    const DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count, cudaStream_t s) {
-    const bool fp32 = precision == ETRAJ_PRECISION_FP32_BULK && !J.mol.on &&
-                      (J.method == ETRAJ_SAMPLER_SPA || J.cutoff >= kSample32MinCutoff);
+    const bool fp32 = precision == ETRAJ_PRECISION_FP32_BULK &&
+                      (J.method == ETRAJ_SAMPLER_SPA ? !J.mol.on : J.cutoff >= kSample32MinCutoff);
     return fp32 ? launch_sample32_range(J, b0, nb, kd, kz, batches, soa, flag, sm_count, s)
                 : launch_sample_range(J, b0, nb, kd, kz, batches, soa, flag, sm_count, s);
 }

@@ -70,6 +70,7 @@ struct DMol {
     const double* clm;   // C_lm (device copy)
     const double* wint;  // WFAT integrals (device copy)
     double* tab;         // per time sample: C D (MO-ADK) or |G|^2 and the W factors (WFAT)
+    float* tabf;         // the same table in FP32 (read by the bulk path's sampler)
 };
 
 struct DJob {

@@ -79,24 +79,37 @@ MOL_INL double mol_powi(double x, int n) {
     return (!dm_isinf(x) && !dm_isnan(x) && !dm_isinf(err) && !dm_isnan(err)) ? fma(x, y, err) : x * y;
 }
 
-// d^j_{m'm}(beta), Wigner's explicit sum (standard convention).
-MOL_FN double mol_wigner_d(int j, int mp, int m, double beta) {
-    double sh, ch;
-    dm_sincos(0.5 * beta, &sh, &ch);
-    const double pref = sqrt(mol_fact(j + mp) * mol_fact(j - mp) * mol_fact(j + m) * mol_fact(j - m));
+// n! for n <= 2 MOL_MAX_L, exact in double (the products mol_fact forms)
+#define MOL_FACT_TABLE {1.0, 1.0, 2.0, 6.0, 24.0, 120.0, 720.0, 5040.0, 40320.0, 362880.0, 3628800.0, \
+                        39916800.0, 479001600.0}
+
+// d^j_{m'm}(beta) from (sin, cos) of beta/2, Wigner's explicit sum (standard
+// convention); the powers are the running products cos^k = cos^(k-1) cos.
+MOL_FN double mol_wigner_d_sc(int j, int mp, int m, double sh, double ch) {
+    const double F[2 * MOL_MAX_L + 1] = MOL_FACT_TABLE;
+    double cp[2 * MOL_MAX_L + 1], sp[2 * MOL_MAX_L + 1];
+    cp[0] = 1.0;
+    sp[0] = 1.0;
+    for (int i = 1; i <= 2 * j; ++i) {
+        cp[i] = cp[i - 1] * ch;
+        sp[i] = sp[i - 1] * sh;
+    }
+    const double pref = sqrt(F[j + mp] * F[j - mp] * F[j + m] * F[j - m]);
     double sum = 0.0;
     for (int s = 0; s <= 2 * j; ++s) {
         const int a1 = j + m - s, a3 = mp - m + s, a4 = j - mp - s;
         if (a1 < 0 || a3 < 0 || a4 < 0) continue;
-        const double den = mol_fact(a1) * mol_fact(s) * mol_fact(a3) * mol_fact(a4);
+        const double den = F[a1] * F[s] * F[a3] * F[a4];
         const double sign = ((mp - m + s) & 1) ? -1.0 : 1.0;
-        const int pc = 2 * j + m - mp - 2 * s, ps = mp - m + 2 * s;
-        double cpow = 1.0, spow = 1.0;
-        for (int i = 0; i < pc; ++i) cpow *= ch;
-        for (int i = 0; i < ps; ++i) spow *= sh;
-        sum = sum + ((sign * pref / den) * cpow) * spow;
+        sum = sum + ((sign * pref / den) * cp[2 * j + m - mp - 2 * s]) * sp[mp - m + 2 * s];
     }
     return sum;
+}
+
+MOL_FN double mol_wigner_d(int j, int mp, int m, double beta) {
+    double sh, ch;
+    dm_sincos(0.5 * beta, &sh, &ch);
+    return mol_wigner_d_sc(j, mp, m, sh, ch);
 }
 
 // D^l_{m' m}(a, b, g) = e^{-i m' a} d^l_{m' m}(b) e^{-i m g}
@@ -254,6 +267,33 @@ MOL_FN dm_cplx mol_wfat_G(int nxi, int m, int nxi_max, int m_max, int lmax, cons
             double s, c;
             dm_sincos(-((double)mp) * chi, &s, &c);
             const dm_cplx t = dm_cmul(dm_cscale(v, mol_wigner_d(l, m, mp, theta)), dm_c(c, s));
+            sum = dm_cadd(sum, t);
+        }
+    }
+    double R[3][3];
+    mol_rotzyz(chi, theta, 0.0, R);
+    const double muz = (R[2][0] * mu[0] + R[2][1] * mu[1]) + R[2][2] * mu[2];
+    return dm_cscale(sum, dm_exp(-kappa * muz));
+}
+
+// mol_wfat_G with its Wigner d values and phase factors taken from tables:
+// d[(l (2L+1) + m + L)(2L+1) + m' + L] = d^l_{m m'}(theta) and
+// cs[2 (m' + L)] = (cos, sin) of -m' chi, L = MOL_MAX_L; the same values and
+// the same sum as mol_wfat_G (the tables are filled by mol_wigner_d and
+// dm_sincos with the same arguments).
+MOL_FN dm_cplx mol_wfat_G_tab(int nxi, int m, int nxi_max, int m_max, int lmax, const double* I, const double mu[3],
+                              double kappa, double theta, double chi, const double* d, const double* cs) {
+    const int L = MOL_MAX_L, W = 2 * MOL_MAX_L + 1;
+    dm_cplx sum = dm_c(0.0, 0.0);
+    const int am = m < 0 ? -m : m;
+    for (int l = am; l <= lmax; ++l) {
+        for (int mp = -l; mp <= l; ++mp) {
+            const long i = (long)nxi + (long)(nxi_max + 1) *
+                                           ((long)(m + m_max) + (long)(2 * m_max + 1) *
+                                                                    ((long)l + (long)(lmax + 1) * (long)(mp + l)));
+            const dm_cplx v = dm_c(I[2 * i], I[2 * i + 1]);
+            const double dv = d[(l * W + m + L) * W + mp + L];
+            const dm_cplx t = dm_cmul(dm_cscale(v, dv), dm_c(cs[2 * (mp + L)], cs[2 * (mp + L) + 1]));
             sum = dm_cadd(sum, t);
         }
     }

@@ -158,24 +158,54 @@ __global__ void k_batch_prepare(const __grid_constant__ DJob J, const double* __
 // Per-time-sample tables of a molecular target: one block per time sample,
 // threads over the table's entries (MO-ADK: C_lm D^l_{m' m}; WFAT: |G|^2 of
 // each channel and the time-sample factors of W).
+// WFAT: the Wigner d values and phase factors of a time sample are computed
+// once into shared memory and shared by its channels (G of every n_xi uses the
+// same d^l_{m m'}(beta)).
 __global__ void __launch_bounds__(128) k_mol_prepare(const __grid_constant__ DJob J, const DBatch* __restrict__ batches) {
+    constexpr int L = MOL_MAX_L, W = 2 * MOL_MAX_L + 1;
+    __shared__ double s_d[(MOL_MAX_L + 1) * W * W];
+    __shared__ double s_cs[2 * W];
     const DMol& M = J.mol;
     for (int64_t b = blockIdx.x; b < J.n_t; b += gridDim.x) {
         const DBatch& B = batches[b];
         double a, be, g;
         mol_euler(M.rot, B.Fx, B.Fy, B.F, &a, &be, &g);
         double* out = M.tab + b * (int64_t)M.stride;
+        float* outf = M.tabf + b * (int64_t)M.stride;
         if (M.wfat) {
+            __syncthreads();  // the previous time sample's tables are no longer read
+            double shb, chb;
+            dm_sincos(0.5 * be, &shb, &chb);
+            for (int q = threadIdx.x; q < (M.wl + 1) * W * W; q += blockDim.x) {
+                const int l = q / (W * W), m = (q / W) % W - L, mp = q % W - L;
+                const int am = m < 0 ? -m : m, amp = mp < 0 ? -mp : mp;
+                if (am <= l && amp <= l && am <= M.mmax) s_d[q] = mol_wigner_d_sc(l, m, mp, shb, chb);
+            }
+            for (int q = threadIdx.x; q < W; q += blockDim.x) {
+                double sn, cn;
+                dm_sincos(-((double)(q - L)) * g, &sn, &cn);
+                s_cs[2 * q] = cn;
+                s_cs[2 * q + 1] = sn;
+            }
+            __syncthreads();
             const int nch = (M.nxi + 1) * (2 * M.mmax + 1), na = (M.nxi + 1) * (M.mmax + 1);
             for (int c = threadIdx.x; c < nch + na; c += blockDim.x) {
-                out[c] = (c < nch) ? mol_wfat_g2(c, M.nxi, M.mmax, M.wl, M.wint, M.mu, J.kappa, be, g)
-                                   : mol_wfat_A(c - nch, M.nxi, J.kappa, J.nstar, B.F);
+                if (c < nch) {
+                    const int nxi = c % (M.nxi + 1), m = c / (M.nxi + 1) - M.mmax;
+                    const dm_cplx G = mol_wfat_G_tab(nxi, m, M.nxi, M.mmax, M.wl, M.wint, M.mu, J.kappa, be, g, s_d, s_cs);
+                    out[c] = G.re * G.re + G.im * G.im;
+                } else {
+                    out[c] = mol_wfat_A(c - nch, M.nxi, J.kappa, J.nstar, B.F);
+                }
+                outf[c] = (float)out[c];
             }
         } else {
             for (int e = threadIdx.x; e < M.T.ncd; e += blockDim.x) {
                 const dm_cplx v = mol_cd_entry(&M.T, M.clm, e, a, be, g);
                 out[2 * e] = v.re;
                 out[2 * e + 1] = v.im;
+                outf[2 * e] = (float)v.re;
+                outf[2 * e + 1] = (float)v.im;
             }
         }
     }

@@ -551,6 +551,48 @@ k_sample_spa32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const dou
     }
 }
 
+// Molecules (mol.h layouts; the per-time-sample tables are FP64): the MO-ADK
+// numerator sum over (l, m, m') of C_lm D^l_{m' m} Y_{l m'}, in FP32.
+__device__ cf mol_num32(const DJob& J, const float* __restrict__ cd, cf nkx, cf nky, cf nkz) {
+    const mol_terms& T = J.mol.T;
+    cf acc = cmk(0.0f, 0.0f), Y[2 * MOL_MAX_L + 1];
+    int e = 0, ycur = -1;
+    for (int k = 0; k < T.n; ++k) {
+        const int l = T.l[k];
+        if (l != ycur) {
+            for (int mp = -l; mp <= l; ++mp) {
+                const int pi = l * l + l + mp;
+                Y[mp + l] = cmul(cmk((float)J.mol.P[2 * pi], (float)J.mol.P[2 * pi + 1]), sph_sum(l, mp, nkx, nky, nkz));
+            }
+            ycur = l;
+        }
+        for (int mp = -l; mp <= l; ++mp, ++e) acc = cadd(acc, cmul(cmk(cd[2 * e], cd[2 * e + 1]), Y[mp + l]));
+    }
+    return acc;
+}
+
+// The WFAT rate (WFATSampler.jl:169) in FP32: channels n_xi fastest; each
+// channel's W as (A E) K, so the time-sample factor A (up to F^-7) never
+// meets K before the exponential has scaled it.
+__device__ float wfat_rate32(const DJob& J, const float* __restrict__ tb, float F, float kd, float kz) {
+    const int nxi = J.mol.nxi, mmax = J.mol.mmax;
+    const float* g2 = tb;
+    const float* A = tb + (nxi + 1) * (2 * mmax + 1);
+    const float k2 = fmaf(kd, kd, kz * kz);
+    const float X = (float)(J.kappa * J.kappa) + k2;
+    const float E = expf((-2.0f * (X * sqrtf(X))) / (3.0f * F));
+    float K[MOL_MAX_L + 1];
+    K[0] = 1.0f;
+    for (int a = 1; a <= mmax; ++a) K[a] = K[a - 1] * k2;
+    float sum = 0.0f;
+    for (int m = -mmax; m <= mmax; ++m) {
+        const int am = m < 0 ? -m : m;
+        for (int n = 0; n <= nxi; ++n)
+            sum = fmaf(g2[n + (m + mmax) * (nxi + 1)], (A[n + am * (nxi + 1)] * E) * K[am], sum);
+    }
+    return sum * (float)J.dkdt;
+}
+
 __global__ void __launch_bounds__(256)
 k_sample32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double* __restrict__ kdv,
            const double* __restrict__ kzv, const DBatch* __restrict__ batches, InitSoA soa,
@@ -586,7 +628,19 @@ k_sample32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double*
         }
         uint8_t keep = 0;
         float x0 = 0.0f, y0 = 0.0f, kx0 = 0.0f, ky0 = 0.0f, rate = 0.0f, ph = 0.0f;
-        if (!(fabsf(kd0) < 1e-4f)) {
+        if (J.method == ETRAJ_SAMPLER_WFAT) {
+            // WFATSampler.jl:173-240: ADK's exit point, the WFAT rate, CTMC rows
+            if (!(fmaf(kd0, kd0, kz0 * kz0) < 1e-8f)) {
+                const float F = B.F;
+                kx0 = kd0 * (-B.sphi);
+                ky0 = kd0 * B.cphi;
+                const float r0 = fmaf(0.5f, fmaf(kd0, kd0, kz0 * kz0), Ip) / F;
+                x0 = r0 * B.cphi;
+                y0 = r0 * B.sphi;
+                rate = wfat_rate32(J, J.mol.tabf + b * (int64_t)J.mol.stride, F, kd0, kz0);
+                keep = (!(rate != rate) && !(rate < cutoff)) ? 1 : 0;
+            }
+        } else if (!(fabsf(kd0) < 1e-4f)) {
             const float F = B.F;
             kx0 = kd0 * (-B.sphi);
             ky0 = kd0 * B.cphi;
@@ -630,10 +684,14 @@ k_sample32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double*
                     const cf nky = cadd(cscale(cconj(kx), B.ny0), cscale(cconj(ky), B.ny1));
                     const cf nkz = cadd(cscale(cconj(kx), B.nz0), cscale(cconj(ky), B.nz1));
                     cf num = cmk(0.0f, 0.0f);
-                    for (int mp = -J.l; mp <= J.l; ++mp) {
-                        const int ii = mp + J.l;
-                        const cf Y = cmul(cmk(J.fPlm[2 * ii], J.fPlm[2 * ii + 1]), sph_sum(J.l, mp, nkx, nky, nkz));
-                        num = cadd(num, cmul(cmk(B.CD[2 * ii], B.CD[2 * ii + 1]), Y));
+                    if (J.mol.on) {
+                        num = mol_num32(J, J.mol.tabf + b * (int64_t)J.mol.stride, nkx, nky, nkz);
+                    } else {
+                        for (int mp = -J.l; mp <= J.l; ++mp) {
+                            const int ii = mp + J.l;
+                            const cf Y = cmul(cmk(J.fPlm[2 * ii], J.fPlm[2 * ii + 1]), sph_sum(J.l, mp, nkx, nky, nkz));
+                            num = cadd(num, cmul(cmk(B.CD[2 * ii], B.CD[2 * ii + 1]), Y));
+                        }
                     }
                     const float cpre = (J.prefix & ETRAJ_PREFIX_PRE) ? c_pre : B.c_cc;
                     const float den = (e_pre == 0.5f) ? sqrtf(X2) : exp2f(e_pre * log2f(X2));

@@ -111,12 +111,37 @@ def test_molecular_bulk_path_within_fp64_band(eng, phase):
     b = job.copy()
     b.precision = abi.PRECISION_FP32_BULK
     r32, s32, _ = eng.run(b)
-    assert r32.num_effective_traj == r64.num_effective_traj > 100000
+    assert r64.num_effective_traj > 100000
+    assert abs(r32.num_effective_traj - r64.num_effective_traj) <= 1e-4 * r64.num_effective_traj + 1
     assert abs(r32.ion_prob - r64.ion_prob) <= 1e-4 * r64.ion_prob
     band = rel_l2(s64b, s64)
     assert rel_l2(s32, s64) <= 1.5 * band, (rel_l2(s32, s64), band)
     c32, c64, c64b = (s.reshape(40, 5, 40, 5).sum(axis=(1, 3)) for s in (s32, s64, s64b))
     assert rel_l2(c32, c64) <= max(1.5 * rel_l2(c64b, c64), 2e-3), (rel_l2(c32, c64), rel_l2(c64b, c64))
+
+
+@pytest.mark.parametrize("kw", [dict(method="MOADK", dim=3, phase="QTMC", rot=ROT, nkd=21, nkz=9),
+                                dict(method="MOSPANE", dim=2, phase="SCTS", mc=True, laser="cos2", nkd=400),
+                                dict(method="WFAT", dim=3, rot=ROT, nkd=21, nkz=9)],
+                         ids=["moadk-3d", "mospane-2d-mc", "wfat-3d"])
+def test_molecular_bulk_sampler_tracks_fp64(eng, kw):
+    """The bulk path samples molecules in FP32 from the FP64 per-time-sample
+    tables: the same electrons but for any within ~1e-6 of the cutoff, with
+    rates and phases to FP32 accuracy."""
+    job = mol_job(nt=60, **kw)
+    a64 = eng.sample_all(job)
+    b = job.copy()
+    b.precision = abi.PRECISION_FP32_BULK
+    a32 = eng.sample_all(b)
+    assert len(a64) > 500 and abs(len(a32) - len(a64)) <= 1e-3 * len(a64) + 1
+    n = min(len(a32), len(a64))
+    rc = 7 if job.dimension == 3 else 5
+    if len(a32) == len(a64):
+        np.testing.assert_allclose(a32[:, :rc], a64[:, :rc], rtol=1e-5, atol=1e-6)
+        np.testing.assert_allclose(a32[:, rc], a64[:, rc], rtol=2e-4)
+        if job.traj_phase_method != abi.PHASE_CTMC:
+            assert np.abs(np.angle(np.exp(1j * (a32[:, -1] - a64[:, -1])))).max() < 1e-4
+    assert abs(a32[:n, rc].sum() - a64[:n, rc].sum()) <= 1e-4 * a64[:, rc].sum()
 
 
 def test_batches_reject_molecules(eng):
