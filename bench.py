@@ -101,6 +101,10 @@ WORKLOADS = {
 # 2*(1+2+3+4+5+6)*5 = 210; error estimate 5*(2*7+6) = 100; compensated update
 # 5*8 = 40; clock, controller and bookkeeping ~40.  Total 702 per step attempt.
 FLOPS_PER_STEP_SAE_2D_SCTS = 702
+# DRAM bytes (read + write) of the integrator's round-0 launch per electron on this
+# workload, from one ncu capture of a 2e6-candidate case (24.91 MB for 8.17e5
+# electrons); traffic grows with the electrons (profiles/launches_spane_ar_scts_1e7.md).
+INTEGRATOR_DRAM_BYTES_PER_ELECTRON = 30.48
 
 
 def rank_env():
@@ -365,7 +369,7 @@ def main():
                     "d2h_bytes_per_step": 8 * grid + 64},
             "gpu_launches": launches,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                         "frac": (achieved / fp32_peak) if achieved else None, "traffic": None,
+                         "frac": (achieved / fp32_peak) if achieved else None, "traffic": (INTEGRATOR_DRAM_BYTES_PER_ELECTRON * statistics.mean(effs)) if headline else None,
                          "kernel": "k_integrate_bulk", "kernel_ms": kern_ms,
                          "flops_per_step_attempt": FLOPS_PER_STEP_SAE_2D_SCTS,
                          "step_attempts_per_job": steps_per_job,
