@@ -14,8 +14,9 @@
 // summed left to right from 0.0.
 //
 // Roofline: HBM bound.  Per trajectory and 8-bit pass: read 4 B key
-// (histogram), read 8 B + write 8 B (scatter); the segmented pass reads 8 B
-// of the sorted pair plus 16 B of contribution; passes = ceil(bits(grid+1)/8).
+// (histogram), read 8 B + write 8 B (scatter); the per-bin pass reads 8 B
+// of the sorted pair plus 16 B of contribution and 8 + 16 B per bin;
+// passes = ceil(bits(grid+1)/8).
 
 #include "engine.h"
 
@@ -174,27 +175,58 @@ k_radix_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ v
     }
 }
 
-// One pass over each bin's segment of the sorted pairs, left to right from 0.0.
+// Per-bin sums over the sorted pairs, each bin left to right from 0.0, in two
+// passes.  k_segment_bounds marks where each bin's segment of the sorted keys
+// starts and ends; k_bin_sum then gives one thread to each bin.  Neighbouring
+// bins of a spectrum hold similar numbers of trajectories, so the lanes of a
+// warp add for about the same number of iterations.  (A thread per segment
+// start instead leaves most lanes of a warp idle while one walks a long
+// segment, and every FP64 add is issued for the whole warp on GB300's narrow
+// FP64 pipe.)  The bounds (first, end) of bin k are two uint32 stored in the
+// 8-byte slot spec_re[k], zeroed beforehand, so an empty bin reads (0, 0) and
+// sums to +0.0, and k_bin_sum reads the slot before it writes the sum there.
 __global__ void __launch_bounds__(256)
-k_segment_sum(const uint32_t* __restrict__ keys, const uint32_t* __restrict__ vals,
-              const unsigned long long* __restrict__ count, uint32_t grid,
-              const double* __restrict__ c_re, const double* __restrict__ c_im, int coherent,
-              double* __restrict__ spec_re, double* __restrict__ spec_im) {
+k_segment_bounds(const uint32_t* __restrict__ keys, const unsigned long long* __restrict__ count,
+                 uint32_t grid, uint32_t* __restrict__ bounds) {
     const int64_t n = (int64_t)*count;
     for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n;
          p += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t k = keys[p];
         if (k >= grid) continue;
-        if (p > 0 && keys[p - 1] == k) continue;
+        if (p == 0 || keys[p - 1] != k) bounds[2 * (int64_t)k] = (uint32_t)p;
+        if (p == n - 1 || keys[p + 1] != k) bounds[2 * (int64_t)k + 1] = (uint32_t)(p + 1);
+    }
+}
+
+__global__ void __launch_bounds__(256)
+k_bin_sum(const uint32_t* __restrict__ vals, int64_t grid, const double* __restrict__ c_re,
+          const double* __restrict__ c_im, int coherent, double* __restrict__ spec_re,
+          double* __restrict__ spec_im) {
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < grid;
+         g += (int64_t)gridDim.x * blockDim.x) {
+        const uint2 b = reinterpret_cast<const uint2*>(spec_re)[g];
         double sr = 0.0, si = 0.0;
-        for (int64_t q = p; q < n && keys[q] == k; ++q) {
+#pragma unroll 4
+        for (uint32_t q = b.x; q < b.y; ++q) {
             const uint32_t v = vals[q];
             sr = sr + c_re[v];
             if (coherent) si = si + c_im[v];
         }
-        spec_re[k] = sr;
-        if (coherent) spec_im[k] = si;
+        spec_re[g] = sr;
+        if (coherent) spec_im[g] = si;
     }
+}
+
+int launch_bin_sums(const uint32_t* keys, const uint32_t* vals, const unsigned long long* count, int64_t max_n,
+                    int64_t grid, const double* c_re, const double* c_im, int coherent, double* spec_re,
+                    double* spec_im, cudaStream_t s) {
+    int64_t pb = (max_n + 255) / 256;
+    if (pb > 152 * 32) pb = 152 * 32;
+    int64_t gb = (grid + 255) / 256;
+    if (gb > 152 * 32) gb = 152 * 32;
+    k_segment_bounds<<<(int)(pb > 0 ? pb : 1), 256, 0, s>>>(keys, count, (uint32_t)grid, (uint32_t*)spec_re);
+    k_bin_sum<<<(int)(gb > 0 ? gb : 1), 256, 0, s>>>(vals, grid, c_re, c_im, coherent, spec_re, spec_im);
+    return 2;
 }
 
 __global__ void k_finalize_spec(const double* __restrict__ re, const double* __restrict__ im,
@@ -381,11 +413,8 @@ int launch_deposit(const DJob& J, const TrajOut& out, const unsigned long long* 
             vin = vbuf[which];
             which ^= 1;
         }
-        int sblocks = (int)((max_n + 255) / 256);
-        if (sblocks > 152 * 64) sblocks = 152 * 64;
-        k_segment_sum<<<sblocks, 256, 0, s>>>(kin, vin, count, (uint32_t)grid, out.c_re, out.c_im,
-                                              coherent, spec_re, spec_im);
-        ++launches;
+        launches += launch_bin_sums(kin, vin, count, max_n, grid, out.c_re, out.c_im, coherent, spec_re,
+                                    spec_im, s);
         // canonical 256-ary trees for ion_prob and ion_prob_uncollected
         const double* a = out.w_ion;
         const double* b = out.w_unc;
@@ -712,9 +741,7 @@ extern "C" int etraj_deposit_noalloc(int64_t n, const uint32_t* key, const doubl
             vin = vbuf[which];
             which ^= 1;
         }
-        int sblocks = (int)((n + 255) / 256);
-        k_segment_sum<<<sblocks, 256, 0, s>>>(kin, vin, count, (uint32_t)grid, c_re, c_im, coherent,
-                                              spec_re, spec_im);
+        launch_bin_sums(kin, vin, count, n, grid, c_re, c_im, coherent, spec_re, spec_im, s);
     }
     int fblocks = (int)((grid + 255) / 256);
     if (fblocks > 152 * 16) fblocks = 152 * 16;
