@@ -144,13 +144,26 @@ __device__ void spa32_base(const DLaser& L, double tr, SpaBase32& S) {
     }
 }
 
+// cosh x and sinh x from one exponential e = e^x and its reciprocal.  Below
+// |x| = 0.5, where e - 1/e would lose bits to cancellation, sinh is its Taylor
+// series x (1 + x^2/3! + x^4/5! + x^6/7!), whose truncation (x^8/9! relative)
+// is under 1.1e-8 there.
+__device__ __forceinline__ void csh32(float x, float& ch, float& sh) {
+    const float e = expf(x), ei = __frcp_rn(e);
+    ch = 0.5f * (e + ei);
+    const float x2 = x * x;
+    const float ps = x * fmaf(x2, fmaf(x2, fmaf(x2, 1.0f / 5040.0f, 1.0f / 120.0f), 1.0f / 6.0f), 1.0f);
+    sh = (fabsf(x) < 0.5f) ? ps : 0.5f * (e - ei);
+}
+
 // A (and F when fx != nullptr) at t_r + i tau
 __device__ void spa32_AF(const SpaBase32& S, float tau, cf& ax, cf& ay, cf* fx, cf* fy) {
     ax = ay = cmk(0.0f, 0.0f);
     if (fx) *fx = *fy = cmk(0.0f, 0.0f);
     for (int k = 0; k < S.n; ++k) {
         const SpaMono32& m = S.m[k];
-        const float ch = coshf(m.om * tau), sh = sinhf(m.om * tau);
+        float ch, sh;
+        csh32(m.om * tau, ch, sh);
         const cf sth = cmk(m.sth * ch, m.cth * sh), cth = cmk(m.cth * ch, -(m.sth * sh));
         cf preA, preF, cx, cy;
         if (m.kind == ETRAJ_LASER_GAUSSIAN) {
@@ -163,7 +176,8 @@ __device__ void spa32_AF(const SpaBase32& S, float tau, cf& ax, cf& ay, cf* fx, 
             cx = cadd(cmul(a, cth), cscale(sth, m.om));
             cy = cadd(cmul(a, sth), cscale(cth, -m.om));
         } else {
-            const float chu = coshf(m.w2n * tau), shu = sinhf(m.w2n * tau);
+            float chu, shu;
+            csh32(m.w2n * tau, chu, shu);
             const cf c = cmk(m.cu * chu, -(m.su * shu)), sv = cmk(m.su * chu, m.cu * shu);
             const cf c2 = cmul(c, c);
             const bool c4 = (m.kind == ETRAJ_LASER_COS4);
@@ -216,14 +230,24 @@ __device__ float spa32_dspe(const SpaBase32& S, float x, float kd, float kz, flo
     return (spa32_spe(S, x + e, kd, kz, Ip) - spa32_spe(S, x - e, kd, kz, Ip)) / (2.0f * e);
 }
 
-// t_i of the saddle point (0: not converged or t_i <= 0); spa_solve_ti in FP32
-__device__ __noinline__ float spa32_solve(const SpaBase32& S, float kd, float kz, float Ip, float x0) {
+// t_i of the saddle point (0: not converged or t_i <= 0); spa_solve_ti in FP32.
+// warm: x0 is the root of a neighbouring equation (the Jacobian's solves at
+// t_r +- 0.01 and k_d +- 0.01 start from the candidate's own t_i instead of
+// the asinh guess).  Its residual is often already inside ftol, and a root
+// accepted there would carry up to ftol / |J| of error into the Jacobian's
+// finite differences, so a warm start is accepted only at |r| <= ftol / 10
+// (ten times the FP32 rounding of the residual); otherwise one Newton step
+// takes it to rounding level.
+__device__ __noinline__ float spa32_solve(const SpaBase32& S, float kd, float kz, float Ip, float x0,
+                                          bool warm = false) {
     const float ftol = 1e-5f, eta = 1e-4f;
     float x = x0;
     float r = spa32_spe(S, x, kd, kz, Ip);
-    float J = spa32_dspe(S, x, kd, kz, Ip);
     if (!isfinite(r) || !isfinite(x)) return 0.0f;
-    bool converged = (fabsf(r) <= ftol);
+    bool converged = (fabsf(r) <= (warm ? 0.1f * ftol : ftol));
+    if (converged) return (x > 0.0f) ? x : 0.0f;
+    // the Jacobian is only needed for a further step
+    float J = spa32_dspe(S, x, kd, kz, Ip);
     float d = fabsf(J);
     if (d == 0.0f) d = 1.0f;
     float delta = fabsf(d * x);
@@ -256,9 +280,10 @@ __device__ __noinline__ float spa32_solve(const SpaBase32& S, float kd, float kz
         const float rho = (r * r - fn * fn) / (r * r - rp * rp);
         if (rho > eta) {
             r = fn;
+            converged = (fabsf(x - xold) <= 0.0f) || (fabsf(r) <= ftol);
+            if (converged) break;
             J = spa32_dspe(S, x, kd, kz, Ip);
             d = fmaxf(0.1f * d, fabsf(J));
-            converged = (fabsf(x - xold) <= 0.0f) || (fabsf(r) <= ftol);
         } else {
             x = x - p;
         }
@@ -403,16 +428,15 @@ __device__ __noinline__ cf spa32_quad_from(int kind, const SpaQ32& Q, Seg32 firs
 
 // jac(kd, kz) of SPASampler.jl:280-292 from four saddle-point solves
 __device__ __noinline__ float spa32_jac(const DLaser& L, double tr, const SpaBase32& S0, float kd, float kz, float Ip,
-                                        float wF, float w) {
+                                        float ti) {
     const float dtr = 0.01f, dkd = 0.01f;
     SpaBase32 Sp, Sm;
     spa32_base(L, tr + 0.01, Sp);
     spa32_base(L, tr - 0.01, Sm);
-    auto guess = [&](float k) { return asinhf(wF * sqrtf(fmaf(k, k, kz * kz) + 2.0f * Ip)) / w; };
-    const float ti_tp = spa32_solve(Sp, kd, kz, Ip, guess(kd));
-    const float ti_tm = spa32_solve(Sm, kd, kz, Ip, guess(kd));
-    const float ti_kp = spa32_solve(S0, kd + dkd, kz, Ip, guess(kd + dkd));
-    const float ti_km = spa32_solve(S0, kd - dkd, kz, Ip, guess(kd - dkd));
+    const float ti_tp = spa32_solve(Sp, kd, kz, Ip, ti, true);
+    const float ti_tm = spa32_solve(Sm, kd, kz, Ip, ti, true);
+    const float ti_kp = spa32_solve(S0, kd + dkd, kz, Ip, ti, true);
+    const float ti_km = spa32_solve(S0, kd - dkd, kz, Ip, ti, true);
     cf ax, ay;
     float pxa, pya, pxb, pyb;
     spa32_AF(Sp, ti_tp, ax, ay, nullptr, nullptr);
@@ -526,7 +550,7 @@ k_sample_spa32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const dou
                         ai = i2;
                     }
                     if (J.prefix & ETRAJ_PREFIX_JAC) {
-                        const double sj = sqrt((double)spa32_jac(J.laser, DB.tr, S, kd0, kz0, Ip, wF, w));
+                        const double sj = sqrt((double)spa32_jac(J.laser, DB.tr, S, kd0, kz0, Ip, ti));
                         ar *= sj;
                         ai *= sj;
                     }

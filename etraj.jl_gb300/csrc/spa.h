@@ -102,10 +102,13 @@ SPA_HEAVY double spa_solve_ti(const SPA_LASER_T* L, spa_win* W, double tr, doubl
     const double ftol = 1e-8, eta = 1e-4;
     double x = x0;
     double r = spa_spe(L, W, tr, x, kd, kz, Ip);
-    double J = spa_dspe(L, W, tr, x, kd, kz, Ip);
     if (dm_isnan(r) || dm_isinf(r)) return 0.0; /* NLsolve rejects a non-finite f(x0) */
     int converged = (fabs(r) <= ftol);
     if (dm_isnan(x)) return 0.0;
+    if (converged) return (x > 0.0) ? x : 0.0;
+    /* the Jacobian is only needed for a further step: it is evaluated after
+     * the convergence test, which changes no iterate */
+    double J = spa_dspe(L, W, tr, x, kd, kz, Ip);
     double d = fabs(J);
     if (d == 0.0) d = 1.0;
     double delta = fabs(d * x);
@@ -144,10 +147,11 @@ SPA_HEAVY double spa_solve_ti(const SPA_LASER_T* L, spa_win* W, double tr, doubl
         const double rho = (r * r - fn * fn) / (r * r - rp * rp);
         if (rho > eta) {
             r = fn;
+            converged = (fabs(x - xold) <= 0.0) || (fabs(r) <= ftol);
+            if (converged) break;
             J = spa_dspe(L, W, tr, x, kd, kz, Ip);
             const double dj = fabs(J), d1 = 0.1 * d;
             d = (d1 > dj) ? d1 : dj;
-            converged = (fabs(x - xold) <= 0.0) || (fabs(r) <= ftol);
         } else {
             x = x - p;
         }
