@@ -629,7 +629,7 @@ int alloc_outputs(etraj_ctx* ctx, const DJob& J, int64_t max_n, bool with_state,
 // WFAT, atoms and molecules, while every kept rate stays in FP32's normal
 // range; SPA for atoms), the FP64 path and molecular SPA in FP64.
 int launch_sampler(int precision, const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
-                   const DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count, cudaStream_t s) {
+                   DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count, cudaStream_t s) {
     const bool fp32 = precision == ETRAJ_PRECISION_FP32_BULK &&
                       (J.method == ETRAJ_SAMPLER_SPA ? !J.mol.on : J.cutoff >= kSample32MinCutoff);
     return fp32 ? launch_sample32_range(J, b0, nb, kd, kz, batches, soa, flag, sm_count, s)

@@ -48,11 +48,27 @@ struct FBatch {
     float CD[2 * 9];
 };
 
+// The laser of one time sample in the form the FP32 SPA sampler evaluates it
+// at complex times t_r + i tau (sampler_fp32.cu, spa32_base and spa32_AF).
+struct SpaMono32 {
+    float cth, sth, cu, su;   // cos, sin of the carrier and envelope phases at t_r
+    float om, w2n, cN;        // carrier and envelope angular frequencies, envelope factor
+    float preA, preF;         // A0 (F0) times the tanh windows (Cos) or the Gaussian at t_r
+    float gt, gi, inv_s2;     // Gaussian: t_r - t_shift, 1/(2 sigma^2), 1/sigma^2
+    float ellip, cphi, sphi;
+    int kind, azi0;
+};
+struct SpaBase32 {
+    int n;
+    SpaMono32 m[2];
+};
+
 struct DBatch {
     double tr, Fx, Fy, dFx, dFy, F, sphi, cphi, c_cc, W;
     double ny0, ny1, nz0, nz1;
     double D[2 * 9];  // D^l_{m' m}, m' = -l..l, interleaved (re, im)
     FBatch f;
+    SpaBase32 spa[3];  // FP32 SPA sampler: the laser at t_r, t_r + 0.01, t_r - 0.01
 };
 
 constexpr int kMaxL = 4;
@@ -131,8 +147,9 @@ int launch_sample_range(const DJob& J, int64_t b0, int64_t nb, const double* kd,
                         cudaStream_t s);
 // FP32 variant of the same kernel for the bulk path (sampler_fp32.cu); used
 // when the rate cutoff keeps every kept rate in FP32's normal range.
+// Its SPA variant first fills batches[b].spa of the batches it samples.
 int launch_sample32_range(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
-                          const DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
+                          DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
                           cudaStream_t s);
 constexpr double kSample32MinCutoff = 1e-30;
 // Order-preserving compaction: idx[k] = k-th i with flag[i] != 0; *count = total.

@@ -89,19 +89,6 @@ __device__ cf sph_sum(int l, int m, cf x, cf y, cf z) {
 enum { Q_IM_AX = 0, Q_IM_AY = 1, Q_ACTION = 2, Q_IM_AXY = 3 };
 constexpr int kSegs32 = 48;  // interval budget of one quadrature
 
-struct SpaMono32 {
-    float cth, sth, cu, su;   // cos, sin of the carrier and envelope phases at t_r
-    float om, w2n, cN;        // carrier and envelope angular frequencies, envelope factor
-    float preA, preF;         // A0 (F0) times the tanh windows (Cos) or the Gaussian at t_r
-    float gt, gi, inv_s2;     // Gaussian: t_r - t_shift, 1/(2 sigma^2), 1/sigma^2
-    float ellip, cphi, sphi;
-    int kind, azi0;
-};
-struct SpaBase32 {
-    int n;
-    SpaMono32 m[2];
-};
-
 __device__ void spa32_base(const DLaser& L, double tr, SpaBase32& S) {
     S.n = L.nmono;
     for (int k = 0; k < L.nmono; ++k) {
@@ -427,12 +414,9 @@ __device__ __noinline__ cf spa32_quad_from(int kind, const SpaQ32& Q, Seg32 firs
 }
 
 // jac(kd, kz) of SPASampler.jl:280-292 from four saddle-point solves
-__device__ __noinline__ float spa32_jac(const DLaser& L, double tr, const SpaBase32& S0, float kd, float kz, float Ip,
-                                        float ti) {
+__device__ __noinline__ float spa32_jac(const SpaBase32& S0, const SpaBase32& Sp, const SpaBase32& Sm, float kd,
+                                        float kz, float Ip, float ti) {
     const float dtr = 0.01f, dkd = 0.01f;
-    SpaBase32 Sp, Sm;
-    spa32_base(L, tr + 0.01, Sp);
-    spa32_base(L, tr - 0.01, Sm);
     const float ti_tp = spa32_solve(Sp, kd, kz, Ip, ti, true);
     const float ti_tm = spa32_solve(Sm, kd, kz, Ip, ti, true);
     const float ti_kp = spa32_solve(S0, kd + dkd, kz, Ip, ti, true);
@@ -466,6 +450,17 @@ __device__ cf num32(const DJob& J, const FBatch& B, cf kx, cf ky, float kz0) {
     return num;
 }
 
+// batches[b].spa of the sampled batches: one thread per (time sample, t_r + {0, 0.01, -0.01})
+__global__ void k_spa32_bases(const __grid_constant__ DJob J, int64_t b0, int64_t nb, DBatch* __restrict__ batches) {
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < 3 * nb;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        DBatch& DB = batches[b0 + q / 3];
+        const int w = (int)(q % 3);
+        const double tr = DB.tr;
+        spa32_base(J.laser, (w == 0) ? tr : (w == 1) ? tr + 0.01 : tr - 0.01, DB.spa[w]);
+    }
+}
+
 __global__ void __launch_bounds__(128)
 k_sample_spa32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double* __restrict__ kdv,
                const double* __restrict__ kzv, const DBatch* __restrict__ batches, InitSoA soa,
@@ -473,6 +468,7 @@ k_sample_spa32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const dou
     const int64_t total = nb * J.n_cand;
     const float Ip = (float)J.Ip, kd_max = (float)J.mc_kd_max, kz_max = (float)J.mc_kz_max;
     const float w = (float)J.spa_omega, e_half = (float)((J.nstar + 1.0) / 2.0);
+    const float log_dkdt = (float)log(J.dkdt);
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
          q += (int64_t)gridDim.x * blockDim.x) {
         const int64_t bl = q / J.n_cand, i = q - bl * J.n_cand, b = b0 + bl;
@@ -500,8 +496,7 @@ k_sample_spa32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const dou
         double x0 = 0.0, y0 = 0.0, kx0 = 0.0, ky0 = 0.0, rate = 0.0, ph = 0.0;
         // the batch is skipped when F(t_r) <= 1e-3 (SPASampler.jl:167-169)
         if (!(fabsf(kd0) < 1e-4f) && DB.F > 1e-3) {
-            SpaBase32 S;
-            spa32_base(J.laser, DB.tr, S);
+            const SpaBase32 S = DB.spa[0];
             const float wF = w / B.F;
             const float guess = asinhf(wF * sqrtf(fmaf(kd0, kd0, kz0 * kz0) + 2.0f * Ip)) / w;
             const float ti = spa32_solve(S, kd0, kz0, Ip, guess);
@@ -525,14 +520,9 @@ k_sample_spa32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const dou
                     y0 = ye;
                     kx0 = (double)(px + A0x.re);
                     ky0 = (double)(py + A0y.re);
-                    // amplitude sqrt(dkdt) exp(i S_tun) [pre] [sqrt(jac)] = sqrt(dkdt) exp(-Q) [...]
-                    double ar = sqrt(J.dkdt) * exp(-(double)Qs.re), ai = 0.0;
-                    {
-                        double sn, cs;
-                        sincos(-(double)Qs.im, &sn, &cs);
-                        ai = ar * sn;
-                        ar = ar * cs;
-                    }
+                    // amplitude sqrt(dkdt) exp(i S_tun) [pre] [sqrt(jac)] = sqrt(dkdt) exp(-Q) [...],
+                    // kept as its log-rate lr = log |amp|^2 - log dkdt and phase arg
+                    float lr = -2.0f * Qs.re, arg = -Qs.im;
                     if (J.prefix & (ETRAJ_PREFIX_PRE | ETRAJ_PREFIX_PRECC)) {
                         const cf kx = cmk(px + Ax.re, Ax.im), ky = cmk(py + Ay.re, Ay.im);
                         const cf num = num32(J, B, kx, ky, kz0);
@@ -545,18 +535,21 @@ k_sample_spa32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const dou
                         const cf den = cmk(mag * cs, mag * sn);
                         const float dd = fmaf(den.re, den.re, den.im * den.im);
                         const cf nd = cscale(cmul(num, cconj(den)), cpre / dd);
-                        const double r2 = ar * nd.re - ai * nd.im, i2 = ar * nd.im + ai * nd.re;
-                        ar = r2;
-                        ai = i2;
+                        lr += 2.0f * logf(hypotf(nd.re, nd.im));
+                        arg += atan2f(nd.im, nd.re);
                     }
-                    if (J.prefix & ETRAJ_PREFIX_JAC) {
-                        const double sj = sqrt((double)spa32_jac(J.laser, DB.tr, S, kd0, kz0, Ip, ti));
-                        ar *= sj;
-                        ai *= sj;
-                    }
-                    rate = ar * ar + ai * ai;
+                    if (J.prefix & ETRAJ_PREFIX_JAC) lr += logf(spa32_jac(S, DB.spa[1], DB.spa[2], kd0, kz0, Ip, ti));
+                    lr += log_dkdt;
+                    // FP32's exp down to its normal range, FP64 below
+                    rate = (lr >= -87.0f) ? (double)expf(lr) : exp((double)lr);
                     keep = (!(rate != rate) && !(rate < J.cutoff)) ? 1 : 0;
-                    if (keep && J.phase != ETRAJ_PHASE_CTMC) ph = atan2(ai, ar);
+                    if (keep && J.phase != ETRAJ_PHASE_CTMC) {
+                        // arg reduced to [-pi, pi]: k 2 pi subtracted with 2 pi split in two
+                        // floats (Cody and Waite's reduction)
+                        const float k = rintf(arg * 0.159154943f);
+                        const float r = fmaf(-k, -1.7484556e-7f, fmaf(-k, 6.28318548f, arg));
+                        ph = (double)r;
+                    }
                 }
             }
         }
@@ -751,15 +744,17 @@ k_sample32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double*
 }  // namespace
 
 int launch_sample32_range(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
-                          const DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
+                          DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
                           cudaStream_t s) {
     if (J.method == ETRAJ_SAMPLER_SPA) {
+        const int64_t bb = (3 * nb + 127) / 128;
+        k_spa32_bases<<<(int)(bb > 0 ? bb : 1), 128, 0, s>>>(J, b0, nb, batches);
         const int threads = 128;
         const int64_t want = (nb * J.n_cand + threads - 1) / threads;
         const int64_t cap = (int64_t)sm_count * 64;
         const int blocks = (int)(want < cap ? (want > 0 ? want : 1) : cap);
         k_sample_spa32<<<blocks, threads, 0, s>>>(J, b0, nb, kd, kz, batches, soa, flag);
-        return 1;
+        return 2;
     }
     const int threads = 256;
     const int64_t want = (nb * J.n_cand + threads - 1) / threads;
