@@ -506,20 +506,14 @@ k_sample_spa32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const dou
                 float px, py;
                 spa32_pxy(kd0, Ax, Ay, px, py);
                 SpaQ32 Q{&S, px, py, kz0, Ip};
-                Seg32 sy;
-                const Seg32 sx = spa32_rule(Q_IM_AXY, Q, 0.0f, ti, &sy);
-                bool okx, oky, oks;
-                const float xe = spa32_quad_from(Q_IM_AX, Q, sx, okx).re;
-                const float ye = spa32_quad_from(Q_IM_AY, Q, sy, oky).re;
+                bool oks;
                 // S_tun = -int_{t_s}^{t_r} f dt = i int_0^{t_i} f(t_r + i tau) dtau
                 const cf Qs = spa32_quad_from(Q_ACTION, Q, spa32_rule(Q_ACTION, Q, 0.0f, ti, nullptr), oks);
-                if (okx && oky && oks) {
-                    cf A0x, A0y;
-                    spa32_AF(S, 0.0f, A0x, A0y, nullptr, nullptr);
-                    x0 = xe;
-                    y0 = ye;
-                    kx0 = (double)(px + A0x.re);
-                    ky0 = (double)(py + A0y.re);
+                // The exit position's two quadratures come after the rate, for the
+                // candidates it keeps only: consecutive candidates share t_r, and the
+                // warps of a time sample whose field keeps none skip them.  A failed
+                // quadrature drops the candidate, as it did before the rate.
+                if (oks) {
                     // amplitude sqrt(dkdt) exp(i S_tun) [pre] [sqrt(jac)] = sqrt(dkdt) exp(-Q) [...],
                     // kept as its log-rate lr = log |amp|^2 - log dkdt and phase arg
                     float lr = -2.0f * Qs.re, arg = -Qs.im;
@@ -543,6 +537,18 @@ k_sample_spa32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const dou
                     // FP32's exp down to its normal range, FP64 below
                     rate = (lr >= -87.0f) ? (double)expf(lr) : exp((double)lr);
                     keep = (!(rate != rate) && !(rate < J.cutoff)) ? 1 : 0;
+                    if (keep) {
+                        Seg32 sy;
+                        const Seg32 sx = spa32_rule(Q_IM_AXY, Q, 0.0f, ti, &sy);
+                        bool okx, oky;
+                        x0 = spa32_quad_from(Q_IM_AX, Q, sx, okx).re;
+                        y0 = spa32_quad_from(Q_IM_AY, Q, sy, oky).re;
+                        keep = (okx && oky) ? 1 : 0;
+                        cf A0x, A0y;
+                        spa32_AF(S, 0.0f, A0x, A0y, nullptr, nullptr);
+                        kx0 = (double)(px + A0x.re);
+                        ky0 = (double)(py + A0y.re);
+                    }
                     if (keep && J.phase != ETRAJ_PHASE_CTMC) {
                         // arg reduced to [-pi, pi]: k 2 pi subtracted with 2 pi split in two
                         // floats (Cody and Waite's reduction)
