@@ -279,6 +279,7 @@ def main():
 
     # accuracy: FP32-bulk against the FP64 plain path on the same sampled electrons
     acc = accuracy_report(eng, job, job64) if not args.no_fp64_compare else None
+    tstats = trajectory_stats(eng, job, job64) if not args.no_fp64_compare else None
 
     def sync_all():
         torch.cuda.synchronize(dev)
@@ -363,6 +364,7 @@ def main():
             "speedup_fp32_bulk_vs_fp64": acc and value / world / acc["fp64_plain"]["value"],
             "pmd_rel_l2_vs_fp64": acc and acc["pmd_rel_l2_vs_fp64"],
             "accuracy": acc,
+            "trajectory_stats": tstats,
             "latency_ms": {"p50": float(np.percentile(ms, 50)), "p99": float(np.percentile(ms, 99))},
             "stages_ms": stages,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * (args.t_num + 2),
@@ -425,6 +427,32 @@ def accuracy_report(eng, job, job64):
         out["pmd_rel_l2_vs_fp64_rebin%d" % f] = l2(rebin(spec, f), rebin(spec64, f))
         out["fp64_rtol1e-7_vs_rtol1e-6_rebin%d" % f] = l2(rebin(spec64b, f), rebin(spec64, f))
     return out
+
+
+def trajectory_stats(eng, job, job64):
+    """The workload's per-trajectory character: the share of survivors that return
+    within r < 5 a.u. of the core (least |r| over the FP64 path's accepted steps)
+    and the distribution of Tsit5 step attempts per survivor on both paths, with
+    power-of-two bins (bin k counts 2^k <= steps < 2^(k+1))."""
+    eng.keep_final_states(True)
+    try:
+        r64, _, _ = eng.run(job64)
+        rmin = eng.dump_min_radius(r64.num_effective_traj)
+        s64 = eng.dump_step_counts(r64.num_effective_traj)
+        r32, _, _ = eng.run(job)
+        s32 = eng.dump_step_counts(r32.num_effective_traj)
+    finally:
+        eng.keep_final_states(False)
+
+    def hist(s):
+        if s.size == 0:
+            return None
+        bins = np.bincount(np.floor(np.log2(np.maximum(s, 1))).astype(np.int64))
+        return {"mean": float(s.mean()), "p50": float(np.percentile(s, 50)), "p99": float(np.percentile(s, 99)),
+                "max": int(s.max()), "log2_bins": [int(x) for x in bins]}
+
+    return {"frac_rmin_below_5": float(np.mean(rmin < 5.0)) if rmin.size else None,
+            "steps_fp64": hist(s64), "steps_bulk": hist(s32)}
 
 
 def serving_requests(n=512, rate=20.0, seed=2024):

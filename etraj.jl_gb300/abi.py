@@ -140,6 +140,7 @@ SIGNATURES = [
     ("etraj_set_keep_final_states", C.c_int, [C.c_void_p, C.c_int]),
     ("etraj_dump_final_states", C.c_int, [C.c_void_p, C.c_uint64, _DP, _DP, _I32P]),
     ("etraj_dump_step_counts", C.c_int, [C.c_void_p, C.c_uint64, _I32P]),
+    ("etraj_dump_min_radius", C.c_int, [C.c_void_p, C.c_uint64, _DP]),
     ("etraj_stage_times", C.c_int, [C.c_void_p, _DP, C.c_int]),
     ("etraj_deposit_noalloc", C.c_int, [C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64,
                                         C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -609,9 +609,11 @@ int alloc_outputs(etraj_ctx* ctx, const DJob& J, int64_t max_n, bool with_state,
     if (ctx->keep_states) {
         ETRAJ_TRY(ensure_t(ctx, "out.p_inf", 3 * n, &P.out.p_inf));
         ETRAJ_TRY(ensure_t(ctx, "out.fphase", n, &P.out.fphase));
+        ETRAJ_TRY(ensure_t(ctx, "out.rmin", n, &P.out.rmin));
     } else {
         P.out.p_inf = nullptr;
         P.out.fphase = nullptr;
+        P.out.rmin = nullptr;
     }
     void* dep = nullptr;
     ETRAJ_TRY(ensure(ctx, "deposit", deposit_scratch_bytes(max_n), &dep));
@@ -1109,6 +1111,7 @@ int enqueue_job(etraj_ctx* ctx, const etraj_job* job, JobRec& r) {
     ctx->dump_valid = ctx->keep_states;
     ctx->dump_ticket = r.ticket;
     ctx->dump_out = P.out;
+    if (job->precision != ETRAJ_PRECISION_FP64) ctx->dump_out.rmin = nullptr;  // filled by the FP64 path only
     ctx->dump_count = P.count;
     return ETRAJ_OK;
 }
@@ -2018,6 +2021,20 @@ int etraj_dump_step_counts(etraj_ctx* ctx, uint64_t ticket, int32_t* steps) {
     if (n == 0) return ETRAJ_OK;
     cudaError_t e = cudaMemcpy(steps, ctx->dump_out.steps, (size_t)n * 4, cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) return cuda_err(ctx, e, "step counts");
+    return ETRAJ_OK;
+}
+
+int etraj_dump_min_radius(etraj_ctx* ctx, uint64_t ticket, double* rmin) {
+    if (!ctx || !rmin) return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    cudaSetDevice(ctx->device);
+    int64_t n = 0;
+    ETRAJ_TRY(dump_prepare(ctx, ticket, &n));
+    if (!ctx->dump_out.rmin)
+        return set_err(ctx, ETRAJ_ERR_UNSUPPORTED, "the least radius is tracked by the FP64 path only");
+    if (n == 0) return ETRAJ_OK;
+    cudaError_t e = cudaMemcpy(rmin, ctx->dump_out.rmin, (size_t)n * 8, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_err(ctx, e, "least radius");
     return ETRAJ_OK;
 }
 

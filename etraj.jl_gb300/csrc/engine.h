@@ -129,6 +129,7 @@ struct TrajOut {
     double* final_state; // optional: n_state doubles per survivor (row-major)
     double* p_inf;       // optional: 3 doubles per survivor
     double* fphase;      // optional: final phase per survivor (0 for CTMC)
+    double* rmin;        // optional, FP64 path: least |r| over the accepted steps
 };
 
 struct Counters {

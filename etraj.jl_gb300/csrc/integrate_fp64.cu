@@ -91,10 +91,19 @@ __device__ double initdt(const DJob& J, double t, const double* u0, const double
     return jmax(dtmin, jmin(jmin(100.0 * dt0, dt1), dtmax));
 }
 
-// One adaptive Tsit5 solve; returns the status (0 Success).
+// r^2 of a state, summed left to right
+template <int DIM>
+__device__ __forceinline__ double radius2(const double* u) {
+    double r2 = u[0] * u[0] + u[1] * u[1];
+    if (DIM == 3) r2 = r2 + u[2] * u[2];
+    return r2;
+}
+
+// One adaptive Tsit5 solve; returns the status (0 Success).  rmin (optional):
+// the least |r| of the initial state and of the end of every accepted step.
 template <int DIM, int PHASE, int TGT, int N>
 __device__ int solve(const DJob& J, double t0, double tf, const double* u0, double* uout,
-                     int32_t& attempts) {
+                     int32_t& attempts, double* rmin = nullptr) {
     double uprev[N], u[N], tmp[N];
     double k1[N], k2[N], k3[N], k4[N], k5[N], k6[N], k7[N];
     double t = t0;
@@ -105,6 +114,7 @@ __device__ int solve(const DJob& J, double t0, double tf, const double* u0, doub
     rhs<DIM, PHASE, TGT>(J, t, uprev, k1);
     double dt = initdt<DIM, PHASE, TGT, N>(J, t, uprev, k1, dtmax, dtmin);
     double dtpropose = dt, qold = QOLDINIT, q11 = 1.0;
+    double r2min = rmin ? radius2<DIM>(uprev) : 0.0;
     bool accept = false;
     int status = 0;
     long iter = 0;
@@ -217,8 +227,10 @@ __device__ int solve(const DJob& J, double t0, double tf, const double* u0, doub
             double dtnew = dt / q;
             t = (fabs(t1 - tf) < 100.0 * d_ulp(jmax(t, tf))) ? tf : t1;
             dtpropose = jmax(jmin(dtmax, dtnew), dtmin);
+            if (rmin) r2min = jmin(r2min, radius2<DIM>(u));
         }
     }
+    if (rmin) *rmin = sqrt(r2min);
 #pragma unroll
     for (int j = 0; j < N; ++j) uout[j] = (status == 0) ? u[j] : uprev[j];
     return status;
@@ -345,8 +357,10 @@ k_integrate_fp64(const __grid_constant__ DJob J, InitSoA soa, const double* __re
         if (PHASE != ETRAJ_PHASE_CTMC) u0[N - 1] = soa.phase[g];
         const double t0 = tsamp[soa.batch[g]];
         int32_t attempts = 0;
-        int st = solve<DIM, PHASE, TGT, N>(J, t0, J.t_final, u0, uf, attempts);
+        double rmin = 0.0;
+        int st = solve<DIM, PHASE, TGT, N>(J, t0, J.t_final, u0, uf, attempts, out.rmin ? &rmin : nullptr);
         out.steps[s] = attempts;
+        if (out.rmin) out.rmin[s] = rmin;
         if (out.final_state) {
 #pragma unroll
             for (int j = 0; j < N; ++j) out.final_state[s * N + j] = uf[j];

@@ -234,6 +234,13 @@ class Engine:
         self._check(self.lib.etraj_dump_step_counts(self.ctx, ticket, steps.ctypes.data_as(C.POINTER(C.c_int32))))
         return steps
 
+    def dump_min_radius(self, n, ticket=0):
+        """Least |r| of each of the last FP64-path job's n survivors (initial state
+        and the end of every accepted step)."""
+        r = np.zeros(n)
+        self._check(self.lib.etraj_dump_min_radius(self.ctx, ticket, abi.dptr(r)))
+        return r
+
     def set_bulk_tile(self, dimension, phase, target, threads, blocks_per_sm, refill_min, multi=False):
         """Pin a bulk-integrator variant's launch shape on this engine."""
         self._check(self.lib.etraj_set_bulk_tile(self.ctx, dimension, phase, target, 1 if multi else 0,

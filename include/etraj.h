@@ -335,10 +335,15 @@ int etraj_set_straggler_repack(etraj_ctx* ctx, int enable);
  * etraj_dump_final_states copies them (n = num_effective_traj rows; any pointer
  * may be NULL) for `ticket` (0: the last job) once the job has finished; the
  * data is kept until the context's next job.  ETRAJ_ERR_NOT_FOUND otherwise.
- * etraj_dump_step_counts gives each survivor's Tsit5 step attempts. */
+ * etraj_dump_step_counts gives each survivor's Tsit5 step attempts, and
+ * etraj_dump_min_radius, for a job of the FP64 path (ETRAJ_ERR_UNSUPPORTED for
+ * the bulk path), each survivor's least distance |r| from the core over its
+ * initial state and the end of every accepted step: how close a trajectory
+ * returns to the core (rescattering), which sets how many steps it needs. */
 int etraj_set_keep_final_states(etraj_ctx* ctx, int enable);
 int etraj_dump_final_states(etraj_ctx* ctx, uint64_t ticket, double* p_inf, double* phase, int32_t* status);
 int etraj_dump_step_counts(etraj_ctx* ctx, uint64_t ticket, int32_t* steps);
+int etraj_dump_min_radius(etraj_ctx* ctx, uint64_t ticket, double* rmin);
 
 /* ---- diagnostics ----------------------------------------------------------------
  * Device time (ms) of the stages of the last etraj_run on this context: sampling,

@@ -45,6 +45,10 @@ int oracle_sample_all(const etraj_job* job, double* init, int64_t capacity,
                       int64_t* count, int nthreads);
 int oracle_integrate(const etraj_job* job, int64_t n, const double* init, double* final_state,
                      int32_t* status, int32_t* steps, int nthreads);
+/* oracle_integrate with each trajectory's least |r| (the initial state and the
+ * end of every accepted step) in rmin[i] (may be NULL). */
+int oracle_integrate_rmin(const etraj_job* job, int64_t n, const double* init, double* final_state,
+                          int32_t* status, int32_t* steps, double* rmin, int nthreads);
 int oracle_collect(const etraj_job* job, int64_t n, const double* init, const double* final_state,
                    const int32_t* status, const int32_t* steps, double* spec, double* amp,
                    double* scalars, double* p_inf, int32_t* bin);

@@ -103,9 +103,18 @@ static double o_initdt(const o_sys* S, double t, const double* u0, const double*
     return o_jmax(dtmin, o_jmin(o_jmin(100.0 * dt0, dt1), dtmax));
 }
 
-/* Integrates one trajectory from (t0, u0) to tf.  Returns the status code. */
+/* r^2 of a state, summed left to right */
+static double o_radius2(const o_sys* S, const double* u) {
+    double r2 = u[0] * u[0] + u[1] * u[1];
+    if (S->dim == 3) r2 = r2 + u[2] * u[2];
+    return r2;
+}
+
+/* Integrates one trajectory from (t0, u0) to tf.  Returns the status code.
+ * rmin (optional): the least |r| of the initial state and of the end of every
+ * accepted step. */
 static int o_solve(const o_sys* S, double t0, double tf, const double* u0, double* u_out,
-                   int32_t* nsteps) {
+                   int32_t* nsteps, double* rmin) {
     const int n = S->n;
     double uprev[7], u[7], k[7][7], tmp[7], s;
     double t = t0;
@@ -115,6 +124,7 @@ static int o_solve(const o_sys* S, double t0, double tf, const double* u0, doubl
     o_rhs(S, t, uprev, k[0]);
     double dt = o_initdt(S, t, uprev, k[0], dtmax, dtmin);
     double dtpropose = dt, qold = TS_QOLDINIT, q11 = 1.0;
+    double r2min = rmin ? o_radius2(S, uprev) : 0.0;
     int accept = 0, status = ST_SUCCESS;
     long iter = 0;
     int32_t attempts = 0;
@@ -180,10 +190,12 @@ static int o_solve(const o_sys* S, double t0, double tf, const double* u0, doubl
             double dtnew = dt / q;
             t = (fabs(ttmp - tf) < 100.0 * o_ulp(o_jmax(t, tf))) ? tf : ttmp;
             dtpropose = o_jmax(o_jmin(dtmax, dtnew), dtmin);
+            if (rmin) r2min = o_jmin(r2min, o_radius2(S, u));
         }
     }
     for (int j = 0; j < n; ++j) u_out[j] = (status == ST_SUCCESS) ? u[j] : uprev[j];
     if (nsteps) *nsteps = attempts;
+    if (rmin) *rmin = sqrt(r2min);
     return status;
 }
 
@@ -277,6 +289,11 @@ int oracle_validate(const etraj_job* job, char* msg, int len) {
 /* ---- integrate ------------------------------------------------------------------------ */
 int oracle_integrate(const etraj_job* job, int64_t n, const double* init, double* final_state,
                      int32_t* status, int32_t* steps, int nthreads) {
+    return oracle_integrate_rmin(job, n, init, final_state, status, steps, NULL, nthreads);
+}
+
+int oracle_integrate_rmin(const etraj_job* job, int64_t n, const double* init, double* final_state,
+                          int32_t* status, int32_t* steps, double* rmin, int nthreads) {
     o_sys S;
     o_sys_prepare(job, &S);
     int rows = (S.dim == 3) ? ((S.phase == ETRAJ_PHASE_CTMC) ? 8 : 9) : ((S.phase == ETRAJ_PHASE_CTMC) ? 6 : 7);
@@ -290,7 +307,7 @@ int oracle_integrate(const etraj_job* job, int64_t n, const double* init, double
         for (int j = 0; j < nq; ++j) u0[j] = r[j];
         if (S.phase != ETRAJ_PHASE_CTMC) u0[nq] = r[rows - 1];
         int32_t ns = 0;
-        int st = o_solve(&S, r[tcol], job->traj_t_final, u0, uf, &ns);
+        int st = o_solve(&S, r[tcol], job->traj_t_final, u0, uf, &ns, rmin ? rmin + i : NULL);
         if (final_state)
             for (int j = 0; j < S.n; ++j) final_state[i * S.n + j] = uf[j];
         if (status) status[i] = st;

@@ -39,6 +39,7 @@ def lib():
             "oracle_sample_batch": (C.c_int, [_JP, C.c_int64, _DP, C.c_int64, _I64P]),
             "oracle_sample_all": (C.c_int, [_JP, _DP, C.c_int64, _I64P, C.c_int]),
             "oracle_integrate": (C.c_int, [_JP, C.c_int64, _DP, _DP, _I32P, _I32P, C.c_int]),
+            "oracle_integrate_rmin": (C.c_int, [_JP, C.c_int64, _DP, _DP, _I32P, _I32P, _DP, C.c_int]),
             "oracle_collect": (C.c_int, [_JP, C.c_int64, _DP, _DP, _I32P, _I32P, _DP, _DP, _DP, _DP, _I32P]),
             "oracle_run": (C.c_int, [_JP, _DP, _DP, _DP, C.c_int]),
             "oracle_contributions": (C.c_int, [_JP, C.c_int64, _DP, _DP, _I32P, C.c_void_p, _DP, _DP]),
@@ -117,6 +118,19 @@ def integrate(job, init):
     lib().oracle_integrate(C.byref(job), n, _p(init), _p(fin), status.ctypes.data_as(_I32P),
                            steps.ctypes.data_as(_I32P), nthreads())
     return fin, status, steps
+
+
+def integrate_rmin(job, init):
+    """integrate() plus each trajectory's least |r| over its accepted steps."""
+    init = np.ascontiguousarray(init, dtype=np.float64)
+    n = init.shape[0]
+    fin = np.zeros((n, job.state_size))
+    status = np.zeros(n, dtype=np.int32)
+    steps = np.zeros(n, dtype=np.int32)
+    rmin = np.zeros(n)
+    lib().oracle_integrate_rmin(C.byref(job), n, _p(init), _p(fin), status.ctypes.data_as(_I32P),
+                                steps.ctypes.data_as(_I32P), _p(rmin), nthreads())
+    return fin, status, steps, rmin
 
 
 def collect(job, init, fin, status, steps=None):

@@ -330,6 +330,31 @@ def test_gpu_dump_final_states_match_oracle(eng, phase):
         np.testing.assert_allclose(w * np.sin(ph[dep]), cim[dep], rtol=1e-12, atol=1e-14 * w.max())
 
 
+@pytest.mark.parametrize("dim", [2, 3])
+def test_gpu_dump_min_radius_matches_oracle(eng, dim):
+    """Each survivor's least |r| over its accepted steps, bit for bit; the bulk
+    path does not track it."""
+    job = job_of(method="ADK", dim=dim, phase="QTMC", target="Ar", nt=16, nkd=9, nkz=5, laser="cos2", ellip=0.5)
+    eng.keep_final_states(True)
+    try:
+        res, _, _ = eng.run(job)
+        n = res.num_effective_traj
+        rmin = eng.dump_min_radius(n)
+        b = job.copy()
+        b.precision = abi.PRECISION_FP32_BULK
+        eng.run(b)
+        with pytest.raises(et.EtrajError) as e:
+            eng.dump_min_radius(n)
+        assert e.value.status == abi.ERR_UNSUPPORTED
+    finally:
+        eng.keep_final_states(False)
+    init = O.sample_all(job)
+    _, _, _, rref = O.integrate_rmin(job, init)
+    assert n == init.shape[0] > 0
+    assert same_bits(rmin, rref)
+    assert rmin.min() < 5.0 < rmin.max()
+
+
 def test_gpu_dump_final_states_bookkeeping(eng):
     job = job_of(method="ADK", dim=2, nt=8, nkd=11)
     eng.run(job)  # not kept

@@ -215,6 +215,24 @@ def test_tsit5_order_conditions():
     assert abs(bt.sum()) < 1e-16
 
 
+def test_least_radius_of_the_oracle():
+    """The least |r| of a trajectory is at most its initial radius and at most
+    its final radius, and matches a plain integrate() step for step."""
+    T = 2 * math.pi / (45.563352525 / 800.0)
+    job = et.make_job(init_cond_method="ADK", laser=et.Cos4Laser(peak_int=1e14, wave_len=800.0, cyc_num=2, ellip=0.0),
+                      target=et.get_atom("H"), dimension=2, sample_t_intv=(-T, T), sample_t_num=6,
+                      traj_t_final=2 * T, final_p_max=(1.5, 1.5), final_p_num=(32, 32), ss_kd_max=1.0,
+                      ss_kd_num=9, ss_kz_num=0, ss_kz_max=0.0, traj_phase_method="CTMC")
+    init = O.sample_all(job)
+    assert init.shape[0] > 10
+    fin, st, steps, rmin = O.integrate_rmin(job, init)
+    fin0, st0, steps0 = O.integrate(job, init)
+    assert np.array_equal(fin, fin0) and np.array_equal(st, st0) and np.array_equal(steps, steps0)
+    r0 = np.hypot(init[:, 0], init[:, 1])
+    rf = np.hypot(fin[:, 0], fin[:, 1])
+    assert np.all(rmin > 0.0) and np.all(rmin <= r0) and np.all(rmin[st == 0] <= rf[st == 0])
+
+
 def _ulp_err(got, ref):
     ref = np.asarray(ref, dtype=np.float64)
     sp = np.spacing(np.abs(ref))
