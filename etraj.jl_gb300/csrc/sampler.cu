@@ -504,14 +504,12 @@ k_sample_spa(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const doubl
                 Q.py = py;
                 Q.kz = kz0;
                 Q.Ip = Ip;
-                int ok01, ok2;
-                spa_exit(&Q, ti, &x0, &y0, &ok01);
-                double axr, ayr;
-                laser_A(J.laser, tr, axr, ayr);
-                kx0 = px + axr;
-                ky0 = py + ayr;
+                int ok2;
                 const dm_cplx Si = spa_quadgk(SPA_INT_ACTION, &Q, dm_c(tr, ti), dm_c(tr, 0.0), &ok2);
-                if (ok01 && ok2) {
+                // the exit position (two quadratures) is computed after the rate, for
+                // the candidates it keeps only; a failed quadrature drops the candidate
+                // as before, and no value changes
+                if (ok2) {
                     const dm_cplx St = dm_cneg(Si);
                     const dm_cplx iS = dm_c(0.0 * St.re - 1.0 * St.im, 0.0 * St.im + 1.0 * St.re);
                     dm_cplx amp = dm_cscale(dm_cexp(iS), sqrt(J.dkdt));
@@ -526,6 +524,15 @@ k_sample_spa(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const doubl
                     if (J.prefix & ETRAJ_PREFIX_JAC) amp = dm_cscale(amp, sqrt(spa_jac(&J.laser, &W, tr, kd0, kz0, Ip, wF, w)));
                     rate = amp.re * amp.re + amp.im * amp.im;
                     keep = (!(rate != rate) && !(rate < J.cutoff)) ? 1 : 0;
+                    if (keep) {
+                        int ok01;
+                        spa_exit(&Q, ti, &x0, &y0, &ok01);
+                        keep = ok01 ? 1 : 0;
+                        double axr, ayr;
+                        laser_A(J.laser, tr, axr, ayr);
+                        kx0 = px + axr;
+                        ky0 = py + ayr;
+                    }
                     if (keep && J.phase != ETRAJ_PHASE_CTMC) ph = dm_carg(amp);
                 }
             }
