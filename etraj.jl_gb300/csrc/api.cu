@@ -316,6 +316,8 @@ void prepare_job(const etraj_job* job, HostJob& H) {
                     const dm_cplx P = mol_sph_prefactor(l, mp, kap);
                     M.P[2 * (l * l + l + mp)] = P.re;
                     M.P[2 * (l * l + l + mp) + 1] = P.im;
+                    M.Pf[2 * (l * l + l + mp)] = (float)P.re;
+                    M.Pf[2 * (l * l + l + mp) + 1] = (float)P.im;
                 }
             M.stride = std::max(2 * M.T.ncd, 2);
         }
@@ -377,6 +379,22 @@ void prepare_job(const etraj_job* job, HostJob& H) {
         H.kz.assign(1, 0.0);
     }
     J.n_total = J.n_t * J.n_cand;
+    FJobConst& fc = J.fc;
+    fc.Ip = (float)J.Ip;
+    fc.kap2 = (float)(J.kappa * J.kappa);
+    fc.dkdt = (float)J.dkdt;
+    fc.sqdkdt = (float)std::sqrt(J.dkdt);
+    fc.inv_dkdt = (float)(1.0 / J.dkdt);
+    fc.log_dkdt = (float)std::log(J.dkdt);
+    fc.cutoff = (float)J.cutoff;
+    fc.e_pre = (float)J.e_pre;
+    fc.c = (float)J.c;
+    fc.e_half = (float)((J.nstar + 1.0) / 2.0);
+    fc.spa_omega = (float)J.spa_omega;
+    fc.kd_max = (float)J.mc_kd_max;
+    fc.kz_max = (float)J.mc_kz_max;
+    fc.kd_zero = (J.mc_kd_max == 0.0) ? 1 : 0;
+    fc.kz_zero = (J.mc_kz_max == 0.0) ? 1 : 0;
     J.rtol = job->traj_rtol;
     J.t_final = job->traj_t_final;
     J.grid = 1;

@@ -44,6 +44,7 @@ struct DTarget {
 // FP32 copies read by the bulk path's sampler (CD = C * D).
 struct FBatch {
     float Fx, Fy, dFx, dFy, F, sphi, cphi, c_cc, W;
+    int spa_on;  // SPA: F(t_r) > 1e-3 (decided in FP64)
     float ny0, ny1, nz0, nz1;
     float CD[2 * 9];
 };
@@ -83,10 +84,21 @@ struct DMol {
     double rot[3];       // MolRotation
     double mu[3];        // WFAT orbital dipole
     double P[2 * MOL_NLM];   // Y_{l m'} prefactors (complex)
+    float Pf[2 * MOL_NLM];   // the same in FP32 (the bulk path's sampler)
     const double* clm;   // C_lm (device copy)
     const double* wint;  // WFAT integrals (device copy)
     double* tab;         // per time sample: C D (MO-ADK) or |G|^2 and the W factors (WFAT)
     float* tabf;         // the same table in FP32 (read by the bulk path's sampler)
+};
+
+// Job constants in FP32 for the bulk path's candidate kernels, rounded once on
+// the host (each is the float nearest the FP64 value, or of the FP64 expression
+// named), so the kernels do no FP64 work to set up.
+struct FJobConst {
+    float Ip, kap2, dkdt, sqdkdt, inv_dkdt, log_dkdt;  // kappa^2, sqrt(dkdt), 1/dkdt, log(dkdt)
+    float cutoff, e_pre, c, e_half, spa_omega;   // e_half = (n* + 1)/2
+    float kd_max, kz_max;                        // Monte-Carlo half-widths
+    int kd_zero, kz_zero;                        // mc_kd_max == 0, mc_kz_max == 0
 };
 
 struct DJob {
@@ -100,6 +112,7 @@ struct DJob {
     uint64_t seed;
     double Plm[2 * (2 * kMaxL + 1)];
     float fPlm[2 * (2 * kMaxL + 1)];  // FP32 copy for the bulk path's sampler
+    FJobConst fc;
     // integration
     double rtol, t_final;
     // collection

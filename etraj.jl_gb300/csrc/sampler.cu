@@ -143,6 +143,7 @@ __global__ void k_batch_prepare(const __grid_constant__ DJob J, const double* __
     B.f.dFx = (float)B.dFx;
     B.f.dFy = (float)B.dFy;
     B.f.F = (float)B.F;
+    B.f.spa_on = (B.F > 1e-3) ? 1 : 0;
     B.f.sphi = (float)B.sphi;
     B.f.cphi = (float)B.cphi;
     B.f.c_cc = (float)B.c_cc;

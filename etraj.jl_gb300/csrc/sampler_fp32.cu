@@ -34,11 +34,29 @@ __device__ __forceinline__ cf cpowi(cf z, int n) {
     return r;
 }
 
-__device__ __forceinline__ float factf(int n) {
-    float f = 1.0f;
-    for (int i = 2; i <= n; ++i) f *= (float)i;
-    return f;
+// Coefficients (-1)^k / (2^(2k+m) (k+m)! k! (l-m-2k)!) of the solid harmonic's
+// k-sum for l <= 6, m = -l..l, k = max(0, -m) + j (j < 4), rounded once at
+// compile time: every factor and product is an integer below 2^24, so the only
+// rounding is the one correctly rounded division a kernel would do.
+struct SphCoef {
+    float c[MOL_MAX_L + 1][2 * MOL_MAX_L + 1][4];
+};
+constexpr float sph_fact(int n) { return n <= 1 ? 1.0f : (float)n * sph_fact(n - 1); }
+constexpr SphCoef sph_coef_table() {
+    SphCoef t{};
+    for (int l = 0; l <= MOL_MAX_L; ++l)
+        for (int m = -l; m <= l; ++m) {
+            const int kmin = (m < 0) ? -m : 0, kmax = (l - m) / 2;
+            for (int k = kmin; k <= kmax && k - kmin < 4; ++k) {
+                float p2 = 1.0f;
+                for (int i = 0; i < 2 * k + m; ++i) p2 *= 2.0f;
+                t.c[l][m + l][k - kmin] =
+                    ((k & 1) ? -1.0f : 1.0f) / (p2 * sph_fact(k + m) * sph_fact(k) * sph_fact(l - m - 2 * k));
+            }
+        }
+    return t;
 }
+__constant__ SphCoef kSph = sph_coef_table();
 
 __device__ __forceinline__ void philox4x32(uint32_t c[4], uint64_t seed) {
     uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
@@ -63,9 +81,7 @@ __device__ cf sph_sum(int l, int m, cf x, cf y, cf z) {
     const int kmin = (m < 0) ? -m : 0, kmax = (l - m) / 2;
     cf acc = cmk(0.0f, 0.0f);
     for (int k = kmin; k <= kmax; ++k) {
-        float p2 = 1.0f;
-        for (int i = 0; i < 2 * k + m; ++i) p2 *= 2.0f;
-        const float coef = ((k & 1) ? -1.0f : 1.0f) / (p2 * factf(k + m) * factf(k) * factf(l - m - 2 * k));
+        const float coef = kSph.c[l][m + l][k - kmin];
         cf tt = cscale(cpowi(xp, k + m), coef);
         tt = cmul(tt, cpowi(xm, k));
         tt = cmul(tt, cpowi(z, l - m - 2 * k));
@@ -466,9 +482,9 @@ k_sample_spa32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const dou
                const double* __restrict__ kzv, const DBatch* __restrict__ batches, InitSoA soa,
                uint8_t* __restrict__ flag) {
     const int64_t total = nb * J.n_cand;
-    const float Ip = (float)J.Ip, kd_max = (float)J.mc_kd_max, kz_max = (float)J.mc_kz_max;
-    const float w = (float)J.spa_omega, e_half = (float)((J.nstar + 1.0) / 2.0);
-    const float log_dkdt = (float)log(J.dkdt);
+    const float Ip = J.fc.Ip, kd_max = J.fc.kd_max, kz_max = J.fc.kz_max;
+    const float w = J.fc.spa_omega, e_half = J.fc.e_half;
+    const float log_dkdt = J.fc.log_dkdt;
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
          q += (int64_t)gridDim.x * blockDim.x) {
         const int64_t bl = q / J.n_cand, i = q - bl * J.n_cand, b = b0 + bl;
@@ -486,8 +502,8 @@ k_sample_spa32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const dou
             kd0 = ((ua - 0.5f) * 2.0f) * kd_max;
             if (J.dim == 3) {
                 kz0 = ((ub - 0.5f) * 2.0f) * kz_max;
-                if (J.mc_kd_max == 0.0) kd0 = 0.0f;
-                else if (J.mc_kz_max == 0.0) kz0 = 0.0f;
+                if (J.fc.kd_zero) kd0 = 0.0f;
+                else if (J.fc.kz_zero) kz0 = 0.0f;
             } else {
                 kz0 = 0.0f;
             }
@@ -495,7 +511,7 @@ k_sample_spa32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const dou
         uint8_t keep = 0;
         double x0 = 0.0, y0 = 0.0, kx0 = 0.0, ky0 = 0.0, rate = 0.0, ph = 0.0;
         // the batch is skipped when F(t_r) <= 1e-3 (SPASampler.jl:167-169)
-        if (!(fabsf(kd0) < 1e-4f) && DB.F > 1e-3) {
+        if (!(fabsf(kd0) < 1e-4f) && B.spa_on) {
             const SpaBase32 S = DB.spa[0];
             const float wF = w / B.F;
             const float guess = asinhf(wF * sqrtf(fmaf(kd0, kd0, kz0 * kz0) + 2.0f * Ip)) / w;
@@ -520,7 +536,7 @@ k_sample_spa32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const dou
                     if (J.prefix & (ETRAJ_PREFIX_PRE | ETRAJ_PREFIX_PRECC)) {
                         const cf kx = cmk(px + Ax.re, Ax.im), ky = cmk(py + Ay.re, Ay.im);
                         const cf num = num32(J, B, kx, ky, kz0);
-                        const float cpre = (J.prefix & ETRAJ_PREFIX_PRE) ? (float)J.c : B.c_cc;
+                        const float cpre = (J.prefix & ETRAJ_PREFIX_PRE) ? J.fc.c : B.c_cc;
                         const cf kF = cadd(cmul(kx, Fx), cmul(ky, Fy));
                         // (k_ts . F(t_s))^((n*+1)/2) as |z|^p cis(p arg z)
                         const float mag = powf(hypotf(kF.re, kF.im), e_half);
@@ -585,7 +601,7 @@ __device__ cf mol_num32(const DJob& J, const float* __restrict__ cd, cf nkx, cf 
         if (l != ycur) {
             for (int mp = -l; mp <= l; ++mp) {
                 const int pi = l * l + l + mp;
-                Y[mp + l] = cmul(cmk((float)J.mol.P[2 * pi], (float)J.mol.P[2 * pi + 1]), sph_sum(l, mp, nkx, nky, nkz));
+                Y[mp + l] = cmul(cmk(J.mol.Pf[2 * pi], J.mol.Pf[2 * pi + 1]), sph_sum(l, mp, nkx, nky, nkz));
             }
             ycur = l;
         }
@@ -602,7 +618,7 @@ __device__ float wfat_rate32(const DJob& J, const float* __restrict__ tb, float 
     const float* g2 = tb;
     const float* A = tb + (nxi + 1) * (2 * mmax + 1);
     const float k2 = fmaf(kd, kd, kz * kz);
-    const float X = (float)(J.kappa * J.kappa) + k2;
+    const float X = J.fc.kap2 + k2;
     const float E = expf((-2.0f * (X * sqrtf(X))) / (3.0f * F));
     float K[MOL_MAX_L + 1];
     K[0] = 1.0f;
@@ -613,38 +629,70 @@ __device__ float wfat_rate32(const DJob& J, const float* __restrict__ tb, float 
         for (int n = 0; n <= nxi; ++n)
             sum = fmaf(g2[n + (m + mmax) * (nxi + 1)], (A[n + am * (nxi + 1)] * E) * K[am], sum);
     }
-    return sum * (float)J.dkdt;
+    return sum * J.fc.dkdt;
 }
 
+// Stores float f as the double of equal value without the FP64 pipe (which on
+// GB300 also executes conversions, at 1/64 of the FP32 rate): IEEE 754 gives a
+// normal float and its double the same sign and significand, with the exponent
+// rebiased from 127 to 1023, and zeros, infinities and NaNs (payload kept) map
+// field by field.  The two 32-bit halves are stored directly.  Subnormal
+// floats take the conversion instruction.
+__device__ __forceinline__ void store_f2d(double* dst, float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t e = (u >> 23) & 0xFFu, m = u & 0x7FFFFFu;
+    if (e == 0u && m != 0u) {
+        *dst = (double)f;
+        return;
+    }
+    const uint32_t ed = (e == 0u) ? 0u : (e == 0xFFu) ? 0x7FFu : e + 896u;
+    *reinterpret_cast<uint2*>(dst) = make_uint2(m << 29, (u & 0x80000000u) | (ed << 20) | (m >> 3));
+}
+
+// x 2^-24 for an integer 0 <= x < 2^24, exactly and without a conversion
+// instruction: 1 + (x >> 1) 2^-23 is built from its bits, 1 subtracted
+// (exact), and the low bit of x added back (the sum has at most 24
+// significant bits, so it is exact too).
+__device__ __forceinline__ float u24_unit(uint32_t x) {
+    const float a = __uint_as_float(0x3F800000u | (x >> 1)) - 1.0f;
+    return a + (float)(x & 1u) * 5.9604644775390625e-8f;
+}
+
+// One candidate per thread.  A thread's (time sample, candidate) pair advances
+// by the grid's stride without dividing, so the 64-bit divisions that split a
+// flat candidate index run once per thread instead of once per candidate.
 __global__ void __launch_bounds__(256)
 k_sample32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double* __restrict__ kdv,
            const double* __restrict__ kzv, const DBatch* __restrict__ batches, InitSoA soa,
            uint8_t* __restrict__ flag) {
-    const int64_t total = nb * J.n_cand;
-    const float Ip = (float)J.Ip, kap2 = (float)(J.kappa * J.kappa), sqdkdt = (float)sqrt(J.dkdt);
-    const float inv_dkdt = (float)(1.0 / J.dkdt), cutoff = (float)J.cutoff, e_pre = (float)J.e_pre;
-    const float c_pre = (float)J.c, kd_max = (float)J.mc_kd_max, kz_max = (float)J.mc_kz_max;
-    const float spane_lim = J.mc ? 0.04f : (float)(1.0 / 9.0);
+    const float Ip = J.fc.Ip, kap2 = J.fc.kap2, sqdkdt = J.fc.sqdkdt;
+    const float inv_dkdt = J.fc.inv_dkdt, cutoff = J.fc.cutoff, e_pre = J.fc.e_pre;
+    const float c_pre = J.fc.c, kd_max = J.fc.kd_max, kz_max = J.fc.kz_max;
+    const float spane_lim = J.mc ? 0.04f : 0.111111111f;  // 1/25, 1/9
     const bool spane = (J.method == ETRAJ_SAMPLER_SPANE);
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
-         q += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t bl = q / J.n_cand, i = q - bl * J.n_cand, b = b0 + bl;
+    const int64_t n = J.n_cand, stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t step_b = stride / n, step_i = stride - step_b * n;
+    const int64_t q0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t bl = q0 / n, i = q0 - bl * n;
+    for (; bl < nb; bl += step_b, i += step_i, bl += (i >= n) ? 1 : 0, i -= (i >= n) ? n : 0) {
+        const int64_t b = b0 + bl;
         const FBatch& B = batches[b].f;
         float kd0, kz0;
         if (!J.mc) {
-            kd0 = (float)kdv[i / J.n_kz];
-            kz0 = (float)kzv[i % J.n_kz];
+            const int64_t ik = i / J.n_kz;
+            kd0 = (float)kdv[ik];
+            kz0 = (float)kzv[i - ik * J.n_kz];
         } else {
             uint32_t c[4] = {(uint32_t)i, (uint32_t)((uint64_t)i >> 32), (uint32_t)b, 0x4B445A00u};
             philox4x32(c, J.seed);
             // the leading 24 bits of the FP64 sampler's 53-bit uniforms
-            const float ua = (float)(c[0] >> 8) * 5.9604644775390625e-8f;
-            const float ub = (float)(c[2] >> 8) * 5.9604644775390625e-8f;
+            const float ua = u24_unit(c[0] >> 8);
+            const float ub = u24_unit(c[2] >> 8);
             kd0 = ((ua - 0.5f) * 2.0f) * kd_max;
             if (J.dim == 3) {
                 kz0 = ((ub - 0.5f) * 2.0f) * kz_max;
-                if (J.mc_kd_max == 0.0) kd0 = 0.0f;
-                else if (J.mc_kz_max == 0.0) kz0 = 0.0f;
+                if (J.fc.kd_zero) kd0 = 0.0f;
+                else if (J.fc.kz_zero) kz0 = 0.0f;
             } else {
                 kz0 = 0.0f;
             }
@@ -735,13 +783,13 @@ k_sample32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double*
         const int64_t g = b * J.n_cand + i;
         flag[g] = keep;
         if (keep) {
-            soa.x[g] = x0;
-            soa.y[g] = y0;
-            soa.kx[g] = kx0;
-            soa.ky[g] = ky0;
-            soa.kz[g] = kz0;
-            soa.rate[g] = rate;
-            if (soa.phase) soa.phase[g] = ph;
+            store_f2d(soa.x + g, x0);
+            store_f2d(soa.y + g, y0);
+            store_f2d(soa.kx + g, kx0);
+            store_f2d(soa.ky + g, ky0);
+            store_f2d(soa.kz + g, kz0);
+            store_f2d(soa.rate + g, rate);
+            if (soa.phase) store_f2d(soa.phase + g, ph);
             soa.batch[g] = (int32_t)b;
         }
     }
