@@ -36,7 +36,7 @@ import numpy as np  # noqa: E402
 import __graft_entry__  # noqa: E402
 
 et = __graft_entry__.load_package()
-from etraj_gb300 import abi  # noqa: E402
+from etraj_gb300 import abi, shards  # noqa: E402
 
 METRIC = "trajectories/sec on 1 GB300 (FP32-bulk vs FP64 plain, PMD L2 <=1e-3); p50/p99 job latency"
 UNIT = "trajectories/s"
@@ -273,8 +273,9 @@ def main():
     if args.t_num is None:
         args.t_num = t_full
     headline = (args.workload == "ar_spane_scts_2d")
-    job = maker(args.precision, seed=rank, t_num=args.t_num)
-    job64 = maker("fp64", seed=rank, t_num=args.t_num)
+    # one Monte-Carlo shard per rank (seed = rank), weight 1/world in a merge
+    job, shard_w = shards.shard_job(maker(args.precision, seed=0, t_num=args.t_num), rank, world)
+    job64, _ = shards.shard_job(maker("fp64", seed=0, t_num=args.t_num), rank, world)
     grid = job.grid_size
 
     # accuracy: FP32-bulk against the FP64 plain path on the same sampled electrons
@@ -316,13 +317,11 @@ def main():
         sync_all()
         t_wall = time.perf_counter() - t_wall
     ms = lat
-    t_max = torch.tensor([t_start.elapsed_time(t_end)], device=dev)
+    t_local = t_start.elapsed_time(t_end) / 1e3
     if world > 1:
-        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
-    eff_total = torch.tensor([float(sum(effs))], device=dev)
-    if world > 1:
-        dist.all_reduce(eff_total)
-    value = eff_total.item() / (t_max.item() / 1e3)
+        _, _, value = shards.aggregate_throughput(sum(effs), t_local)
+    else:
+        value = sum(effs) / t_local
 
     # kernel-level timing of the bulk integrator for the roofline
     stages = stage_times(eng, job)
@@ -348,13 +347,20 @@ def main():
             tk, r = inflight.pop(0)
             eng.wait(tk, r)
             e2e_effs.append(r.num_effective_traj)
-    t_e2e = torch.tensor([time.perf_counter() - t_e2e], device=dev)
+    t_e2e = time.perf_counter() - t_e2e
     if world > 1:
-        dist.all_reduce(t_e2e, op=dist.ReduceOp.MAX)
-    e2e_total = torch.tensor([float(sum(e2e_effs))], device=dev)
+        _, _, e2e_value = shards.aggregate_throughput(sum(e2e_effs), t_e2e)
+    else:
+        e2e_value = sum(e2e_effs) / t_e2e
+
+    # N > 1 (untimed): the shards merged into one job's result by one all-reduce
+    merged = None
     if world > 1:
-        dist.all_reduce(e2e_total)
-    e2e_value = e2e_total.item() / t_e2e.item()
+        coh = shards.is_coherent(job)
+        r1, s1, a1 = eng.run(job, want_spectrum=not coh, want_amplitude=coh)
+        mspec, mion, munc, meff = shards.merge_shards(r1, s1, a1, shard_w, coh)
+        merged = {"num_effective_traj": meff, "ion_prob": mion, "ion_prob_uncollected": munc,
+                  "momentum_spec_sum": float(mspec.sum())}
 
     if rank == 0:
         peaks = measured_peaks()
@@ -381,6 +387,7 @@ def main():
             "pmd_rel_l2_vs_fp64": acc and acc["pmd_rel_l2_vs_fp64"],
             "accuracy": acc,
             "trajectory_stats": tstats,
+            "merged_shards": merged,
             "latency_ms": {"p50": float(np.percentile(ms, 50)), "p99": float(np.percentile(ms, 99))},
             "stages_ms": stages,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * (args.t_num + 2),
