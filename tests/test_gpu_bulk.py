@@ -264,3 +264,39 @@ def test_bulk_spa_pmd_within_fp64_band(eng):
     assert rel_l2(s32, s64) <= 1.5 * rel_l2(s64b, s64), (rel_l2(s32, s64), rel_l2(s64b, s64))
     c32, c64, c64b = (rebin(s, (100, 100), 10) for s in (s32, s64, s64b))
     assert rel_l2(c32, c64) <= max(2.0 * rel_l2(c64b, c64), 5e-3), (rel_l2(c32, c64), rel_l2(c64b, c64))
+
+
+# ---- edge cases of the bulk path ---------------------------------------------------------
+
+@pytest.mark.parametrize("method", ["ADK", "SPANE"])
+def test_bulk_empty_job(eng, method):
+    """No candidate survives the cutoff: no trajectory, zero spectrum and
+    probabilities, as on the FP64 path (ADKSampler.jl:392-394)."""
+    job = bulk(job_of(method=method, dim=2, phase="SCTS", target="Ar", cutoff=1e300))
+    res, spec, amp = eng.run(job, want_amplitude=True)
+    assert res.num_effective_traj == 0 and res.ion_prob == 0.0 and res.ion_prob_uncollected == 0.0
+    assert not spec.any() and not amp.any()
+
+
+def test_bulk_two_electrons(eng):
+    """Four candidates (kd = -0.2 at t = -T, -T/3, T/3, T; the field vanishes at
+    +-T): the bulk path keeps the FP64 path's two electrons and their weights."""
+    job = job_of(method="ADK", dim=2, phase="QTMC", target="H", nt=4, nkd=1, nkz=1, intensity=4e14)
+    job.ss_kd_max = 0.2
+    r64, s64, _ = eng.run(job)
+    r32, s32, _ = eng.run(bulk(job))
+    assert r64.num_effective_traj == r32.num_effective_traj == 2
+    assert r32.ion_prob == pytest.approx(r64.ion_prob, rel=1e-5)
+    assert s32.sum() == pytest.approx(s64.sum(), rel=1e-4)
+
+
+@pytest.mark.parametrize("pnum", [(1, 50), (50, 1)])
+def test_bulk_single_bin_axis(eng, pnum):
+    """final_p_num = 1 along an axis puts every electron in its one bin
+    (TrajectorySimulation.jl:254-260, the index rule for num = 1)."""
+    job = job_of(method="ADK", dim=2, phase="CTMC", target="H", nt=40, nkd=21, pnum=pnum)
+    r64, s64, _ = eng.run(job)
+    r32, s32, _ = eng.run(bulk(job))
+    assert r32.num_effective_traj == r64.num_effective_traj > 0
+    assert s32.sum() == pytest.approx(s64.sum(), rel=1e-4)
+    assert rel_l2(s32, s64) <= 0.05
