@@ -162,10 +162,15 @@ int validate_job(const etraj_job* job, std::string& err) {
             if (!(job->ss_kd_num > 0 && job->ss_kz_num > 0)) return fail("[ADKSampler] Invalid kd,kz sample number.");
             if (!(job->ss_kd_max > 0 || job->ss_kz_max > 0))
                 return fail("[ADKSampler] Invalid kd,kz sample boundaries (cannot be zero simultaneously).");
+            if (job->ss_kz_num == 1 && job->ss_kz_max != 0)
+                return fail("range(-abs(ss_kz_max), abs(ss_kz_max); length=1): endpoints differ.");
         } else {
             if (!(job->ss_kd_num > 0)) return fail("[ADKSampler] Invalid kd sample number.");
             if (!(job->ss_kd_max > 0)) return fail("[ADKSampler] Invalid kd sample boundaries.");
         }
+        // Julia's range(a, b; length=1) needs a == b (ADKSampler.jl:85,97)
+        if (job->ss_kd_num == 1 && job->ss_kd_max != 0)
+            return fail("range(-abs(ss_kd_max), abs(ss_kd_max); length=1): endpoints differ.");
     } else {
         if (!(job->mc_kt_num > 0)) return fail("[ADKSampler] Invalid sampling kt_num.");
         if (job->dimension == 3) {

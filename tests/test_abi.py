@@ -80,6 +80,10 @@ def test_validate_without_gpu():
     bad.ss_kd_num = 0
     assert lib.etraj_validate(C.byref(bad), buf, 256) == abi.ERR_INVALID_ARGUMENT
     bad = job.copy()
+    bad.ss_kd_num = 1  # Julia's range(-1.0, 1.0; length=1) throws: the endpoints differ
+    assert lib.etraj_validate(C.byref(bad), buf, 256) == abi.ERR_INVALID_ARGUMENT
+    assert b"endpoints differ" in buf.value
+    bad = job.copy()
     bad.target.l = 5
     bad.target.m = 0
     assert lib.etraj_validate(C.byref(bad), buf, 256) == abi.ERR_UNSUPPORTED

@@ -278,14 +278,14 @@ def test_bulk_empty_job(eng, method):
     assert not spec.any() and not amp.any()
 
 
-def test_bulk_two_electrons(eng):
-    """Four candidates (kd = -0.2 at t = -T, -T/3, T/3, T; the field vanishes at
-    +-T): the bulk path keeps the FP64 path's two electrons and their weights."""
-    job = job_of(method="ADK", dim=2, phase="QTMC", target="H", nt=4, nkd=1, nkz=1, intensity=4e14)
+def test_bulk_four_electrons(eng):
+    """Eight candidates (kd = +-0.2 at t = -T, -T/3, T/3, T; the field vanishes
+    at +-T): the bulk path keeps the FP64 path's four electrons and their weights."""
+    job = job_of(method="ADK", dim=2, phase="QTMC", target="H", nt=4, nkd=2, nkz=1, intensity=4e14)
     job.ss_kd_max = 0.2
     r64, s64, _ = eng.run(job)
     r32, s32, _ = eng.run(bulk(job))
-    assert r64.num_effective_traj == r32.num_effective_traj == 2
+    assert r64.num_effective_traj == r32.num_effective_traj == 4
     assert r32.ion_prob == pytest.approx(r64.ion_prob, rel=1e-5)
     assert s32.sum() == pytest.approx(s64.sum(), rel=1e-4)
 

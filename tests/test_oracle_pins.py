@@ -276,6 +276,10 @@ def test_validation_messages():
     bad.rate_prefix = 3
     st, msg = O.validate(bad)
     assert st == 1 and "conflict" in msg
+    bad = job.copy()
+    bad.ss_kd_num = 1
+    st, msg = O.validate(bad)
+    assert st == 1 and "endpoints differ" in msg
     with pytest.raises(ValueError):
         et.rate_prefix_bits(["Pre", "PreCC"])
     with pytest.raises(AssertionError):
