@@ -132,8 +132,23 @@ struct HostJob {
     std::vector<double> mol_clm, mol_wint;  // molecular target: copies of the caller's tables
 };
 
+// The sampler's name as the reference's messages carry it (ADKSampler.jl:79-102,
+// SPANESampler.jl:101-124, SPASampler.jl:79-102 share their checks).
+const char* sampler_tag(int method) {
+    switch (method) {
+        case ETRAJ_SAMPLER_SPANE: return "[SPANESampler]";
+        case ETRAJ_SAMPLER_SPA: return "[SPASampler]";
+        case ETRAJ_SAMPLER_WFAT: return "[WFATSampler]";
+        default: return "[ADKSampler]";
+    }
+}
+
 int validate_job(const etraj_job* job, std::string& err) {
-    auto fail = [&](const char* m) { err = m; return (int)ETRAJ_ERR_INVALID_ARGUMENT; };
+    auto fail = [&](const char* m) {
+        err = m;
+        if (job && err.compare(0, 12, "[ADKSampler]") == 0) err.replace(0, 12, sampler_tag(job->init_cond_method));
+        return (int)ETRAJ_ERR_INVALID_ARGUMENT;
+    };
     if (!job) return fail("job is NULL");
     if (!(job->sample_t_intv[0] < job->sample_t_intv[1]))
         return fail("[TrajectorySimulationJob] `sample_t_intv` must be a valid interval.");

@@ -21,6 +21,8 @@
  *                       binary tree over its 256 slots (absent slots +0.0),
  *                       so no chain of dependent additions exceeds 8.
  */
+#include <stdio.h>
+
 #include "oracle_internal.h"
 #include "oracle_sampler.h"
 
@@ -201,15 +203,25 @@ static int o_solve(const o_sys* S, double t0, double tf, const double* u0, doubl
 
 /* ---- validation (TrajectorySimulation.jl:178-186, ADKSampler.jl:43-105,
  *      HydrogenLikeAtom.jl:53-56, SAEAtom.jl:240-244, Cos4Laser.jl:57-58) ----------- */
+/* the sampler of the job being validated: its name replaces "[ADKSampler]" in the
+ * shared checks, as the reference's SPANE / SPA / WFAT samplers word them */
+static __thread int o_method = ETRAJ_SAMPLER_ADK;
+
 static int o_fail(char* msg, int len, const char* text) {
     if (msg && len > 0) {
-        strncpy(msg, text, (size_t)len - 1);
-        msg[len - 1] = 0;
+        const char* tag = (o_method == ETRAJ_SAMPLER_SPANE) ? "[SPANESampler]"
+                          : (o_method == ETRAJ_SAMPLER_SPA) ? "[SPASampler]"
+                          : (o_method == ETRAJ_SAMPLER_WFAT) ? "[WFATSampler]" : "[ADKSampler]";
+        if (strncmp(text, "[ADKSampler]", 12) == 0)
+            snprintf(msg, (size_t)len, "%s%s", tag, text + 12);
+        else
+            snprintf(msg, (size_t)len, "%s", text);
     }
     return ETRAJ_ERR_INVALID_ARGUMENT;
 }
 
 int oracle_validate(const etraj_job* job, char* msg, int len) {
+    o_method = job ? job->init_cond_method : ETRAJ_SAMPLER_ADK;
     if (msg && len > 0) msg[0] = 0;
     if (!(job->sample_t_intv[0] < job->sample_t_intv[1]))
         return o_fail(msg, len, "[TrajectorySimulationJob] `sample_t_intv` must be a valid interval.");

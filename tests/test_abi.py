@@ -79,6 +79,9 @@ def test_validate_without_gpu():
     bad = job.copy()
     bad.ss_kd_num = 0
     assert lib.etraj_validate(C.byref(bad), buf, 256) == abi.ERR_INVALID_ARGUMENT
+    bad.init_cond_method = abi.SAMPLER_SPANE  # the reference's message names the sampler
+    assert lib.etraj_validate(C.byref(bad), buf, 256) == abi.ERR_INVALID_ARGUMENT
+    assert buf.value.startswith(b"[SPANESampler] Invalid kd sample number")
     bad = job.copy()
     bad.ss_kd_num = 1  # Julia's range(-1.0, 1.0; length=1) throws: the endpoints differ
     assert lib.etraj_validate(C.byref(bad), buf, 256) == abi.ERR_INVALID_ARGUMENT

@@ -16,6 +16,7 @@ import pytest
 
 import _oracle as O
 import etraj_gb300 as et
+from etraj_gb300 import abi
 from _mol import hydrogen
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -280,6 +281,9 @@ def test_validation_messages():
     bad.ss_kd_num = 1
     st, msg = O.validate(bad)
     assert st == 1 and "endpoints differ" in msg
+    bad.ss_kd_num, bad.init_cond_method = 0, abi.SAMPLER_SPA
+    st, msg = O.validate(bad)
+    assert st == 1 and msg.startswith("[SPASampler] Invalid kd sample number")
     with pytest.raises(ValueError):
         et.rate_prefix_bits(["Pre", "PreCC"])
     with pytest.raises(AssertionError):
