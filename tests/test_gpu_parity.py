@@ -1,8 +1,8 @@
 """GPU parity of the FP64 path against the CPU oracle, through the C ABI.
 
-Bar (north star of this path): per-trajectory final momenta within 1e-9
-relative and the momentum distribution within 1e-10 relative L2 of the CPU
-path on the same sampled inputs.  The FP64 kernels use the same
+Bar of this path: per-trajectory final momenta within 1e-9 relative and the
+momentum distribution within 1e-10 relative L2 of the CPU path on the same
+sampled inputs.  The FP64 kernels use the same
 elementary-function implementation and operation order as the oracle, so
 these tests also assert bit-exact equality where the arithmetic is
 identical (sampled rows, final states, spectra).
@@ -135,7 +135,7 @@ def test_gpu_integrate_bit_exact(eng, dim, phase, target):
     assert np.array_equal(st, rst)
     assert np.array_equal(steps, rsteps)
     ok = rst == 0
-    # spec tolerance, then the stronger bit-exact claim
+    # the path's tolerance, then the stronger bit-exact claim
     np.testing.assert_allclose(fin[ok], rfin[ok], rtol=1e-9, atol=1e-12)
     assert same_bits(fin[ok], rfin[ok])
 
