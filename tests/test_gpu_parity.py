@@ -276,7 +276,7 @@ def test_gpu_budget_refusal():
     e.close()
 
 
-def test_gpu_config1_full_size(eng):
+def test_gpu_h_adk_3d_full_size(eng):
     """The plain-path workload at full size (hydrogen, Cos4 1e14 W/cm^2 800 nm 2 cycles,
     ADK 2000 t x 21 x 21 in 3D, CTMC, 500 x 500 px-py grid): same spectrum as the oracle."""
     T = period()
