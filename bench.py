@@ -334,19 +334,23 @@ def main():
     # buffer when the job is waited on, so every host<->device copy and that host
     # copy are inside the timed region.
     spec_host = [np.zeros(grid) for _ in range(4)]
-    for _ in range(args.warmup):
-        eng.run(job, want_spectrum=True)
+
+    def e2e_pass(steps):
+        inflight, effs_done = [], []
+        for i in range(steps):
+            res = abi.Result()
+            res.momentum_spec = abi.dptr(spec_host[i % 4])
+            inflight.append((eng.submit(job, res), res))
+            while inflight and (len(inflight) == 4 or i == steps - 1):
+                tk, r = inflight.pop(0)
+                eng.wait(tk, r)
+                effs_done.append(r.num_effective_traj)
+        return effs_done
+
+    e2e_pass(max(args.warmup, 4))  # the same pattern untimed: the pinned staging blocks exist
     sync_all()
     t_e2e = time.perf_counter()
-    inflight, e2e_effs = [], []
-    for i in range(args.steps):
-        res = abi.Result()
-        res.momentum_spec = abi.dptr(spec_host[i % 4])
-        inflight.append((eng.submit(job, res), res))
-        while inflight and (len(inflight) == 4 or i == args.steps - 1):
-            tk, r = inflight.pop(0)
-            eng.wait(tk, r)
-            e2e_effs.append(r.num_effective_traj)
+    e2e_effs = e2e_pass(args.steps)
     t_e2e = time.perf_counter() - t_e2e
     if world > 1:
         _, _, e2e_value = shards.aggregate_throughput(sum(e2e_effs), t_e2e)
