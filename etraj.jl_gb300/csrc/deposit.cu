@@ -125,26 +125,45 @@ k_scan_apply(uint32_t* __restrict__ a, int64_t n, const uint32_t* __restrict__ p
     }
 }
 
-// Stable scatter of one 8-bit digit.  Within a block the tile is processed in
-// kRounds rounds of kThreads consecutive keys; inside a round the rank of a
-// key among equal digits of lower index comes from __match_any_sync within
-// the warp and a per-digit prefix over warps.
+// Stable scatter of one 8-bit digit.  Warp w of a block owns the tile's keys
+// [w kSub, (w + 1) kSub): it first counts its digits (ranks within a round of
+// 32 keys come from __match_any_sync, and only the warp's leader lanes write
+// its row of counts), one prefix over the warps then turns the rows into each
+// warp's first position per digit (after the block's offset from the scan), and
+// the warp writes its keys in index order, advancing its own offsets.  Keys
+// land in index order within each digit, as a stable sort needs, with three
+// block barriers per tile.
+constexpr int kSub = kTile / kWarps;  // keys per warp and tile
 __global__ void __launch_bounds__(kThreads)
 k_radix_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
                 uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
                 const unsigned long long* __restrict__ count, int shift, int64_t nblocks,
                 const uint32_t* __restrict__ offs) {
-    __shared__ uint32_t base[256];
     __shared__ uint32_t wc[kWarps][256];
     const int64_t n = (int64_t)*count;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    base[threadIdx.x] = offs[(int64_t)threadIdx.x * nblocks + blockIdx.x];
+    const unsigned lt_mask = (1u << lane) - 1u;
     for (int w = 0; w < kWarps; ++w) wc[w][threadIdx.x] = 0u;
     __syncthreads();
-    const int64_t tile = (int64_t)blockIdx.x * kTile;
-    const unsigned lt_mask = (1u << lane) - 1u;
-    for (int r = 0; r < kRounds; ++r) {
-        const int64_t i = tile + (int64_t)r * kThreads + threadIdx.x;
+    const int64_t sub = (int64_t)blockIdx.x * kTile + (int64_t)warp * kSub;
+    for (int r = 0; r < kSub / 32; ++r) {
+        const int64_t i = sub + r * 32 + lane;
+        const uint32_t d = (i < n) ? (kin[i] >> shift) & 255u : 256u;
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        if (d < 256u && lane == __ffs(peers) - 1) wc[warp][d] += __popc(peers);
+    }
+    __syncthreads();
+    {
+        uint32_t run = offs[(int64_t)threadIdx.x * nblocks + blockIdx.x];
+        for (int w = 0; w < kWarps; ++w) {
+            const uint32_t c = wc[w][threadIdx.x];
+            wc[w][threadIdx.x] = run;
+            run += c;
+        }
+    }
+    __syncthreads();
+    for (int r = 0; r < kSub / 32; ++r) {
+        const int64_t i = sub + r * 32 + lane;
         const bool valid = i < n;
         uint32_t key = 0u, val = 0u, d = 256u;
         if (valid) {
@@ -153,25 +172,14 @@ k_radix_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ v
             d = (key >> shift) & 255u;
         }
         const unsigned peers = __match_any_sync(0xffffffffu, d);
-        const uint32_t rank = __popc(peers & lt_mask);
-        const int leader = __ffs(peers) - 1;
-        if (valid && lane == leader) wc[warp][d] = __popc(peers);
-        __syncthreads();
+        const uint32_t pos = valid ? wc[warp][d] + __popc(peers & lt_mask) : 0u;
+        __syncwarp();
+        if (valid && lane == __ffs(peers) - 1) wc[warp][d] += __popc(peers);
+        __syncwarp();
         if (valid) {
-            uint32_t before = 0u;
-            for (int w = 0; w < warp; ++w) before += wc[w][d];
-            const uint32_t pos = base[d] + before + rank;
             kout[pos] = key;
             vout[pos] = val;
         }
-        __syncthreads();
-        uint32_t tot = 0u;
-        for (int w = 0; w < kWarps; ++w) {
-            tot += wc[w][threadIdx.x];
-            wc[w][threadIdx.x] = 0u;
-        }
-        base[threadIdx.x] += tot;
-        __syncthreads();
     }
 }
 
