@@ -13,10 +13,10 @@
 // ion_prob_uncollected are 256-ary trees over trajectory order, each node
 // summed left to right from 0.0.
 //
-// Roofline: HBM bound.  Per trajectory and 8-bit pass: read 4 B key
-// (histogram), read 8 B + write 8 B (scatter); the per-bin pass reads 8 B
-// of the sorted pair plus 16 B of contribution and 8 + 16 B per bin;
-// passes = ceil(bits(grid+1)/8).
+// Roofline: HBM bound.  Per trajectory and pass: read 4 B key (histogram),
+// read 8 B + write 8 B (scatter); the per-bin pass reads 8 B of the sorted
+// pair plus 16 B of contribution and 8 + 16 B per bin; passes =
+// ceil(bits(grid+1)/9), each on at most 9 key bits.
 
 #include "engine.h"
 
@@ -27,21 +27,27 @@ constexpr int kThreads = 256;
 constexpr int kRounds = 16;
 constexpr int kTile = kThreads * kRounds;  // keys per block and pass
 constexpr int kWarps = kThreads / 32;
+constexpr int kMaxDigitBits = 9;           // a pass sorts on up to 9 key bits
+constexpr int kMaxDigits = 1 << kMaxDigitBits;
 
+// Digit counts of one tile for a pass over `bits` key bits from `shift`,
+// digit-major: hist[d nblocks + block].
 __global__ void __launch_bounds__(kThreads)
 k_radix_hist(const uint32_t* __restrict__ keys, const unsigned long long* __restrict__ count, int shift,
-             int64_t nblocks, uint32_t* __restrict__ hist) {
-    __shared__ uint32_t h[256];
+             int bits, int64_t nblocks, uint32_t* __restrict__ hist) {
+    __shared__ uint32_t h[kMaxDigits];
     const int64_t n = (int64_t)*count;
-    h[threadIdx.x] = 0u;
+    const int nd = 1 << bits;
+    const uint32_t mask = (uint32_t)nd - 1u;
+    for (int d = threadIdx.x; d < nd; d += kThreads) h[d] = 0u;
     __syncthreads();
     const int64_t base = (int64_t)blockIdx.x * kTile;
     for (int r = 0; r < kRounds; ++r) {
         int64_t i = base + (int64_t)r * kThreads + threadIdx.x;
-        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
+        if (i < n) atomicAdd(&h[(keys[i] >> shift) & mask], 1u);
     }
     __syncthreads();
-    hist[(int64_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+    for (int d = threadIdx.x; d < nd; d += kThreads) hist[(int64_t)d * nblocks + blockIdx.x] = h[d];
 }
 
 // ---- exclusive scan of a uint32 array (reduce, scan partials, scan) --------
@@ -125,7 +131,7 @@ k_scan_apply(uint32_t* __restrict__ a, int64_t n, const uint32_t* __restrict__ p
     }
 }
 
-// Stable scatter of one 8-bit digit.  Warp w of a block owns the tile's keys
+// Stable scatter of one digit (`bits` <= 9 key bits from `shift`).  Warp w of a block owns the tile's keys
 // [w kSub, (w + 1) kSub): it first counts its digits (ranks within a round of
 // 32 keys come from __match_any_sync, and only the warp's leader lanes write
 // its row of counts), one prefix over the warps then turns the rows into each
@@ -137,27 +143,29 @@ constexpr int kSub = kTile / kWarps;  // keys per warp and tile
 __global__ void __launch_bounds__(kThreads)
 k_radix_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
                 uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
-                const unsigned long long* __restrict__ count, int shift, int64_t nblocks,
+                const unsigned long long* __restrict__ count, int shift, int bits, int64_t nblocks,
                 const uint32_t* __restrict__ offs) {
-    __shared__ uint32_t wc[kWarps][256];
+    __shared__ uint32_t wc[kWarps][kMaxDigits];
     const int64_t n = (int64_t)*count;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned lt_mask = (1u << lane) - 1u;
-    for (int w = 0; w < kWarps; ++w) wc[w][threadIdx.x] = 0u;
+    const uint32_t nd = 1u << bits, mask = nd - 1u;
+    for (uint32_t d = threadIdx.x; d < nd; d += kThreads)
+        for (int w = 0; w < kWarps; ++w) wc[w][d] = 0u;
     __syncthreads();
     const int64_t sub = (int64_t)blockIdx.x * kTile + (int64_t)warp * kSub;
     for (int r = 0; r < kSub / 32; ++r) {
         const int64_t i = sub + r * 32 + lane;
-        const uint32_t d = (i < n) ? (kin[i] >> shift) & 255u : 256u;
+        const uint32_t d = (i < n) ? (kin[i] >> shift) & mask : nd;
         const unsigned peers = __match_any_sync(0xffffffffu, d);
-        if (d < 256u && lane == __ffs(peers) - 1) wc[warp][d] += __popc(peers);
+        if (d < nd && lane == __ffs(peers) - 1) wc[warp][d] += __popc(peers);
     }
     __syncthreads();
-    {
-        uint32_t run = offs[(int64_t)threadIdx.x * nblocks + blockIdx.x];
+    for (uint32_t d = threadIdx.x; d < nd; d += kThreads) {
+        uint32_t run = offs[(int64_t)d * nblocks + blockIdx.x];
         for (int w = 0; w < kWarps; ++w) {
-            const uint32_t c = wc[w][threadIdx.x];
-            wc[w][threadIdx.x] = run;
+            const uint32_t c = wc[w][d];
+            wc[w][d] = run;
             run += c;
         }
     }
@@ -165,11 +173,11 @@ k_radix_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ v
     for (int r = 0; r < kSub / 32; ++r) {
         const int64_t i = sub + r * 32 + lane;
         const bool valid = i < n;
-        uint32_t key = 0u, val = 0u, d = 256u;
+        uint32_t key = 0u, val = 0u, d = nd;
         if (valid) {
             key = kin[i];
             val = vin ? vin[i] : (uint32_t)i;
-            d = (key >> shift) & 255u;
+            d = (key >> shift) & mask;
         }
         const unsigned peers = __match_any_sync(0xffffffffu, d);
         const uint32_t pos = valid ? wc[warp][d] + __popc(peers & lt_mask) : 0u;
@@ -359,11 +367,46 @@ int key_bits(int64_t grid) {
     return b;
 }
 
+// Stable LSD radix sort of (key, index) pairs on the low `bits` key bits, in as
+// few passes of at most kMaxDigitBits as cover them (20 bits: 7 + 7 + 6; 25:
+// 9 + 8 + 8).  Wider digits would save the 20-bit case a pass, but two
+// 1024-digit passes measured slower than three narrow ones (larger histogram
+// scans, writes spread over more runs).  The order is the same for any split: by key, then by index.  The
+// sorted pairs are left in the buffers *kout, *vout point to.
+int radix_sort(const uint32_t* keys, const unsigned long long* count, int64_t max_n, int bits,
+               uint32_t* const kbuf[2], uint32_t* const vbuf[2], uint32_t* hist, uint32_t* scan_tmp,
+               const uint32_t** kout, const uint32_t** vout, cudaStream_t s) {
+    const int64_t nb = tiles_for(max_n);
+    const int npass = (bits + kMaxDigitBits - 1) / kMaxDigitBits;
+    const uint32_t* kin = keys;
+    const uint32_t* vin = nullptr;
+    int which = 0, launches = 0;
+    for (int p = 0, shift = 0; p < npass; ++p) {
+        const int w = bits / npass + ((p < bits % npass) ? 1 : 0);
+        const int64_t hist_n = ((int64_t)1 << w) * nb;
+        const int64_t parts = scan_parts_for(hist_n);
+        k_radix_hist<<<(unsigned)nb, kThreads, 0, s>>>(kin, count, shift, w, nb, hist);
+        k_scan_reduce<<<(unsigned)parts, kScanThreads, 0, s>>>(hist, hist_n, scan_tmp);
+        k_scan_partials<<<1, kScanThreads, 0, s>>>(scan_tmp, parts);
+        k_scan_apply<<<(unsigned)parts, kScanThreads, 0, s>>>(hist, hist_n, scan_tmp);
+        k_radix_scatter<<<(unsigned)nb, kThreads, 0, s>>>(kin, vin, kbuf[which], vbuf[which], count, shift, w, nb,
+                                                           hist);
+        launches += 5;
+        kin = kbuf[which];
+        vin = vbuf[which];
+        which ^= 1;
+        shift += w;
+    }
+    *kout = kin;
+    *vout = vin;
+    return launches;
+}
+
 }  // namespace
 
 size_t deposit_scratch_bytes(int64_t max_n) {
     int64_t nb = tiles_for(max_n > 0 ? max_n : 1);
-    int64_t hist = 256 * nb;
+    int64_t hist = (int64_t)kMaxDigits * nb;
     size_t bytes = 0;
     bytes += 4 * (size_t)max_n * sizeof(uint32_t) + 4 * 256;  // keys a/b, vals a/b
     bytes += (size_t)hist * sizeof(uint32_t) + 256;
@@ -377,7 +420,7 @@ void deposit_scratch_carve(void* base, int64_t max_n, DepositScratch* d) {
     char* p = (char*)base;
     size_t off = 0;
     int64_t nb = tiles_for(max_n > 0 ? max_n : 1);
-    int64_t hist = 256 * nb;
+    int64_t hist = (int64_t)kMaxDigits * nb;
     d->keys_a = (uint32_t*)(p + off); off = align(off + (size_t)max_n * 4);
     d->keys_b = (uint32_t*)(p + off); off = align(off + (size_t)max_n * 4);
     d->vals_a = (uint32_t*)(p + off); off = align(off + (size_t)max_n * 4);
@@ -400,27 +443,10 @@ int launch_deposit(const DJob& J, const TrajOut& out, const unsigned long long* 
     cudaMemsetAsync(counters, 0, sizeof(Counters), s);
     if (max_n > 0) {
         // stable LSD radix sort of (key, survivor index); keys are in [0, grid]
-        const int64_t nb = tiles_for(max_n);
-        const int64_t hist_n = 256 * nb;
-        const int64_t parts = scan_parts_for(hist_n);
-        const int bits = key_bits(grid);
-        const uint32_t* kin = out.key;
-        const uint32_t* vin = nullptr;
         uint32_t* kbuf[2] = {d.keys_a, d.keys_b};
         uint32_t* vbuf[2] = {d.vals_a, d.vals_b};
-        int which = 0;
-        for (int shift = 0; shift < bits; shift += 8) {
-            k_radix_hist<<<(unsigned)nb, kThreads, 0, s>>>(kin, count, shift, nb, d.hist);
-            k_scan_reduce<<<(unsigned)parts, kScanThreads, 0, s>>>(d.hist, hist_n, d.scan_tmp);
-            k_scan_partials<<<1, kScanThreads, 0, s>>>(d.scan_tmp, parts);
-            k_scan_apply<<<(unsigned)parts, kScanThreads, 0, s>>>(d.hist, hist_n, d.scan_tmp);
-            k_radix_scatter<<<(unsigned)nb, kThreads, 0, s>>>(kin, vin, kbuf[which], vbuf[which], count,
-                                                               shift, nb, d.hist);
-            launches += 5;
-            kin = kbuf[which];
-            vin = vbuf[which];
-            which ^= 1;
-        }
+        const uint32_t *kin = nullptr, *vin = nullptr;
+        launches += radix_sort(out.key, count, max_n, key_bits(grid), kbuf, vbuf, d.hist, d.scan_tmp, &kin, &vin, s);
         launches += launch_bin_sums(kin, vin, count, max_n, grid, out.c_re, out.c_im, coherent, spec_re,
                                     spec_im, s);
         // canonical 256-ary trees for ion_prob and ion_prob_uncollected
@@ -662,7 +688,7 @@ namespace {
 
 constexpr int64_t kNoallocMaxN = (int64_t)1 << 19;
 constexpr int64_t kNoallocTiles = (kNoallocMaxN + kTile - 1) / kTile;
-constexpr int64_t kNoallocHist = 256 * kNoallocTiles;
+constexpr int64_t kNoallocHist = (int64_t)kMaxDigits * kNoallocTiles;
 constexpr int64_t kNoallocParts = (kNoallocHist + kScanChunk - 1) / kScanChunk;
 // layout: keys_a | keys_b | vals_a | vals_b | hist | scan partials | count
 constexpr size_t kNoallocOffHist = (size_t)4 * kNoallocMaxN * sizeof(uint32_t);
@@ -731,24 +757,8 @@ extern "C" int etraj_deposit_noalloc(int64_t n, const uint32_t* key, const doubl
     if (coherent) cudaMemsetAsync(spec_im, 0, (size_t)grid * sizeof(double), s);
     k_set_count<<<1, 1, 0, s>>>(count, (unsigned long long)n);
     if (n > 0) {
-        const int64_t nb = tiles_for(n);
-        const int64_t hist_n = 256 * nb;
-        const int64_t np = scan_parts_for(hist_n);
-        const int bits = key_bits(grid);
-        const uint32_t* kin = key;
-        const uint32_t* vin = nullptr;
-        int which = 0;
-        for (int shift = 0; shift < bits; shift += 8) {
-            k_radix_hist<<<(unsigned)nb, kThreads, 0, s>>>(kin, count, shift, nb, hist);
-            k_scan_reduce<<<(unsigned)np, kScanThreads, 0, s>>>(hist, hist_n, parts);
-            k_scan_partials<<<1, kScanThreads, 0, s>>>(parts, np);
-            k_scan_apply<<<(unsigned)np, kScanThreads, 0, s>>>(hist, hist_n, parts);
-            k_radix_scatter<<<(unsigned)nb, kThreads, 0, s>>>(kin, vin, kbuf[which], vbuf[which], count,
-                                                               shift, nb, hist);
-            kin = kbuf[which];
-            vin = vbuf[which];
-            which ^= 1;
-        }
+        const uint32_t *kin = nullptr, *vin = nullptr;
+        radix_sort(key, count, n, key_bits(grid), kbuf, vbuf, hist, parts, &kin, &vin, s);
         launch_bin_sums(kin, vin, count, n, grid, c_re, c_im, coherent, spec_re, spec_im, s);
     }
     int fblocks = (int)((grid + 255) / 256);
