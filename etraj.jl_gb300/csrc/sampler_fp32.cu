@@ -282,10 +282,17 @@ __device__ __noinline__ float spa32_solve(const SpaBase32& S, float kd, float kz
         const float rp = J * p + r;
         const float rho = (r * r - fn * fn) / (r * r - rp * rp);
         if (rho > eta) {
+            const float rold = r;
             r = fn;
             converged = (fabsf(x - xold) <= 0.0f) || (fabsf(r) <= ftol);
             if (converged) break;
-            J = spa32_dspe(S, x, kd, kz, Ip);
+            // a cold solve takes the secant through its last two iterates as the
+            // derivative, which costs no evaluation; a step too short for FP32 to
+            // resolve the difference, and the warm solves' one step, take the
+            // central difference
+            const float dx = x - xold;
+            if (!warm && fabsf(dx) > 1e-3f * fmaxf(fabsf(x), 1.0f)) J = (fn - rold) / dx;
+            else J = spa32_dspe(S, x, kd, kz, Ip);
             d = fmaxf(0.1f * d, fabsf(J));
         } else {
             x = x - p;
