@@ -97,10 +97,11 @@ __device__ cf sph_sum(int l, int m, cf x, cf y, cf z) {
 // phases at t_r (up to ~1e3 rad) are therefore reduced once in FP64, and
 // A(t_r + i tau), F(t_r + i tau) follow in FP32 from cosh/sinh of the
 // imaginary parts.  The solve and the quadratures are the algorithms of spa.h
-// (NLsolve's trust-region dogleg with a central-difference derivative;
-// QuadGK's adaptive Gauss-Kronrod (7,15) with an interval heap) at FP32's
-// tolerances: ftol 1e-5 on the saddle-point residual, derivative step
-// cbrt(eps(Float32)), quadrature rtol sqrt(eps(Float32)), which is the
+// (NLsolve's trust-region dogleg with a central-difference derivative, which
+// a cold solve replaces by the secant of its last two iterates after an
+// accepted step; QuadGK's adaptive Gauss-Kronrod (7,15) with an interval heap)
+// at FP32's tolerances: ftol 1e-5 on the saddle-point residual, derivative
+// step cbrt(eps(Float32)), quadrature rtol sqrt(eps(Float32)), which is the
 // tolerance QuadGK picks for Float32 integrands.
 enum { Q_IM_AX = 0, Q_IM_AY = 1, Q_ACTION = 2, Q_IM_AXY = 3 };
 constexpr int kSegs32 = 48;  // interval budget of one quadrature
