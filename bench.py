@@ -261,9 +261,9 @@ def main():
     import torch.distributed as dist
 
     rank, world, local = rank_env()
+    torch.cuda.set_device(local)  # before the process group, so NCCL binds this rank's GPU
     if world > 1:
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     eng = et.Engine(device=local)
     stream = torch.cuda.Stream(device=dev)
