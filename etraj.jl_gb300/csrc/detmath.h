@@ -372,12 +372,17 @@ DM_FN dm_cplx dm_cpowi(dm_cplx z, int n) {
 }
 /* sin and cos of one complex argument from one sincos and one sinh/cosh
  * (the same values as dm_csin and dm_ccos) */
-DM_FN void dm_csincos(dm_cplx a, dm_cplx* sn, dm_cplx* cs) {
-    double s, c, sh, ch;
-    dm_sincos(a.re, &s, &c);
-    dm_sinhcosh(a.im, &sh, &ch);
+/* sin and cos of a + i im from s = sin(a), c = cos(a) */
+DM_FN void dm_csincos_re(double s, double c, double im, dm_cplx* sn, dm_cplx* cs) {
+    double sh, ch;
+    dm_sinhcosh(im, &sh, &ch);
     *sn = dm_c(s * ch, c * sh);
     *cs = dm_c(c * ch, -(s * sh));
+}
+DM_FN void dm_csincos(dm_cplx a, dm_cplx* sn, dm_cplx* cs) {
+    double s, c;
+    dm_sincos(a.re, &s, &c);
+    dm_csincos_re(s, c, a.im, sn, cs);
 }
 /* cos and sin of a complex argument */
 DM_FN dm_cplx dm_ccos(dm_cplx a) {

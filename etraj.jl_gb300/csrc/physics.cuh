@@ -113,12 +113,16 @@ __host__ __device__ __forceinline__ void laser_A(const DLaser& L, double t, doub
 // A and (optionally) F at complex time t_r + i t_i, as SPASampler.jl evaluates
 // them; the tanh windows take real(t) (Cos4Laser.jl:93), so callers that hold
 // Re t fixed pass them precomputed in `win` (w1, w2), or nullptr.
+// doubles per laser in the `win` cache of the complex-time evaluations (laser_windows)
+constexpr int kWinPerMono = 6;
+
 __host__ __device__ __forceinline__ void mono_AF_complex(const DMono& L, dm_cplx t, dm_cplx& Ax, dm_cplx& Ay,
                                                          dm_cplx* Fx, dm_cplx* Fy, const double* win = nullptr) {
     const dm_cplx tt = dm_c(t.re - L.t_shift, t.im);
     const dm_cplx th = dm_caddr(dm_cscale(tt, L.omega), L.cep);
     dm_cplx sth, cth;
-    dm_csincos(th, &sth, &cth);
+    if (win) dm_csincos_re(win[2], win[3], th.im, &sth, &cth);
+    else dm_csincos(th, &sth, &cth);
     dm_cplx preA, preF, cx, cy;
     if (L.kind == ETRAJ_LASER_GAUSSIAN) {
         const dm_cplx g = dm_cexp(dm_cscale(dm_cneg(dm_cmul(tt, tt)), L.inv_2s2));
@@ -131,7 +135,8 @@ __host__ __device__ __forceinline__ void mono_AF_complex(const DMono& L, dm_cplx
         double w1, w2;
         const dm_cplx u = dm_cscale(tt, L.w2n);
         dm_cplx s, c;
-        dm_csincos(u, &s, &c);
+        if (win) dm_csincos_re(win[4], win[5], u.im, &s, &c);
+        else dm_csincos(u, &s, &c);
         if (win) {
             w1 = win[0];
             w2 = win[1];
@@ -172,7 +177,7 @@ __host__ __device__ __forceinline__ void laser_AF_complex(const DLaser& L, dm_cp
     if (L.nmono == 2) {
         dm_cplx ax2, ay2, fx2, fy2;
         mono_AF_complex(L.m[1], dm_c(t.re - L.delay, t.im), ax2, ay2, Fx ? &fx2 : nullptr, Fx ? &fy2 : nullptr,
-                        win ? win + 2 : nullptr);
+                        win ? win + kWinPerMono : nullptr);
         Ax = dm_cadd(Ax, ax2);
         Ay = dm_cadd(Ay, ay2);
         if (Fx) {
@@ -182,10 +187,19 @@ __host__ __device__ __forceinline__ void laser_AF_complex(const DLaser& L, dm_cp
     }
 }
 
-// window factors (w1, w2) of each laser at real time tre
+// What a complex-time evaluation at Re t = tre needs of each laser that depends
+// on tre only, computed with the expressions mono_AF_complex uses, so a cache
+// of them keyed by tre changes no bit: the window factors (w1, w2), then sin
+// and cos of Re(theta) (carrier) and of Re(u) (envelope).
 __host__ __device__ __forceinline__ void laser_windows(const DLaser& L, double tre, double* win) {
-    window(L.m[0], tre - L.m[0].t_shift, win[0], win[1]);
-    if (L.nmono == 2) window(L.m[1], (tre - L.delay) - L.m[1].t_shift, win[2], win[3]);
+    for (int k = 0; k < L.nmono; ++k) {
+        const DMono& M = L.m[k];
+        double* w = win + kWinPerMono * k;
+        const double ttre = ((k == 0) ? tre : tre - L.delay) - M.t_shift;
+        window(M, ttre, w[0], w[1]);
+        dm_sincos(ttre * M.omega + M.cep, &w[2], &w[3]);
+        if (M.kind != ETRAJ_LASER_GAUSSIAN) dm_sincos(ttre * M.w2n, &w[4], &w[5]);
+    }
 }
 
 __host__ __device__ __forceinline__ void laser_A_complex(const DLaser& L, dm_cplx t, const double* win, dm_cplx* Ax,

@@ -28,13 +28,15 @@
  *
  * The including file defines
  *   SPA_LASER_T                       the laser description type,
- *   SPA_WIN(L, tre, w)                the tanh window factors of its lasers
- *                                     at real time tre (double w[4]), and
+ *   SPA_WIN(L, tre, w)                what A at complex time needs of its
+ *                                     real part tre alone (the tanh window
+ *                                     factors, and whatever else the includer
+ *                                     caches; double w[12] at most), and
  *   SPA_AW(L, t, w, ax, ay)           A_x, A_y at complex time t (dm_cplx*)
- *                                     with the window factors w at Re t.
+ *                                     from those values w at Re t.
  * Re t is the same for all but a few evaluations of one electron (every
- * quadrature node and every iterate of a solve share t_r), so the window
- * factors are cached per thread in a spa_win keyed by Re t.
+ * quadrature node and every iterate of a solve share t_r), so those values
+ * are cached per thread in a spa_win keyed by Re t.
  */
 #ifndef ETRAJ_SPA_H
 #define ETRAJ_SPA_H
@@ -54,7 +56,7 @@
 
 typedef struct {
     double key; /* Re t of w[] (NaN: empty) */
-    double w[4];
+    double w[12]; /* what the including file caches per Re t (SPA_WIN), at most 6 per laser */
 } spa_win;
 
 DM_FN void spa_win_init(spa_win* W) { W->key = dm_u2d(0x7ff8000000000000ull); }
