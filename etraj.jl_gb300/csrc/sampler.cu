@@ -212,6 +212,30 @@ __global__ void __launch_bounds__(128) k_mol_prepare(const __grid_constant__ DJo
     }
 }
 
+// Coefficients (-1)^k / (2^(2k+m) (k+m)! k! (l-m-2k)!) of the k-sum below for
+// l <= kMaxL, k = max(0, -m) + j (j < 3), rounded at compile time: every factor
+// and product is an exact integer, so the one rounding is the correctly
+// rounded division the loop used to do per candidate.
+struct SphCoef64 {
+    double c[kMaxL + 1][2 * kMaxL + 1][3];
+};
+constexpr double sph_fact64(int n) { return n <= 1 ? 1.0 : (double)n * sph_fact64(n - 1); }
+constexpr SphCoef64 sph_coef64_table() {
+    SphCoef64 t{};
+    for (int l = 0; l <= kMaxL; ++l)
+        for (int m = -l; m <= l; ++m) {
+            const int kmin = (m < 0) ? -m : 0, kmax = (l - m) / 2;
+            for (int k = kmin; k <= kmax && k - kmin < 3; ++k) {
+                double p2 = 1.0;
+                for (int i = 0; i < 2 * k + m; ++i) p2 *= 2.0;
+                t.c[l][m + l][k - kmin] =
+                    ((k & 1) ? -1.0 : 1.0) / (p2 * (sph_fact64(k + m) * sph_fact64(k) * sph_fact64(l - m - 2 * k)));
+            }
+        }
+    return t;
+}
+__constant__ SphCoef64 kSph64 = sph_coef64_table();
+
 // The k-sum of the solid harmonic (shared_methods.jl:21).
 __device__ dm_cplx sph_sum(int l, int m, dm_cplx x, dm_cplx y, dm_cplx z) {
     dm_cplx xp = dm_c(x.re - y.im, x.im + y.re);
@@ -219,10 +243,7 @@ __device__ dm_cplx sph_sum(int l, int m, dm_cplx x, dm_cplx y, dm_cplx z) {
     int kmin = (m < 0) ? -m : 0, kmax = (l - m) / 2;
     dm_cplx acc = dm_c(0.0, 0.0);
     for (int k = kmin; k <= kmax; ++k) {
-        double den = fact(k + m) * fact(k) * fact(l - m - 2 * k);
-        double p2 = 1.0;
-        for (int i = 0; i < 2 * k + m; ++i) p2 *= 2.0;
-        double coef = ((k & 1) ? -1.0 : 1.0) / (p2 * den);
+        const double coef = kSph64.c[l][m + l][k - kmin];
         dm_cplx tt = dm_cscale(dm_cpowi(xp, k + m), coef);
         tt = dm_cmul(tt, dm_cpowi(xm, k));
         tt = dm_cmul(tt, dm_cpowi(z, l - m - 2 * k));
