@@ -15,16 +15,16 @@ import etraj_gb300 as et
 from etraj_gb300 import shards
 
 
-def _job(mc=False, phase="QTMC", nt=12, cutoff=0.0):
+def _job(mc=False, phase="QTMC", nt=12, cutoff=0.0, dim=2):
     T = 2 * math.pi / (45.563352525 / 800.0)
     kw = dict(init_cond_method="ADK", laser=et.Cos4Laser(peak_int=1e14, wave_len=800.0, cyc_num=2, ellip=0.0),
-              target=et.get_atom("H"), dimension=2, sample_t_intv=(-T, T), sample_t_num=nt,
-              traj_t_final=2 * T, final_p_max=(1.5, 1.5), final_p_num=(48, 48), traj_phase_method=phase,
+              target=et.get_atom("H"), dimension=dim, sample_t_intv=(-T, T), sample_t_num=nt,
+              traj_t_final=2 * T, final_p_max=(1.5,) * dim, final_p_num=(48, 48, 8)[:dim], traj_phase_method=phase,
               sample_cutoff_limit=cutoff, seed=5)
     if mc:
-        kw.update(sample_monte_carlo=True, mc_kt_num=40, mc_kd_max=1.0, mc_kz_max=0.0)
+        kw.update(sample_monte_carlo=True, mc_kt_num=40, mc_kd_max=1.0, mc_kz_max=1.0 if dim == 3 else 0.0)
     else:
-        kw.update(ss_kd_max=1.0, ss_kd_num=15, ss_kz_max=0.0, ss_kz_num=0)
+        kw.update(ss_kd_max=1.0, ss_kd_num=15, ss_kz_max=1.0 if dim == 3 else 0.0, ss_kz_num=5 if dim == 3 else 0)
     return et.make_job(**kw)
 
 
@@ -60,12 +60,12 @@ class _Res:
         self.num_effective_traj = int(sc["num_effective"])
 
 
-@pytest.mark.parametrize("phase", ["CTMC", "QTMC"])
-def test_grid_shards_merge_to_the_whole_job(phase):
+@pytest.mark.parametrize("phase,dim", [("CTMC", 2), ("QTMC", 2), ("SCTS", 3)])
+def test_grid_shards_merge_to_the_whole_job(phase, dim):
     """Two grid shards, each weighted by its step(t), sum to the whole job's
     spectrum, probabilities and trajectory count (the shards' time samples
     agree with the whole job's to rounding)."""
-    job = _job(phase=phase)
+    job = _job(phase=phase, dim=dim)
     coherent = shards.is_coherent(job)
     spec, amp, sc = O.run(job)
     vec, tot = 0.0, 0.0
