@@ -10,8 +10,8 @@ rtol 1e-6; coherent 1000 x 1000 momentum grid spanning +-2 a.u.
 A step is one whole job: sampling, integration, collection and the
 deterministic deposit.  `value` is effective trajectories per second of the
 FP32-bulk path with all buffers resident on the device; `e2e` is the same
-metric through etraj_run with host output buffers (spectrum copied back every
-step).  The FP64 plain path is run on the same job for the speed ratio and
+metric through the C ABI's etraj_submit / etraj_wait with host output buffers
+(time samples copied in and the spectrum copied back every step).  The FP64 plain path is run on the same job for the speed ratio and
 the PMD error (relative L2 of |A|^2 against the FP64 result).
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
@@ -103,7 +103,7 @@ WORKLOADS = {
 FLOPS_PER_STEP_SAE_2D_SCTS = 702
 # DRAM bytes (read + write) of the integrator's round-0 launch per electron on this
 # workload, from one ncu capture of a 2e6-candidate case (24.91 MB for 8.17e5
-# electrons); traffic grows with the electrons (profiles/launches_spane_ar_scts_1e7.md).
+# electrons); traffic grows with the electrons.
 INTEGRATOR_DRAM_BYTES_PER_ELECTRON = 30.48
 
 

@@ -678,8 +678,10 @@ int launch_weighted_sum(const double* mspec, int n_inst, int64_t grid, const dou
 // of (bin, electron), per-bin sums in electron order, |A|^2) on caller-owned
 // inputs and outputs, with its sort scratch in one fixed device array declared
 // below.  The array's size is fixed at build time (kNoallocMaxN contributions,
-// about 8 MiB) and every GPU that loads this library holds it until the
-// process exits.
+// about 10 MiB) and every GPU that loads this library holds it until the
+// process exits.  Keys above the grid are taken as the grid ("not deposited")
+// before the sort, so a bad key can neither alias a bin nor leave the sort's
+// key range.
 
 #include <mutex>
 
@@ -690,8 +692,8 @@ constexpr int64_t kNoallocMaxN = (int64_t)1 << 19;
 constexpr int64_t kNoallocTiles = (kNoallocMaxN + kTile - 1) / kTile;
 constexpr int64_t kNoallocHist = (int64_t)kMaxDigits * kNoallocTiles;
 constexpr int64_t kNoallocParts = (kNoallocHist + kScanChunk - 1) / kScanChunk;
-// layout: keys_a | keys_b | vals_a | vals_b | hist | scan partials | count
-constexpr size_t kNoallocOffHist = (size_t)4 * kNoallocMaxN * sizeof(uint32_t);
+// layout: clamped keys | keys_a | keys_b | vals_a | vals_b | hist | scan partials | count
+constexpr size_t kNoallocOffHist = (size_t)5 * kNoallocMaxN * sizeof(uint32_t);
 constexpr size_t kNoallocOffParts = kNoallocOffHist + (size_t)kNoallocHist * sizeof(uint32_t);
 constexpr size_t kNoallocOffCount = (kNoallocOffParts + (size_t)(kNoallocParts + 64) * sizeof(uint32_t) + 255) & ~(size_t)255;
 constexpr size_t kNoallocBytes = kNoallocOffCount + 256;
@@ -699,8 +701,18 @@ constexpr size_t kNoallocBytes = kNoallocOffCount + 256;
 constexpr int kMaxDevices = 64;
 std::mutex g_noalloc_mu;
 void* g_noalloc_ptr[kMaxDevices] = {};
+int g_noalloc_sms[kMaxDevices] = {};
 
 __global__ void k_set_count(unsigned long long* c, unsigned long long n) { *c = n; }
+
+// The caller's keys with every key above the grid replaced by the grid, the
+// "not deposited" key: the sort then sees only keys in [0, grid].
+__global__ void k_clamp_keys(const uint32_t* __restrict__ in, int64_t n, uint32_t grid, uint32_t* __restrict__ out) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t k = in[i];
+        out[i] = k > grid ? grid : k;
+    }
+}
 
 }  // namespace
 }  // namespace etraj
@@ -712,8 +724,9 @@ namespace {
 
 // Device address of g_noalloc_scratch on the current device.  The symbol's
 // host-side name is only a stand-in, so the address is looked up once per
-// device with that device current (cudaGetSymbolAddress) and cached.
-int noalloc_scratch(void** out) {
+// device with that device current (cudaGetSymbolAddress) and cached, with the
+// device's SM count (grid sizes).
+int noalloc_scratch(void** out, int* sms) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return ETRAJ_ERR_CUDA;
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
@@ -724,9 +737,16 @@ int noalloc_scratch(void** out) {
             cudaGetLastError();
             return ETRAJ_ERR_CUDA;
         }
+        int nsm = 0;
+        if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm < 1) {
+            cudaGetLastError();
+            return ETRAJ_ERR_CUDA;
+        }
+        g_noalloc_sms[dev] = nsm;
         g_noalloc_ptr[dev] = p;
     }
     *out = g_noalloc_ptr[dev];
+    *sms = g_noalloc_sms[dev];
     return ETRAJ_OK;
 }
 
@@ -742,12 +762,14 @@ extern "C" int etraj_deposit_noalloc(int64_t n, const uint32_t* key, const doubl
     if (!spec_re || !momentum_spec || (coherent && !spec_im)) return ETRAJ_ERR_INVALID_ARGUMENT;
     if (n > 0 && (!key || !c_re || (coherent && !c_im))) return ETRAJ_ERR_INVALID_ARGUMENT;
     void* base = nullptr;
-    int st = noalloc_scratch(&base);
+    int sms = 0;
+    int st = noalloc_scratch(&base, &sms);
     if (st != ETRAJ_OK) return st;
     cudaStream_t s = (cudaStream_t)cuda_stream;
     unsigned char* p = (unsigned char*)base;
-    uint32_t* kbuf[2] = {(uint32_t*)p, (uint32_t*)p + kNoallocMaxN};
-    uint32_t* vbuf[2] = {(uint32_t*)p + 2 * kNoallocMaxN, (uint32_t*)p + 3 * kNoallocMaxN};
+    uint32_t* kclamp = (uint32_t*)p;
+    uint32_t* kbuf[2] = {(uint32_t*)p + kNoallocMaxN, (uint32_t*)p + 2 * kNoallocMaxN};
+    uint32_t* vbuf[2] = {(uint32_t*)p + 3 * kNoallocMaxN, (uint32_t*)p + 4 * kNoallocMaxN};
     uint32_t* hist = (uint32_t*)(p + kNoallocOffHist);
     uint32_t* parts = (uint32_t*)(p + kNoallocOffParts);
     unsigned long long* count = (unsigned long long*)(p + kNoallocOffCount);
@@ -758,11 +780,14 @@ extern "C" int etraj_deposit_noalloc(int64_t n, const uint32_t* key, const doubl
     k_set_count<<<1, 1, 0, s>>>(count, (unsigned long long)n);
     if (n > 0) {
         const uint32_t *kin = nullptr, *vin = nullptr;
-        radix_sort(key, count, n, key_bits(grid), kbuf, vbuf, hist, parts, &kin, &vin, s);
+        int cblocks = (int)((n + 255) / 256);
+        if (cblocks > sms * 8) cblocks = sms * 8;
+        k_clamp_keys<<<cblocks, 256, 0, s>>>(key, n, (uint32_t)grid, kclamp);
+        radix_sort(kclamp, count, n, key_bits(grid), kbuf, vbuf, hist, parts, &kin, &vin, s);
         launch_bin_sums(kin, vin, count, n, grid, c_re, c_im, coherent, spec_re, spec_im, s);
     }
     int fblocks = (int)((grid + 255) / 256);
-    if (fblocks > 152 * 16) fblocks = 152 * 16;
+    if (fblocks > sms * 16) fblocks = sms * 16;
     k_finalize_spec<<<fblocks, 256, 0, s>>>(spec_re, spec_im, grid, coherent, momentum_spec);
     return (cudaGetLastError() == cudaSuccess) ? ETRAJ_OK : ETRAJ_ERR_CUDA;
 }

@@ -133,7 +133,7 @@ __device__ __forceinline__ void field(const float4* __restrict__ tab, int n_int,
 }
 
 // Momentum derivatives K = F_target(X) - F_laser(t) and the phase rate
-// (HydrogenLikeAtom.jl:78-159, SAEAtom.jl:278-366); x . F_target = coef r^2.
+// (HydrogenLikeAtom.jl:78-159, SAEAtom.jl:98-186); x . F_target = coef r^2.
 // mK and mph are the magnitudes of the terms summed into K and the phase rate
 // (for the rounding-noise bound of the error estimate; unused outputs of the
 // inlined call are removed by the compiler).
@@ -175,7 +175,7 @@ __device__ __forceinline__ void accel(const BulkParams& P, const float4* __restr
             num = fmaf(P.a3, e3, fmaf(P.a2 * r, e2, fmaf(P.a1, e1, P.Z)));
         }
         if (PHASE != ETRAJ_PHASE_CTMC) {
-            // the 2D SCTS reference divides by r^2+sc, not its square root (SAEAtom.jl:316)
+            // the 2D SCTS reference divides by r^2+sc, not its square root (SAEAtom.jl:136)
             V = (DIM == 2 && PHASE == ETRAJ_PHASE_SCTS) ? num * (ris * ris) : num * ris;
         }
     }

@@ -3,7 +3,7 @@
 //
 // Reference: src/Lasers/Cos4Laser.jl:89-152, Cos2Laser.jl:89-152,
 // GaussianLaser.jl:97-160, BichromaticLaser.jl:59-85;
-// src/Targets/HydrogenLikeAtom.jl:75-159, SAEAtom.jl:264-366.
+// src/Targets/HydrogenLikeAtom.jl:75-159, SAEAtom.jl:84-186.
 //
 // Every expression keeps the reference's left-to-right association and uses
 // detmath for transcendentals, so with --fmad=false the results are
@@ -294,7 +294,7 @@ __host__ __device__ __forceinline__ double sae_exp(const DTarget& T, double b, d
     return dm_exp(-b * r);
 }
 
-// TargetPotential (HydrogenLikeAtom.jl:75, SAEAtom.jl:264-269)
+// TargetPotential (HydrogenLikeAtom.jl:75, SAEAtom.jl:84-89)
 __host__ __device__ __forceinline__ double target_V(const DTarget& T, double x, double y, double z) {
     if (T.kind == ETRAJ_TARGET_HYDROGEN_LIKE) {
         double s = ((x * x + y * y) + z * z) + T.sc;
@@ -306,7 +306,7 @@ __host__ __device__ __forceinline__ double target_V(const DTarget& T, double x, 
     return -num / sqrt(r * r + T.sc);
 }
 
-// ODE right-hand side (TrajectoryFunction, HydrogenLikeAtom.jl:78-159, SAEAtom.jl:278-366).
+// ODE right-hand side (TrajectoryFunction, HydrogenLikeAtom.jl:78-159, SAEAtom.jl:98-186).
 // DIM: 2 or 3; PHASE: ETRAJ_PHASE_*; TGT: ETRAJ_TARGET_*.
 template <int DIM, int PHASE, int TGT>
 __host__ __device__ __forceinline__ void rhs(const DJob& J, double t, const double* u, double* du) {
@@ -333,7 +333,7 @@ __host__ __device__ __forceinline__ void rhs(const DJob& J, double t, const doub
             tFy = y * coef;
             if (PHASE != ETRAJ_PHASE_CTMC) {
                 double num = ((T.Z + T.a1 * e1) + (T.a2 * r) * e2) + T.a3 * e3;
-                // the 2D SCTS reference divides by r^2+sc, not its square root (SAEAtom.jl:316)
+                // the 2D SCTS reference divides by r^2+sc, not its square root (SAEAtom.jl:136)
                 Vphase = (PHASE == ETRAJ_PHASE_SCTS) ? num / s : num / rs;
             } else {
                 Vphase = 0.0;

@@ -95,7 +95,7 @@ class HydrogenLikeAtom(SAEAtomBase):
 
 
 class SAEAtom(SAEAtomBase):
-    """Single-active-electron atom with the Tong-Lin potential (SAEAtom.jl:187-252)."""
+    """Single-active-electron atom with the Tong-Lin potential (SAEAtom.jl:7-72)."""
 
     def __init__(self, Ip, Z, l=0, m=0, asymp_coeff="hartree", quan_ax_θ=0.0, quan_ax_ϕ=0.0,
                  a1=0.0, b1=0.0, a2=0.0, b2=0.0, a3=0.0, b3=0.0, soft_core=1e-10, name="[NA]"):

@@ -359,16 +359,21 @@ int etraj_stage_times(etraj_ctx* ctx, double* ms, int n);
  * per-electron contributions into a momentum grid, with no cudaMalloc, no
  * cudaFree and no context.  All pointers are device pointers owned by the
  * caller:
- *   key[i]        bin of electron i in [0, grid], grid meaning "not deposited"
- *                 (larger values are not allowed)
+ *   key[i]        bin of electron i in [0, grid), or grid for "not deposited";
+ *                 a key above grid is taken as grid (not deposited)
  *   c_re, c_im    its contribution (c_im read only when coherent != 0)
  *   spec_re/im    outputs: per-bin sums in electron order (spec_im when coherent)
  *   momentum_spec output: spec_re (CTMC) or spec_re^2 + spec_im^2 (coherent)
  * Work is queued on cuda_stream (NULL = legacy default stream); the call
  * returns without synchronizing.  The sort scratch is one fixed device array
  * of the library, sized for at most 524288 (2^19) contributions per call
- * (about 8 MiB, held by every GPU that loads the library until the process
- * exits); larger n returns ETRAJ_ERR_INVALID_ARGUMENT.  The array is shared
+ * (about 10 MiB, held by every GPU that loads the library until the process
+ * exits); larger n returns ETRAJ_ERR_INVALID_ARGUMENT.  That array comes into
+ * being when the library's device code is loaded on a device, which with
+ * CUDA's lazy module loading can be this entry point's first call: make that
+ * first call (or any other call of this library on the device) before a memory
+ * pool of the caller claims the device's free memory, or it can fail with
+ * ETRAJ_ERR_CUDA.  The array is shared
  * by all calls: calls whose work overlaps on the GPU (different streams,
  * different host threads) race, so serialize them.  The first call on a
  * device looks up the array's device address; make that first call before

@@ -5,7 +5,7 @@
  * Restates:
  *   src/Lasers/Cos4Laser.jl:81-152, Cos2Laser.jl:81-152,
  *   GaussianLaser.jl:85-160, BichromaticLaser.jl:59-85
- *   src/Targets/HydrogenLikeAtom.jl:66-159, SAEAtom.jl:255-366,
+ *   src/Targets/HydrogenLikeAtom.jl:66-159, SAEAtom.jl:84-186,
  *   SAEAtomBase_shared.jl:3-11
  *
  * Canonical arithmetic: every expression keeps the reference's
@@ -337,7 +337,7 @@ void o_target_prepare(const etraj_target* in, o_target* T) {
     }
 }
 
-/* TargetPotential (HydrogenLikeAtom.jl:75, SAEAtom.jl:264-269) */
+/* TargetPotential (HydrogenLikeAtom.jl:75, SAEAtom.jl:84-89) */
 double o_target_V(const o_target* T, double x, double y, double z) {
     if (T->kind == ETRAJ_TARGET_HYDROGEN_LIKE) {
         double s = ((x * x + y * y) + z * z) + T->sc;
@@ -349,7 +349,7 @@ double o_target_V(const o_target* T, double x, double y, double z) {
     return -num / sqrt(r * r + T->sc);
 }
 
-/* TargetForce (HydrogenLikeAtom.jl:76, SAEAtom.jl:271-276) */
+/* TargetForce (HydrogenLikeAtom.jl:76, SAEAtom.jl:91-96) */
 void o_target_F(const o_target* T, double x, double y, double z, double* F) {
     if (T->kind == ETRAJ_TARGET_HYDROGEN_LIKE) {
         double s = ((x * x + y * y) + z * z) + T->sc;
@@ -373,7 +373,7 @@ double oracle_hartree_asymp_coeff(int Z, double Ip, int l) {
     return pow(2.0, n - 1.0) / sqrt(n * tgamma(n + l + 1.0) * tgamma(n - l));
 }
 
-/* ODE right-hand sides: HydrogenLikeAtom.jl:78-159 and SAEAtom.jl:278-366. */
+/* ODE right-hand sides: HydrogenLikeAtom.jl:78-159 and SAEAtom.jl:98-186. */
 void o_rhs(const o_sys* S, double t, const double* u, double* du) {
     const o_target* T = &S->target;
     double Fx, Fy;
@@ -396,7 +396,7 @@ void o_rhs(const o_sys* S, double t, const double* u, double* du) {
             double coef = -((1.0 / (s * rs)) * br + ((T->a2 * T->b2) / rs) * e2);
             tFx = x * coef; tFy = y * coef;
             double num = ((T->Z + T->a1 * e1) + (T->a2 * r) * e2) + T->a3 * e3;
-            /* SCTS 2D divides by r^2+sc, not its square root (SAEAtom.jl:316) */
+            /* SCTS 2D divides by r^2+sc, not its square root (SAEAtom.jl:136) */
             Vphase = (S->phase == ETRAJ_PHASE_SCTS) ? num / s : num / rs;
         }
         du[0] = px;

@@ -202,7 +202,7 @@ static int o_solve(const o_sys* S, double t0, double tf, const double* u0, doubl
 }
 
 /* ---- validation (TrajectorySimulation.jl:178-186, ADKSampler.jl:43-105,
- *      HydrogenLikeAtom.jl:53-56, SAEAtom.jl:240-244, Cos4Laser.jl:57-58) ----------- */
+ *      HydrogenLikeAtom.jl:53-56, SAEAtom.jl:60-64, Cos4Laser.jl:57-58) ----------- */
 /* the sampler of the job being validated: its name replaces "[ADKSampler]" in the
  * shared checks, as the reference's SPANE / SPA / WFAT samplers word them */
 static __thread int o_method = ETRAJ_SAMPLER_ADK;

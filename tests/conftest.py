@@ -11,6 +11,11 @@ import __graft_entry__  # noqa: E402
 
 __graft_entry__.load_package()
 
+# A checkout of the reference (eTraj.jl), read as data by a few CPU tests (its
+# molecule database files); those tests skip when ETRAJ_REFERENCE_DIR is unset.
+REFERENCE_DIR = os.environ.get("ETRAJ_REFERENCE_DIR", "")
+REFERENCE_DB = os.path.join(REFERENCE_DIR, "src", "Targets", "Database") if REFERENCE_DIR else ""
+
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built library")

@@ -1,8 +1,8 @@
 """Extracts the numeric known-answer pins of eTraj.jl's own test suite into
 sampler_survivors.json and physics_pins.json.
 
-Run in a checkout that has the reference at /root/reference (read as text,
-nothing is executed):  python tests/golden/make_golden.py [reference_dir]
+Run with a checkout of the reference (read as text, nothing is executed):
+  python tests/golden/make_golden.py <reference_dir>
 
 Sources:
   test/ElectronSamplers_test.jl:11-50   common parameters of the sampler tests
@@ -92,4 +92,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <reference_dir>")
+    main(sys.argv[1])

@@ -2,9 +2,9 @@
 molecule_hydrogen.npz, and the numeric molecule pins of its test suite into
 molecule_pins.json.
 
-Run in a checkout that has the reference at /root/reference (the data file is
-read with this package's JLD2 reader; the test file is read as text, nothing
-is executed):  python tests/golden/make_molecule_fixture.py [reference_dir]
+Run with a checkout of the reference (the data file is read with this
+package's JLD2 reader; the test file is read as text, nothing is executed):
+  python tests/golden/make_molecule_fixture.py <reference_dir>
 
 Sources:
   src/Targets/Database/Molecule_Hydrogen.jld2   the data get_mol("Hydrogen") loads
@@ -81,4 +81,6 @@ def main(ref):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_molecule_fixture.py <reference_dir>")
+    main(sys.argv[1])

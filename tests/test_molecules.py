@@ -20,8 +20,10 @@ from etraj_gb300 import abi
 with open(os.path.join(GOLDEN, "molecule_pins.json"), encoding="utf-8") as f:
     PINS = json.load(f)
 
-REF_DB = os.path.join("/root/reference", "src", "Targets", "Database")
-need_db = pytest.mark.skipif(not os.path.isdir(REF_DB), reason="the reference's molecule database is not present")
+from conftest import REFERENCE_DB as REF_DB  # noqa: E402
+
+need_db = pytest.mark.skipif(not (REF_DB and os.path.isdir(REF_DB)),
+                             reason="set ETRAJ_REFERENCE_DIR to a reference checkout (its molecule database)")
 
 
 def close(a, b):

@@ -11,7 +11,7 @@ import pytest
 
 from etraj_gb300 import h5write, jld2
 
-REF_DB = os.path.join("/root/reference", "src", "Targets", "Database")
+from conftest import REFERENCE_DB as REF_DB  # noqa: E402
 
 
 def test_lookup3_published_vectors():
@@ -22,7 +22,8 @@ def test_lookup3_published_vectors():
     assert h5write.lookup3(b"Four score and seven years ago", 1) == 0xCD628161
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_DB), reason="the reference's database files are not present")
+@pytest.mark.skipif(not (REF_DB and os.path.isdir(REF_DB)),
+                    reason="set ETRAJ_REFERENCE_DIR to a reference checkout (its database files)")
 def test_lookup3_reproduces_the_checksums_of_jld2_files():
     for name in ("Molecule_Hydrogen.jld2", "Molecule_Oxygen.jld2"):
         b = open(os.path.join(REF_DB, name), "rb").read()

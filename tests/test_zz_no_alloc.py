@@ -5,6 +5,10 @@ memory before a run).  Its sort scratch is a fixed array inside the library.
 The test feeds it the per-electron bins and contributions of a job and checks
 that it reproduces the momentum distribution that etraj_run computes for the
 same job, on two calls in a row (the scratch keeps the first call's contents).
+Between them runs a call with fewer electrons, another grid and some keys above
+that grid (taken as "not deposited"), checked against a deposit done on the
+host: left-over pairs, histograms or counts of a larger call must not leak into
+a smaller one, nor the smaller one's into the next.
 Tolerance: the same 1e-10 relative L2 as the other parity tests (the deposit
 order is fixed, so the results are in fact bit-identical).  Inputs and outputs
 are device buffers the test allocates with torch, as such a caller would.
@@ -60,8 +64,8 @@ def test_noalloc_deposit_matches_run(phase):
     d_re = torch.from_numpy(cre).to(dev)
     d_im = torch.from_numpy(cim).to(dev)
     stream = torch.cuda.Stream(device=dev)
-    outs = []
-    for _ in range(2):
+
+    def deposit(d_key, d_re, d_im, n, grid):
         s_re = torch.full((grid,), 7.0, dtype=torch.float64, device=dev)  # outputs start dirty
         s_im = torch.full((grid,), 7.0, dtype=torch.float64, device=dev)
         mspec = torch.empty(grid, dtype=torch.float64, device=dev)
@@ -72,12 +76,35 @@ def test_noalloc_deposit_matches_run(phase):
                                         C.c_void_p(mspec.data_ptr()), C.c_void_p(stream.cuda_stream))
         assert stc == abi.OK
         stream.synchronize()
-        outs.append((mspec.cpu().numpy(), s_re.cpu().numpy(), s_im.cpu().numpy()))
-    for mspec, s_re, s_im in outs:
+        return mspec.cpu().numpy(), s_re.cpu().numpy(), s_im.cpu().numpy()
+
+    def check_full(out):
+        mspec, s_re, s_im = out
         assert _rel_l2(mspec, spec_ref) <= 1e-10
         assert np.array_equal(mspec, spec_ref)
         if coherent:
             assert _rel_l2(s_re + 1j * s_im, amp_ref[0::2] + 1j * amp_ref[1::2]) <= 1e-10
+
+    check_full(deposit(d_key, d_re, d_im, n, grid))
+    # a smaller call on another grid: a prefix of the electrons, their bins folded
+    # onto grid2, every 97th key replaced by one far above grid2
+    n2 = n // 3
+    grid2 = grid // 2 + 7
+    k2 = key[:n2].astype(np.int64)
+    k2 = np.where(k2 == grid, grid2, k2 % grid2)
+    k2[::97] = 0xFFFFFFF0
+    k2 = k2.astype(np.uint32)
+    want_re, want_im = np.zeros(grid2), np.zeros(grid2)
+    for i in range(n2):  # bins summed in electron order, from 0.0, as the device does
+        if k2[i] < grid2:
+            want_re[k2[i]] += cre[i]
+            want_im[k2[i]] += cim[i]
+    want = want_re * want_re + want_im * want_im if coherent else want_re
+    m2, r2, i2 = deposit(torch.from_numpy(k2.view(np.int32)).to(dev), d_re, d_im, n2, grid2)
+    assert _rel_l2(m2, want) <= 1e-10 and np.array_equal(m2, want)
+    assert np.array_equal(r2, want_re) and (not coherent or np.array_equal(i2, want_im))
+    # and the first call again, after the smaller one
+    check_full(deposit(d_key, d_re, d_im, n, grid))
 
 
 def test_noalloc_deposit_rejects_oversize_and_empty_is_zero():
