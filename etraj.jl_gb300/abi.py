@@ -26,7 +26,7 @@ MOL_MAX_L = 6
 SAMPLER_ADK, SAMPLER_SPANE, SAMPLER_SPA, SAMPLER_WFAT = 0, 1, 2, 3
 PREFIX_PRE, PREFIX_PRECC, PREFIX_JAC = 1, 2, 4
 PHASE_CTMC, PHASE_QTMC, PHASE_SCTS = 0, 1, 2
-PRECISION_FP64, PRECISION_FP32_BULK = 0, 1
+PRECISION_FP64, PRECISION_FP32_BULK, PRECISION_FP32_DF = 0, 1, 2
 
 
 class MonoLaser(C.Structure):

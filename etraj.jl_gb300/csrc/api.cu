@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "integrate_setup.h"
 #include "mol_check.h"
 
 using namespace etraj;
@@ -42,31 +43,6 @@ namespace {
 constexpr bool kHaveFp32Bulk = true;
 
 // ---- host-side job set-up (same expressions as the reference's getters) ----------
-void mono_prepare(const etraj_mono_laser& in, DMono& L) {
-    std::memset(&L, 0, sizeof L);
-    L.kind = in.kind;
-    L.omega = 45.563352525 / in.wave_len;        // AngFreq, Cos4Laser.jl:81
-    L.period = 6.283185307179586 / L.omega;      // Period = 2pi/omega
-    L.F0 = std::sqrt((in.peak_int / (1.0 + in.ellip * in.ellip)) / 3.50944521e16);  // :85
-    L.A0 = L.F0 / L.omega;
-    L.N = in.cyc_num;
-    L.cep = in.cep;
-    L.t_shift = in.t_shift;
-    L.ellip = in.ellip;
-    L.azi_zero = (in.azi == 0.0);
-    dm_sincos(in.azi, &L.sphi, &L.cphi);
-    if (L.kind == ETRAJ_LASER_GAUSSIAN) {
-        L.sigma = in.cyc_num * L.period;          // SpreadDuration, GaussianLaser.jl:85
-        L.inv_s2 = 1.0 / (L.sigma * L.sigma);
-        L.inv_2s2 = 1.0 / (2.0 * (L.sigma * L.sigma));
-    } else {
-        L.w2n = L.omega / (2.0 * L.N);
-        L.cN = (L.kind == ETRAJ_LASER_COS4) ? 2.0 / L.N : 1.0 / L.N;
-        L.k = 200.0 / L.period;
-        L.Npiw = (L.N * 3.141592653589793) / L.omega;
-    }
-}
-
 double fact(int n) {
     double f = 1.0;
     for (int i = 2; i <= n; ++i) f *= (double)i;
@@ -165,7 +141,8 @@ int validate_job(const etraj_job* job, std::string& err) {
         err = "the FP32-bulk integrator is not built in this library.";
         return ETRAJ_ERR_UNSUPPORTED;
     }
-    if (job->precision != ETRAJ_PRECISION_FP64 && job->precision != ETRAJ_PRECISION_FP32_BULK)
+    if (job->precision != ETRAJ_PRECISION_FP64 && job->precision != ETRAJ_PRECISION_FP32_BULK &&
+        job->precision != ETRAJ_PRECISION_FP32_DF)
         return fail("unknown precision.");
     if (job->rate_prefix & ~7) return fail("[ADKSampler] Undefined tunneling rate prefix.");
     if ((job->rate_prefix & ETRAJ_PREFIX_PRE) && (job->rate_prefix & ETRAJ_PREFIX_PRECC))
@@ -254,6 +231,17 @@ int validate_job(const etraj_job* job, std::string& err) {
             return ETRAJ_ERR_UNSUPPORTED;
         }
     }
+    if (job->precision == ETRAJ_PRECISION_FP32_DF) {
+        // the double-float integrator's clock counts field-table intervals of T/1024 below 2^24
+        double T = 6.283185307179586 * job->laser.mono[0].wave_len / 45.563352525;
+        if (nm == 2) T = std::min(T, 6.283185307179586 * job->laser.mono[1].wave_len / 45.563352525);
+        const double span = (job->traj_t_final - job->sample_t_intv[0]) / (T / (double)kDfTablePerPeriod);
+        if (!(span < (double)(1 << 24) - 8.0)) {
+            err = "the double-float integrator covers at most 16000 laser periods from the first time sample "
+                  "to traj_t_final; use FP64 precision.";
+            return ETRAJ_ERR_UNSUPPORTED;
+        }
+    }
     return ETRAJ_OK;
 }
 
@@ -273,29 +261,10 @@ void prepare_job(const etraj_job* job, HostJob& H) {
     J.mono = (job->laser.kind != ETRAJ_LASER_BICHROMATIC) ? 1 : 0;
     J.cutoff = job->sample_cutoff_limit;
     J.seed = job->seed;
-    J.laser.kind = job->laser.kind;
-    mono_prepare(job->laser.mono[0], J.laser.m[0]);
-    if (job->laser.kind == ETRAJ_LASER_BICHROMATIC) {
-        mono_prepare(job->laser.mono[1], J.laser.m[1]);
-        J.laser.delay = job->laser.delay;
-        J.laser.nmono = 2;
-    } else {
-        J.laser.nmono = 1;
-    }
+    prepare_integration(job, J);  // laser, target, rtol, t_final
     // the SPA initial guess uses the laser's omega, or the mean of the two (SPASampler.jl:160-166)
     J.spa_omega = (J.laser.nmono == 2) ? (J.laser.m[0].omega + J.laser.m[1].omega) / 2.0 : J.laser.m[0].omega;
     const etraj_target& T = job->target;
-    J.target.kind = T.kind;
-    J.target.Z = (double)T.Z;
-    J.target.Ip = T.Ip;
-    J.target.sc = T.soft_core;
-    J.target.a1 = T.a1; J.target.b1 = T.b1;
-    J.target.a2 = T.a2; J.target.b2 = T.b2;
-    J.target.a3 = T.a3; J.target.b3 = T.b3;
-    {
-        const double a[3] = {T.a1, T.a2, T.a3}, b[3] = {T.b1, T.b2, T.b3};
-        J.target.skip_ok = etraj_sae_skip_exact((double)T.Z, a, b, T.soft_core);
-    }
     J.Ip = T.Ip;
     J.Z = (double)T.Z;
     J.l = T.l;
@@ -305,10 +274,7 @@ void prepare_job(const etraj_job* job, HostJob& H) {
         // GenericMolecule's trajectories are the hydrogen-like equations with
         // Z = charge + 1, soft core 1.0 and the phase's Ip = IonPotential(mol)
         // (GenericMolecule.jl:438-445); the sampler uses the orbital's Ip (J.Ip)
-        J.target.kind = ETRAJ_TARGET_HYDROGEN_LIKE;
-        J.target.Ip = T.mol_Ip_traj;
-        J.target.sc = 1.0;
-        J.target.skip_ok = 0;
+        // (the trajectories' target is set by prepare_integration)
         J.l = 0;
         J.m = 0;
         J.C = 0.0;
@@ -415,8 +381,6 @@ void prepare_job(const etraj_job* job, HostJob& H) {
     fc.kz_max = (float)J.mc_kz_max;
     fc.kd_zero = (J.mc_kd_max == 0.0) ? 1 : 0;
     fc.kz_zero = (J.mc_kz_max == 0.0) ? 1 : 0;
-    J.rtol = job->traj_rtol;
-    J.t_final = job->traj_t_final;
     J.grid = 1;
     for (int d = 0; d < 3; ++d) {
         if (d < J.dim) {
@@ -761,6 +725,18 @@ void prepare_bulk(const DJob& J, double tmin, BulkParams& B) {
     B.r_far = sae_far_radius(T_);
 }
 
+// Double-float integrator parameters (integrate_setup.h) and its launch shape: a
+// persistent grid of 128-thread blocks, as many as are resident, and no more
+// than the job keeps busy (~4 electrons per lane).
+void prepare_df(const DJob& J, double tmin, int64_t max_n, int sm_count, DFParams& D) {
+    prepare_df_params(J, tmin, max_n, D);
+    D.threads = 128;
+    const int64_t lanes_per_block = (int64_t)D.threads * 4;
+    const int64_t want = (max_n + lanes_per_block - 1) / lanes_per_block;
+    const int64_t cap = (int64_t)sm_count * df_blocks_per_sm(D.dim, D.phase, D.tgt, D.threads);
+    D.blocks = (int)(want < 1 ? 1 : (want < cap ? want : cap));
+}
+
 // ---- autotuner of the bulk integrator's launch shape ----------------------------------
 // Candidates: threads per block x blocks per SM x the register budget of the
 // build (<= 128 registers: 16 warps per SM; <= 85: 24 warps) x the number of
@@ -897,6 +873,21 @@ int launch_integrate(etraj_ctx* ctx, const DJob& J, const InitSoA& soa, const do
                      int precision, double tmin, int* launches, cudaEvent_t* ev = nullptr) {
     // ev (optional): events recorded after the field table [0] and the integrator [1]
     cudaStream_t s = ctx->stream;
+    if (precision == ETRAJ_PRECISION_FP32_DF) {
+        DFParams D;
+        prepare_df(J, tmin, max_n, ctx->sm_count, D);
+        float4* tab = nullptr;
+        ETRAJ_TRY(ensure_t(ctx, "field_table_df", (size_t)D.n_int * kDfTableF4, &tab));
+        D.table = tab;
+        DfTableNodes nodes;
+        df_table_nodes(nodes);
+        *launches += launch_field_table_df(J, D.T0, D.h_d, D.n_int, nodes, tab, s);
+        if (ev) rec(ctx, ev[0], s);
+        *launches += launch_integrate_df(D, soa, t, idx, count, work, out, s);
+        if (ev) rec(ctx, ev[1], s);
+        *launches += launch_collect_fp64(J, soa, t, idx, count, out, max_n, ctx->sm_count, s);
+        return ETRAJ_OK;
+    }
     if (precision != ETRAJ_PRECISION_FP32_BULK) {
         if (ev) rec(ctx, ev[0], s);
         *launches += launch_integrate_fp64(J, soa, t, idx, count, out, max_n, ctx->sm_count, s);
@@ -978,7 +969,13 @@ size_t plan_growth(etraj_ctx* ctx, const etraj_job* job) {
     ctx->dry_bytes = 0;
     alloc_sampling(ctx, H, P);
     const bool bulk = (job->precision == ETRAJ_PRECISION_FP32_BULK);
-    alloc_outputs(ctx, H.J, H.J.n_total, bulk, P);
+    alloc_outputs(ctx, H.J, H.J.n_total, job->precision != ETRAJ_PRECISION_FP64, P);
+    if (job->precision == ETRAJ_PRECISION_FP32_DF) {
+        DFParams D;
+        prepare_df_params(H.J, H.t.front(), H.J.n_total, D);
+        float4* tab = nullptr;
+        ensure_t(ctx, "field_table_df", (size_t)D.n_int * kDfTableF4, &tab);
+    }
     if (bulk) {
         BulkParams B;
         prepare_bulk(H.J, H.t.front(), B);
@@ -1034,8 +1031,16 @@ int enqueue_kernels_maybe_graph(etraj_ctx* ctx, const etraj_job* job, const Host
         ETRAJ_TRY(ensure_t(ctx, "field_table", n_int * 2, &tab));
         ETRAJ_TRY(attach_park(ctx, B));
     }
+    if (use_graph && job->precision == ETRAJ_PRECISION_FP32_DF) {
+        DFParams D;  // allocate the field table outside the capture
+        prepare_df_params(J, H.t.front(), J.n_total, D);
+        n_int = (size_t)D.n_int;
+        float4* tab = nullptr;
+        ETRAJ_TRY(ensure_t(ctx, "field_table_df", n_int * kDfTableF4, &tab));
+    }
     if (!use_graph) return enqueue_kernels(ctx, job, H, P, launches);
-    void* tab_ptr = ctx->bufs.count("field_table") ? ctx->bufs["field_table"].p : nullptr;
+    const char* tab_name = (job->precision == ETRAJ_PRECISION_FP32_DF) ? "field_table_df" : "field_table";
+    void* tab_ptr = ctx->bufs.count(tab_name) ? ctx->bufs[tab_name].p : nullptr;
     std::vector<unsigned char> key(sizeof J + sizeof P + sizeof(int) * 3 + sizeof(size_t) + sizeof(void*));
     unsigned char* k = key.data();
     std::memcpy(k, &J, sizeof J);
@@ -1099,7 +1104,7 @@ int enqueue_job(etraj_ctx* ctx, const etraj_job* job, JobRec& r) {
     const DJob& J = H.J;
     Pipeline P;
     ETRAJ_TRY(alloc_sampling(ctx, H, P));
-    ETRAJ_TRY(alloc_outputs(ctx, J, J.n_total, job->precision == ETRAJ_PRECISION_FP32_BULK, P));
+    ETRAJ_TRY(alloc_outputs(ctx, J, J.n_total, job->precision != ETRAJ_PRECISION_FP64, P));
     r.grid = J.grid;
     r.coherent = (J.phase != ETRAJ_PHASE_CTMC);
     const bool want_spec = r.res.momentum_spec != nullptr;

@@ -28,6 +28,7 @@ UNITS = {
     "integrate_fp64.cu": ["--fmad=false"],
     "deposit.cu": ["--fmad=false"],
     "integrate_fp32.cu": ["--fmad=true"],
+    "integrate_df.cu": ["--fmad=false"],
     "sampler_fp32.cu": ["--fmad=true"],
 }
 HEADERS = sorted(f for f in os.listdir(HERE) if f.endswith((".h", ".cuh")))

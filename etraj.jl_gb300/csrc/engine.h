@@ -250,6 +250,40 @@ int launch_integrate_bulk(const BulkParams& P, InitSoA soa, const double* t, con
                           const unsigned long long* count, unsigned long long* queue, TrajOut out,
                           int sm_count, cudaStream_t s);
 
+// Parameters of the double-float integrator (integrate_df.cu).  float2 values are
+// double-float pairs (x = high float, y = low float), rounded on the host.
+struct DFParams {
+    int dim, phase, tgt;
+    int n_int;            // field-table intervals (kDfTableF4 float4 each: degree-7 pieces of Fx, Fy)
+    const float4* table;
+    double T0, h_d, inv_h_d, t_final;
+    float2 h, inv_h;      // table spacing and its inverse
+    int nf;               // t_final = T0 + h (nf + ff)
+    float2 ff;
+    float2 rtol;
+    float t_snap;         // 100 ulp of t_final: a step ending closer than this ends the solve
+    float2 Z, Ip, sc, a1, b1, a2, b2, a3, b3, a2b2;
+    int max_iters;
+    int threads, blocks;  // launch shape (persistent grid)
+    int64_t max_n;
+};
+constexpr int kDfTablePerPeriod = 1024;  // table intervals per shortest laser period
+constexpr int kDfTableF4 = 7;            // float4 per table interval
+// Chebyshev nodes of a field-table piece and the values of T_0..T_7 there
+struct DfTableNodes {
+    double u[8];
+    double Tm[8][8];
+};
+int launch_field_table_df(const DJob& J, double T0, double h, int n_int, const DfTableNodes& nodes, float4* tab,
+                          cudaStream_t s);
+// Work-stealing double-float Tsit5 solve of the survivors; writes out.final_state
+// (FP64), out.status and out.steps, for launch_collect_fp64.
+int launch_integrate_df(const DFParams& P, InitSoA soa, const double* t, const int64_t* idx,
+                        const unsigned long long* count, unsigned long long* queue, TrajOut out,
+                        cudaStream_t s);
+// Resident blocks per SM of a double-float integrator variant (threads per block given).
+int df_blocks_per_sm(int dim, int phase, int tgt, int threads);
+
 // Deterministic deposit: stable radix sort of (key, survivor) and segmented sums.
 struct DepositScratch {
     uint32_t *keys_a, *keys_b, *vals_a, *vals_b;

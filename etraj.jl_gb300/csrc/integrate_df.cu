@@ -1,0 +1,244 @@
+// integrate_df.cu -- the double-float integrator: persistent, warp-cooperative,
+// work-stealing Tsit5 on the FP32 pipe with every stage value, sum, error
+// estimate and controller power a double-float pair (dfloat.h), each stage
+// formed as a difference from the accepted state (df_solve.cuh).
+//
+// It restates the plain FP64 solve of integrate_fp64.cu step for step, so it
+// takes the FP64 path's step sequence and its final states agree with the FP64
+// path's to ~1e-11 (the spread a 1-ulp change of an FP64 input gives); the FP64
+// collection (Kepler asymptote, SCTS phase) and deposit then run on them
+// unchanged.  What FP32 stage values cannot do is resolve the error estimate,
+// whose weighted sums cancel to ~1e-10 of the stage derivatives in an electron's
+// first steps: with FP32 stages the controller sees another error and takes
+// another step sequence.
+//
+// Schedule.  A warp advances its lanes stage by stage in lock-step: a counter
+// st = 1..6 shared by the warp selects the Tsit5 stage every stepping lane
+// evaluates, and each turn of the loop makes exactly one right-hand-side
+// evaluation, so the kernel holds one copy of that (long) double-float code and
+// the instruction cache keeps it.  The stage differences of the attempt live in
+// shared memory (6 slots per lane).  At each attempt boundary (st = 1) lanes that
+// finished take new electrons from a global queue (warp-aggregated atomicAdd); a
+// new electron spends the first two turns on its starting step and joins the
+// stepping lanes at the next boundary.  The laser table at the end of the
+// attempt (stage 5) serves stage 6 and the new accepted state too.
+//
+// Field table.  F(t) is one function of time for every electron, tabulated once
+// per job in FP64: pieces of width h = T_min/1024 (T_min the shortest laser
+// period), each the degree-7 polynomial through F at the piece's 8 Chebyshev
+// nodes, stored as monomials in u in [-1, 1] (c0 exact as three floats, c1..c3 as
+// double-float pairs, c4..c7 as floats), 112 B per piece read through the L1
+// cache.  Time is a clock of an integer piece index and a double-float fraction.
+//
+// Roofline: FP32 issue bound (a double-float add is ~11 FP32 instructions, a
+// product ~7); no tensor cores (not a contraction).  Compiled with
+// --fmad=false: every fused multiply-add is an explicit fmaf(), as the
+// error-free transformations need.
+
+#include "df_solve.cuh"
+
+namespace etraj {
+
+__device__ const float g_df_exp2[2 * kExpTabN] = {ETRAJ_DF_EXP2_TABLE};
+__device__ const float g_df_log2c[2 * kLogTabN] = {ETRAJ_DF_LOG2C_TABLE};
+__device__ const float g_df_rcpc[2 * kLogTabN] = {ETRAJ_DF_RCPC_TABLE};
+
+namespace {
+
+constexpr int kDfThreads = 128;
+
+template <int DIM, int PHASE>
+constexpr int slot_floats() {
+    return 6 * dfs::Lane<DIM, PHASE>::KW;
+}
+
+enum LaneMode { kFree = 0, kInit0 = 1, kInit1 = 2, kWait = 3, kStep = 4 };
+
+template <int DIM, int PHASE, int TGT>
+__global__ void __launch_bounds__(kDfThreads)
+k_integrate_df(const __grid_constant__ DFParams P, InitSoA soa, const double* __restrict__ tsamp,
+               const int64_t* __restrict__ idx, const unsigned long long* __restrict__ count,
+               unsigned long long* __restrict__ queue, TrajOut out) {
+    using LaneT = dfs::Lane<DIM, PHASE>;
+    constexpr int KW = LaneT::KW;
+    constexpr int N = LaneT::N;
+    extern __shared__ float s_slots[];
+    __shared__ float s_exp2[2 * kExpTabN], s_log2c[2 * kLogTabN], s_rcpc[2 * kLogTabN];
+    for (int i = threadIdx.x; i < 2 * kExpTabN; i += blockDim.x) s_exp2[i] = g_df_exp2[i];
+    for (int i = threadIdx.x; i < 2 * kLogTabN; i += blockDim.x) {
+        s_log2c[i] = g_df_log2c[i];
+        s_rcpc[i] = g_df_rcpc[i];
+    }
+    __syncthreads();
+    const dfs::Tabs T{s_exp2, s_log2c, s_rcpc};
+    const dfs::Slots<KW> ks{s_slots + threadIdx.x, (int)blockDim.x};
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const unsigned long long n_traj = *count;
+
+    LaneT L = {};
+    int mode = kFree;
+    unsigned long long s = 0;
+    bool drained = false;
+
+    auto finish = [&](int status) {
+        out.status[s] = status;
+        out.steps[s] = L.attempts;
+        double fs[N];
+        dfs::final_state(L, fs);
+#pragma unroll
+        for (int j = 0; j < N; ++j) out.final_state[s * N + j] = fs[j];
+        mode = kFree;
+    };
+
+    for (int st = 1;; st = (st == 6) ? 1 : st + 1) {
+        if (st == 1) {
+            // ---- attempt boundary: start the next attempts, refill free lanes ----------
+            if (mode == kWait) mode = kStep;
+            if (mode == kStep) {
+                const int status = dfs::prologue(L, P);
+                if (status) finish(status);
+            }
+            const unsigned freem = __ballot_sync(FULL, mode == kFree);
+            if (freem && !drained) {
+                const int leader = __ffs(freem) - 1;
+                unsigned long long base = 0ull;
+                if (lane == leader) base = atomicAdd(queue, (unsigned long long)__popc(freem));
+                base = __shfl_sync(FULL, base, leader);
+                drained = base + (unsigned long long)__popc(freem) >= n_traj;
+                if (mode == kFree) {
+                    s = base + __popc(freem & lt_mask);
+                    if (s < n_traj) {
+                        const int64_t g = idx ? idx[s] : (int64_t)s;
+                        double x0[DIM], p0[DIM];
+                        x0[0] = soa.x[g];
+                        x0[1] = soa.y[g];
+                        p0[0] = soa.kx[g];
+                        p0[1] = soa.ky[g];
+                        if (DIM == 3) {
+                            x0[2] = 0.0;
+                            p0[2] = soa.kz[g];
+                        }
+                        dfs::load(L, P, x0, p0, LaneT::HASPH ? soa.phase[g] : 0.0, tsamp[soa.batch[g]]);
+                        mode = kInit0;
+                    }
+                }
+            }
+            if (__ballot_sync(FULL, mode != kFree) == 0u) break;
+        }
+        // ---- the inputs of this turn's evaluation ------------------------------------------
+        if (mode == kStep) {
+            switch (st) {
+                case 1: dfs::stage_in<1>(L, ks); break;
+                case 2: dfs::stage_in<2>(L, ks); break;
+                case 3: dfs::stage_in<3>(L, ks); break;
+                case 4: dfs::stage_in<4>(L, ks); break;
+                case 5: dfs::stage_in<5>(L, ks); break;
+                default: dfs::stage_in<6>(L, ks); break;
+            }
+        }
+        // ---- one stage evaluation: the laser table and the target's change from the
+        //      accepted state ---------------------------------------------------------------
+        bool base = (mode == kInit0);  // evaluate the target directly at the accepted state
+        if (mode == kStep || mode == kInit1) {
+            dfs::FieldAt F;
+            const bool step6 = (mode == kStep && st == 6);
+            if (step6) F = L.F5;  // stage 6 is at stage 5's time
+            else dfs::field_at(P, L.ni, L.fi, F);
+            dfs::TAt Tl;
+            df dKT[DIM], dkph;
+            dfs::target_step<DIM, PHASE, TGT>(P, T.exp2, L.X, L.Pv, L.B, L.kph0, L.dX, L.dP, Tl, dKT, dkph);
+            dfs::set_diff(L, ks, (mode == kInit1) ? 1 : st, F, dKT, dkph);
+            if (mode == kInit1) {
+                dfs::init_second(L, P, ks, T);
+                mode = kWait;
+            } else if (st == 5) {
+                L.F5 = F;
+            } else if (step6) {
+                const int status = dfs::epilogue(L, P, ks, T);
+                if (status) finish(status < 0 ? 0 : status);
+                else base = L.accept;
+            }
+        }
+        // ---- the target at a new accepted state (a new electron's, or the end of an
+        //      accepted step) ------------------------------------------------------------------
+        if (base) {
+            dfs::FieldAt F;
+            if (mode == kInit0) dfs::field_at(P, L.ni, L.fi, F);
+            else F = L.F5;
+            df KT[DIM], kph;
+            dfs::target_at<DIM, PHASE, TGT>(P, T.exp2, L.X, L.Pv, L.B, KT, kph);
+            dfs::set_base(L, F, kph);
+            if (mode == kInit0) mode = dfs::init_first(L, P) ? kInit1 : kWait;
+        }
+    }
+}
+
+__global__ void k_field_table_df(const __grid_constant__ DJob J, double T0, double h, int n_int,
+                                 const __grid_constant__ DfTableNodes nodes, float4* __restrict__ tab) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n_int) return;
+    dfs::table_piece(J.laser, T0, h, k, nodes, tab + kDfTableF4 * (size_t)k);
+}
+
+template <int DIM, int PHASE, int TGT>
+int launch_df_t(const DFParams& P, InitSoA soa, const double* t, const int64_t* idx, const unsigned long long* count,
+                unsigned long long* queue, TrajOut out, cudaStream_t s) {
+    const size_t smem = (size_t)slot_floats<DIM, PHASE>() * sizeof(float) * (size_t)P.threads;
+    cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
+    k_integrate_df<DIM, PHASE, TGT><<<P.blocks, P.threads, smem, s>>>(P, soa, t, idx, count, queue, out);
+    return 1;
+}
+
+template <int DIM, int PHASE, int TGT>
+int blocks_t(int threads) {
+    const size_t smem = (size_t)slot_floats<DIM, PHASE>() * sizeof(float) * (size_t)threads;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_integrate_df<DIM, PHASE, TGT>, threads, smem) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return 1;
+    }
+    return nb > 0 ? nb : 1;
+}
+
+}  // namespace
+
+int launch_field_table_df(const DJob& J, double T0, double h, int n_int, const DfTableNodes& nodes, float4* tab,
+                          cudaStream_t s) {
+    k_field_table_df<<<(n_int + 127) / 128, 128, 0, s>>>(J, T0, h, n_int, nodes, tab);
+    return 1;
+}
+
+#define ETRAJ_DF_DISPATCH(FN, ARGS)                                                                  \
+    if (dim == 2) {                                                                                  \
+        if (phase == ETRAJ_PHASE_CTMC)                                                               \
+            return tgt == ETRAJ_TARGET_HYDROGEN_LIKE ? FN<2, ETRAJ_PHASE_CTMC, ETRAJ_TARGET_HYDROGEN_LIKE> ARGS \
+                                                     : FN<2, ETRAJ_PHASE_CTMC, ETRAJ_TARGET_SAE> ARGS;         \
+        if (phase == ETRAJ_PHASE_QTMC)                                                               \
+            return tgt == ETRAJ_TARGET_HYDROGEN_LIKE ? FN<2, ETRAJ_PHASE_QTMC, ETRAJ_TARGET_HYDROGEN_LIKE> ARGS \
+                                                     : FN<2, ETRAJ_PHASE_QTMC, ETRAJ_TARGET_SAE> ARGS;         \
+        return tgt == ETRAJ_TARGET_HYDROGEN_LIKE ? FN<2, ETRAJ_PHASE_SCTS, ETRAJ_TARGET_HYDROGEN_LIKE> ARGS     \
+                                                 : FN<2, ETRAJ_PHASE_SCTS, ETRAJ_TARGET_SAE> ARGS;             \
+    }                                                                                                \
+    if (phase == ETRAJ_PHASE_CTMC)                                                                   \
+        return tgt == ETRAJ_TARGET_HYDROGEN_LIKE ? FN<3, ETRAJ_PHASE_CTMC, ETRAJ_TARGET_HYDROGEN_LIKE> ARGS     \
+                                                 : FN<3, ETRAJ_PHASE_CTMC, ETRAJ_TARGET_SAE> ARGS;             \
+    if (phase == ETRAJ_PHASE_QTMC)                                                                   \
+        return tgt == ETRAJ_TARGET_HYDROGEN_LIKE ? FN<3, ETRAJ_PHASE_QTMC, ETRAJ_TARGET_HYDROGEN_LIKE> ARGS     \
+                                                 : FN<3, ETRAJ_PHASE_QTMC, ETRAJ_TARGET_SAE> ARGS;             \
+    return tgt == ETRAJ_TARGET_HYDROGEN_LIKE ? FN<3, ETRAJ_PHASE_SCTS, ETRAJ_TARGET_HYDROGEN_LIKE> ARGS         \
+                                             : FN<3, ETRAJ_PHASE_SCTS, ETRAJ_TARGET_SAE> ARGS;
+
+int launch_integrate_df(const DFParams& P, InitSoA soa, const double* t, const int64_t* idx,
+                        const unsigned long long* count, unsigned long long* queue, TrajOut out, cudaStream_t s) {
+    const int dim = P.dim, phase = P.phase, tgt = P.tgt;
+    ETRAJ_DF_DISPATCH(launch_df_t, (P, soa, t, idx, count, queue, out, s))
+}
+
+int df_blocks_per_sm(int dim, int phase, int tgt, int threads) { ETRAJ_DF_DISPATCH(blocks_t, (threads)) }
+
+#undef ETRAJ_DF_DISPATCH
+
+}  // namespace etraj

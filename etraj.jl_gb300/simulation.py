@@ -25,7 +25,7 @@ _METHODS = {"ADK": abi.SAMPLER_ADK, "MOADK": abi.SAMPLER_ADK,
             "WFAT": abi.SAMPLER_WFAT}
 _PHASES = {"CTMC": abi.PHASE_CTMC, "QTMC": abi.PHASE_QTMC, "SCTS": abi.PHASE_SCTS}
 _PREFIX_BITS = {"Pre": abi.PREFIX_PRE, "PreCC": abi.PREFIX_PRECC, "Jac": abi.PREFIX_JAC}
-_PRECISIONS = {"fp64": abi.PRECISION_FP64, "fp32_bulk": abi.PRECISION_FP32_BULK}
+_PRECISIONS = {"fp64": abi.PRECISION_FP64, "fp32_bulk": abi.PRECISION_FP32_BULK, "fp32_df": abi.PRECISION_FP32_DF}
 
 
 def _sym(x):
@@ -391,7 +391,7 @@ def perform_traj_simulation(*, init_cond_method, laser, target, dimension, sampl
     :h5 as write_output! does (h5write.py; uncompressed), or "npz".  As in the
     reference (:199-215) an existing file is not overwritten (a time-stamped
     name is used instead) and the extension is appended when missing.  Extra
-    keywords: `precision` ("fp64" or "fp32_bulk"), `seed` (Monte-Carlo
+    keywords: `precision` ("fp64", "fp32_df" or "fp32_bulk"), `seed` (Monte-Carlo
     stream), `engine`."""
     job = make_job(init_cond_method=init_cond_method, laser=laser, target=target,
                    dimension=dimension, sample_t_intv=sample_t_intv, sample_t_num=sample_t_num,

@@ -132,7 +132,11 @@ typedef enum etraj_phase_method {
 
 typedef enum etraj_precision {
     ETRAJ_PRECISION_FP64 = 0,      /* one thread per trajectory, FP64, bit-compatible with the oracle */
-    ETRAJ_PRECISION_FP32_BULK = 1  /* persistent work-stealing integrator, FP32 stages, compensated state */
+    ETRAJ_PRECISION_FP32_BULK = 1, /* persistent work-stealing integrator, FP32 stages, compensated state */
+    ETRAJ_PRECISION_FP32_DF = 2    /* persistent work-stealing integrator on the FP32 pipe, every stage value
+                                      a double-float pair (~48-bit significand) formed as a difference from the
+                                      accepted state: the FP64 path's step sequence, final states within ~1e-10
+                                      of it; FP64 sampling, collection and deposit */
 } etraj_precision;
 
 typedef struct etraj_job {
