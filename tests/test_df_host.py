@@ -43,14 +43,18 @@ def dfhost(tmp_path_factory):
     return lib
 
 
-def host_integrate(lib, job, init):
+def host_integrate(lib, job, init, tmin=None):
+    """The host build's solve of init's electrons; tmin (default: the job's first time
+    sample) places the field table as the library does for the job."""
+    if tmin is None:
+        tmin = float(O.t_samples(job).min())
     n = init.shape[0]
     fin = np.zeros((n, job.state_size))
     st = np.zeros(n, np.int32)
     steps = np.zeros(n, np.int32)
     DP, IP = C.POINTER(C.c_double), C.POINTER(C.c_int32)
     lib.dfhost_integrate(C.addressof(job), n, np.ascontiguousarray(init).ctypes.data_as(DP),
-                         float(O.t_samples(job).min()), fin.ctypes.data_as(DP), st.ctypes.data_as(IP),
+                         tmin, fin.ctypes.data_as(DP), st.ctypes.data_as(IP),
                          steps.ctypes.data_as(IP))
     return fin, st, steps
 
