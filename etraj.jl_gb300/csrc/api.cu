@@ -725,16 +725,28 @@ void prepare_bulk(const DJob& J, double tmin, BulkParams& B) {
     B.r_far = sae_far_radius(T_);
 }
 
-// Double-float integrator parameters (integrate_setup.h) and its launch shape: a
-// persistent grid of 128-thread blocks, as many as are resident, and no more
+// Double-float integrator parameters (integrate_setup.h) and its launch shapes:
+// persistent grids of 128-thread blocks, as many as are resident, and no more
 // than the job keeps busy (~4 electrons per lane).
 void prepare_df(const DJob& J, double tmin, int64_t max_n, int sm_count, DFParams& D) {
     prepare_df_params(J, tmin, max_n, D);
     D.threads = 128;
     const int64_t lanes_per_block = (int64_t)D.threads * 4;
     const int64_t want = (max_n + lanes_per_block - 1) / lanes_per_block;
-    const int64_t cap = (int64_t)sm_count * df_blocks_per_sm(D.dim, D.phase, D.tgt, D.threads);
-    D.blocks = (int)(want < 1 ? 1 : (want < cap ? want : cap));
+    for (int main = 0; main < 2; ++main) {
+        const int64_t cap = (int64_t)sm_count * df_blocks_per_sm(D.dim, D.phase, D.tgt, main != 0, D.threads);
+        (main ? D.blocks_main : D.blocks) = (int)(want < 1 ? 1 : (want < cap ? want : cap));
+    }
+}
+
+// The double-float integrator's buffers: the field table and the carried electrons
+// (kDfCarryWords x max_n words).
+int attach_df(etraj_ctx* ctx, DFParams& D) {
+    float4* tab = nullptr;
+    ETRAJ_TRY(ensure_t(ctx, "field_table_df", (size_t)D.n_int * kDfTableF4, &tab));
+    ETRAJ_TRY(ensure_t(ctx, "df_carry", (size_t)kDfCarryWords * (size_t)(D.max_n > 0 ? D.max_n : 1), &D.carry));
+    D.table = tab;
+    return ETRAJ_OK;
 }
 
 // ---- autotuner of the bulk integrator's launch shape ----------------------------------
@@ -876,12 +888,10 @@ int launch_integrate(etraj_ctx* ctx, const DJob& J, const InitSoA& soa, const do
     if (precision == ETRAJ_PRECISION_FP32_DF) {
         DFParams D;
         prepare_df(J, tmin, max_n, ctx->sm_count, D);
-        float4* tab = nullptr;
-        ETRAJ_TRY(ensure_t(ctx, "field_table_df", (size_t)D.n_int * kDfTableF4, &tab));
-        D.table = tab;
+        ETRAJ_TRY(attach_df(ctx, D));
         DfTableNodes nodes;
         df_table_nodes(nodes);
-        *launches += launch_field_table_df(J, D.T0, D.h_d, D.n_int, nodes, tab, s);
+        *launches += launch_field_table_df(J, D.T0, D.h_d, D.n_int, nodes, (float4*)D.table, s);
         if (ev) rec(ctx, ev[0], s);
         *launches += launch_integrate_df(D, soa, t, idx, count, work, out, s);
         if (ev) rec(ctx, ev[1], s);
@@ -973,8 +983,7 @@ size_t plan_growth(etraj_ctx* ctx, const etraj_job* job) {
     if (job->precision == ETRAJ_PRECISION_FP32_DF) {
         DFParams D;
         prepare_df_params(H.J, H.t.front(), H.J.n_total, D);
-        float4* tab = nullptr;
-        ensure_t(ctx, "field_table_df", (size_t)D.n_int * kDfTableF4, &tab);
+        attach_df(ctx, D);
     }
     if (bulk) {
         BulkParams B;
@@ -1032,16 +1041,17 @@ int enqueue_kernels_maybe_graph(etraj_ctx* ctx, const etraj_job* job, const Host
         ETRAJ_TRY(attach_park(ctx, B));
     }
     if (use_graph && job->precision == ETRAJ_PRECISION_FP32_DF) {
-        DFParams D;  // allocate the field table outside the capture
+        DFParams D;  // allocate the field table and the carry buffer outside the capture
         prepare_df_params(J, H.t.front(), J.n_total, D);
         n_int = (size_t)D.n_int;
-        float4* tab = nullptr;
-        ETRAJ_TRY(ensure_t(ctx, "field_table_df", n_int * kDfTableF4, &tab));
+        ETRAJ_TRY(attach_df(ctx, D));
     }
     if (!use_graph) return enqueue_kernels(ctx, job, H, P, launches);
     const char* tab_name = (job->precision == ETRAJ_PRECISION_FP32_DF) ? "field_table_df" : "field_table";
-    void* tab_ptr = ctx->bufs.count(tab_name) ? ctx->bufs[tab_name].p : nullptr;
-    std::vector<unsigned char> key(sizeof J + sizeof P + sizeof(int) * 3 + sizeof(size_t) + sizeof(void*));
+    const char* aux_name = (job->precision == ETRAJ_PRECISION_FP32_DF) ? "df_carry" : "park";
+    void* ptrs[2] = {ctx->bufs.count(tab_name) ? ctx->bufs[tab_name].p : nullptr,
+                     ctx->bufs.count(aux_name) ? ctx->bufs[aux_name].p : nullptr};
+    std::vector<unsigned char> key(sizeof J + sizeof P + sizeof(int) * 3 + sizeof(size_t) + sizeof ptrs);
     unsigned char* k = key.data();
     std::memcpy(k, &J, sizeof J);
     k += sizeof J;
@@ -1055,7 +1065,7 @@ int enqueue_kernels_maybe_graph(etraj_ctx* ctx, const etraj_job* job, const Host
     k += sizeof extra;
     std::memcpy(k, &n_int, sizeof n_int);
     k += sizeof n_int;
-    std::memcpy(k, &tab_ptr, sizeof tab_ptr);
+    std::memcpy(k, ptrs, sizeof ptrs);
     cudaStream_t s = ctx->stream;
     if (ctx->gexec && key == ctx->gkey) {
         cudaError_t e = cudaGraphLaunch(ctx->gexec, s);

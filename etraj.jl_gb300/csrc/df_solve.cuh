@@ -24,9 +24,19 @@
 // stage sums are (row sum) K_0 + sum a dK.  Only the accepted state itself is
 // rounded to double-float once per step (harmless: it is where the next step
 // starts, not an error the controller sees).  The target's terms at each newly
-// accepted state are evaluated directly, not carried from the step's last
-// stage: summed differences keep absolute errors of the largest r^2 they saw,
-// which relative to r^2 grow without bound as an electron falls to the core.
+// accepted state are evaluated directly (stage 6 always is), not carried as sums
+// of differences: those keep absolute errors of the largest r^2 they saw, which
+// relative to r^2 grow without bound as an electron falls to the core.
+//
+// Differences are needed only where the error estimate cancels that far: in an
+// electron's first attempts, while the last accepted error estimate is below 1e-3
+// (the "start-up" attempts, ~10% of all on the argon jobs of the tests).  There
+// the stages are differences; from the first attempt that follows an estimate
+// above 1e-3 on, each stage's target terms are evaluated directly at x0 + dX
+// (later attempts with small estimates, where the controller is held back by
+// qmax, are another ~7%: taking them directly changed no step count and no
+// status on those jobs), and the sixth stage's direct terms are the new accepted
+// state's.
 //
 // The code compiles for the device and, unchanged, for the host (the CPU tests
 // run it against the FP64 oracle).
@@ -91,6 +101,7 @@ DFS_TABLES(static const)
 
 constexpr double kAbstol = 1e-6, kBeta1 = 0.14, kBeta2 = 0.08, kQminInv = 5.0, kQmaxInv = 0.1, kGamma = 0.9,
                  kQoldInit = 1e-4, kLog2QoldInit = -13.287712379549449;
+constexpr double kLog2Precise = -9.965784284662087;  // log2(1e-3)
 constexpr float kSaeSkip = 50.0f;      // exp(-b r) with b r > 50 (< 2e-22 of the sum it joins) is dropped
 constexpr float kExpm1Small = 1.4e-3f;  // below this |x| exp(x) - 1 is taken from its series
 
@@ -323,32 +334,22 @@ DFS_HD void exp_step(df b, df r_l, df dr, df e0, const float* exptab, df& el, df
     }
 }
 
-// The target's terms T at x0 + dX from those at x0 (B) as differences: the changes
-// dKT of the force and dkph of the phase rate (P0 + dP the stage momentum, kph0 the
-// phase rate at x0).  A stage whose s = r^2 + sc is not within a factor 2 of s_0
-// (passes near the core, where r changes by orders of magnitude within a step) is
-// evaluated directly instead: there y_l = y_0 / b and its kin would be small
-// remainders of cancelling terms, while the step's error estimate, far from the
-// 1e-10 cancellation of the first steps, needs no differences.
+// The changes dKT of the target's force and dkph of the phase rate from x0 (terms B)
+// to x0 + dX (P0 + dP the stage momentum), written as differences.  Returns false,
+// leaving them to a direct evaluation, when s = r^2 + sc is not within a factor 2
+// of s_0 (a pass near the core, where r changes by orders of magnitude within a
+// step): there y_l = y_0 / b and its kin would be small remainders of cancelling
+// terms, while such a step's error estimate needs no differences.
 template <int DIM, int PHASE, int TGT>
-DFS_HD void target_step(const DFParams& P, const float* exptab, const df* X0, const df* P0, const TAt& B,
-                        df kph0, const df* dX, const df* dP, TAt& T, df* dKT, df& dkph) {
+DFS_HD bool target_diff(const DFParams& P, const float* exptab, const df* X0, const df* P0, const TAt& B,
+                        const df* dX, const df* dP, df* dKT, df& dkph) {
+    TAt T;
     // ds = r_l^2 - r_0^2 = 2 x0.dX + dX.dX,  delta = ds / s_0,  b = sqrt(1 + delta)
     df ds = df_add(df_mul(df_f(2.0f), df_mul(X0[0], dX[0])), df_sqr(dX[0]));
     for (int d = 1; d < DIM; ++d) ds = df_add(ds, df_add(df_mul(df_f(2.0f), df_mul(X0[d], dX[d])), df_sqr(dX[d])));
     const df y02 = df_sqr(B.y);
     const df delta = df_mul(ds, y02);
-    if (!(delta.hi >= -0.5f && delta.hi <= 1.0f)) {
-        df Xl[DIM], Pl[DIM], KT[DIM], kph;
-        for (int d = 0; d < DIM; ++d) {
-            Xl[d] = df_add(X0[d], dX[d]);
-            Pl[d] = df_add(P0[d], dP[d]);
-        }
-        target_at<DIM, PHASE, TGT>(P, exptab, Xl, Pl, T, KT, kph);
-        for (int d = 0; d < DIM; ++d) dKT[d] = df_sub(KT[d], df_mul(B.coef, X0[d]));
-        dkph = df_sub(kph, kph0);
-        return;
-    }
+    if (!(delta.hi >= -0.5f && delta.hi <= 1.0f)) return false;
     const df opd = df_add_f(delta, 1.0f);
     const df b = df_sqrt(opd);
     const df bm1 = df_div(delta, df_add_f(b, 1.0f));  // b - 1
@@ -413,6 +414,7 @@ DFS_HD void target_step(const DFParams& P, const float* exptab, const df* X0, co
     } else {
         dkph = df{0.0f, 0.0f};
     }
+    return true;
 }
 
 // ---- one electron ---------------------------------------------------------------------
@@ -423,7 +425,7 @@ struct Lane {
     static constexpr int KW = 2 * DIM + (HASPH ? 2 : 0);  // floats of one stage slot (dK, dkph)
     df X[DIM], Pv[DIM], PH;   // accepted state (position, momentum, phase)
     df K0[DIM], kph0;         // derivative at the accepted state (momentum rows), phase rate
-    TAt B;                    // the target's terms at the accepted state
+    df KT0[DIM];              // the target's force there (coef x)
     FieldAt F0;               // laser table at the accepted state's time
     df dX[DIM], dP[DIM];      // increments of the state to evaluate next
     df dt, dth, dt2, dtprop, dtmax, lqold, q11;
@@ -471,12 +473,13 @@ DFS_HD void load(Lane<DIM, PHASE>& L, const DFParams& P, const double* x0, const
     L.q11 = df_f(1.0f);
 }
 
-// The accepted state's derivative from its target terms (KT = coef X, kph) and laser table.
+// The accepted state's derivative from its target force KT = coef X, phase rate kph
+// and laser table F.
 template <int DIM, int PHASE>
-DFS_HD void set_base(Lane<DIM, PHASE>& L, const FieldAt& F, df kph) {
+DFS_HD void set_base(Lane<DIM, PHASE>& L, const FieldAt& F, const df* KT, df kph) {
     L.F0 = F;
     L.kph0 = kph;
-    for (int d = 0; d < DIM; ++d) L.K0[d] = df_mul(L.B.coef, L.X[d]);
+    for (int d = 0; d < DIM; ++d) L.K0[d] = L.KT0[d] = KT[d];
     L.K0[0] = df_sub(L.K0[0], df_add(c0_df(F.c0x), F.qx));
     L.K0[1] = df_sub(L.K0[1], df_add(c0_df(F.c0y), F.qy));
 }
@@ -618,37 +621,68 @@ struct Acc {
     DFS_HD df get() const { return two_sum(s, e); }
 };
 
-// The increments and clock of stage ST (1..6; 6 is the new state):
+// The increments and clock of stage st (1..6; 6 is the new state):
 // dP = dt ((sum_l A_l) K_0 + sum_l A_l dK_l) and
 // dX = (sum_l A_l) dt p0 + dt^2 ((sum_l (A A)_l) K_0 + sum_l (A A)_l dK_l).
-template <int ST, int DIM, int PHASE, int KW>
-DFS_HD void stage_in(Lane<DIM, PHASE>& L, const Slots<KW>& k) {
-    const df adt = df_mul(DFS_T RA[ST], L.dt);
-#pragma unroll
+// st is the same for every stepping lane of a warp, so the coefficients are
+// uniform constant-memory reads and one copy of the code serves all stages.
+template <int DIM, int PHASE, int KW>
+DFS_HD void stage_in(Lane<DIM, PHASE>& L, const Slots<KW>& k, int st) {
+    const df adt = df_mul(DFS_T RA[st], L.dt);
     for (int d = 0; d < DIM; ++d) {
-        Acc sa(df_mul(DFS_T RA[ST], L.K0[d])), saa(df_mul(DFS_T RAA[ST], L.K0[d]));
-#pragma unroll
-        for (int l = 1; l < ST; ++l) {
+        Acc sa(df_mul(DFS_T RA[st], L.K0[d])), saa(df_mul(DFS_T RAA[st], L.K0[d]));
+        for (int l = 1; l < st; ++l) {
             const df kl = k.get(l, d);
-            sa.add(DFS_T A[ST][l], kl);
-            if (l + 1 < ST) saa.add(DFS_T AA[ST][l], kl);  // (A A)[ST][ST-1] = 0
+            sa.add(DFS_T A[st][l], kl);
+            if (l + 1 < st) saa.add(DFS_T AA[st][l], kl);  // (A A)[st][st-1] = 0
         }
         L.dP[d] = df_mul(L.dt, sa.get());
         L.dX[d] = df_fma(adt, L.Pv[d], df_mul(L.dt2, saa.get()));
     }
-    if (ST < 5) {
-        clk_adv(L.tn, L.tfr, df_mul(DFS_T C[ST], L.dth), L.ni, L.fi);
+    if (st < 5) {
+        clk_adv(L.tn, L.tfr, df_mul(DFS_T C[st], L.dth), L.ni, L.fi);
     } else {
         L.ni = L.n1;
         L.fi = L.f1;
     }
 }
 
+// Whether the coming start-up attempt forms its stages as differences (the last
+// accepted error estimate was below 1e-3); the first attempt for which it does
+// not ends the start-up.
+template <int DIM, int PHASE>
+DFS_HD bool precise(const Lane<DIM, PHASE>& L) {
+    return df_lt(L.lqold, dfc(kLog2Precise));
+}
+
+// One evaluation of the target at x0 + (dX, dP): the change of its terms from the
+// accepted state (dKT, dkph), as differences from its terms B there when wanted
+// (DIFF and diff) and possible, and with direct terms T, KT = coef x and kph at
+// the new point when wanted (direct) or when the difference was not formed.
+template <int DIM, int PHASE, int TGT, bool DIFF>
+DFS_HD void target_eval(const DFParams& P, const float* exptab, const Lane<DIM, PHASE>& L, const TAt& B, bool diff,
+                        bool direct, TAt& T, df* KT, df* dKT, df& dkph, df& kph) {
+    bool ok = false;
+    if (DIFF && diff) ok = target_diff<DIM, PHASE, TGT>(P, exptab, L.X, L.Pv, B, L.dX, L.dP, dKT, dkph);
+    if (direct || !ok) {
+        df Xl[DIM], Pl[DIM];
+        for (int d = 0; d < DIM; ++d) {
+            Xl[d] = df_add(L.X[d], L.dX[d]);
+            Pl[d] = df_add(L.Pv[d], L.dP[d]);
+        }
+        target_at<DIM, PHASE, TGT>(P, exptab, Xl, Pl, T, KT, kph);
+        if (!ok) {
+            for (int d = 0; d < DIM; ++d) dKT[d] = df_sub(KT[d], L.KT0[d]);
+            dkph = df_sub(kph, L.kph0);
+        }
+    }
+}
+
 // After the evaluation of stage 6 (slot 6): error estimate, controller and the
 // decision (the bottom of solve()'s loop).  Returns -1 when t_final is reached, a
 // status > 0 on failure (3 Unstable, 4 DtNaN), 0 to go on; after an accepted step
-// that goes on (L.accept) the caller evaluates the new state's target terms
-// (target_at) and passes them to set_base with the laser table L.F5.
+// that goes on (L.accept) the caller makes stage 6's direct target terms the new
+// state's (set_base with the laser table L.F5).
 template <int DIM, int PHASE, int KW>
 DFS_HD int epilogue(Lane<DIM, PHASE>& L, const DFParams& P, const Slots<KW>& k, const Tabs& T) {
     constexpr bool HASPH = Lane<DIM, PHASE>::HASPH;
@@ -724,6 +758,83 @@ DFS_HD int epilogue(Lane<DIM, PHASE>& L, const DFParams& P, const Slots<KW>& k, 
     const df rem = df_mul(df_add(df_f((float)(P.nf - L.tn)), df_sub(d2(P.ff), L.tfr)), d2(P.h));
     if (rem.hi < P.t_snap) return -1;
     return bad ? 3 : 0;
+}
+
+// ---- the start-up pass's hand-over -----------------------------------------------------
+// An electron leaves the start-up pass at the first attempt boundary where its
+// last accepted error estimate is not below 1e-3 (always right after an accepted
+// step): word w of carried electron k at c[w * cap + k].  What it carries is what
+// the next attempt reads; the main pass evaluates the target and the laser at the
+// state again, which gives the bits stage 6 gave (x + 0 is x).
+struct Carry {
+    float* c;
+    int64_t cap;
+    DFS_HD float& w(int i, int64_t k) const { return c[(int64_t)i * cap + k]; }
+    DFS_HD void put(int& i, int64_t k, df v) const {
+        w(i++, k) = v.hi;
+        w(i++, k) = v.lo;
+    }
+    DFS_HD df take(int& i, int64_t k) const {
+        const df v{w(i, k), w(i + 1, k)};
+        i += 2;
+        return v;
+    }
+    DFS_HD void put_i(int& i, int64_t k, uint32_t v) const {
+        uint32_t* u = reinterpret_cast<uint32_t*>(c);
+        u[(int64_t)(i++) * cap + k] = v;
+    }
+    DFS_HD uint32_t take_i(int& i, int64_t k) const {
+        const uint32_t* u = reinterpret_cast<const uint32_t*>(c);
+        return u[(int64_t)(i++) * cap + k];
+    }
+};
+
+template <int DIM, int PHASE>
+DFS_HD void save_carry(const Lane<DIM, PHASE>& L, const Carry& C, int64_t k, uint64_t s) {
+    int i = 0;
+    for (int d = 0; d < DIM; ++d) {
+        C.put(i, k, L.X[d]);
+        C.put(i, k, L.Pv[d]);
+    }
+    C.put(i, k, L.PH);
+    C.put(i, k, L.tfr);
+    C.put(i, k, L.dtprop);
+    C.put(i, k, L.dtmax);
+    C.put(i, k, L.lqold);
+    C.w(i++, k) = L.dtmin;
+    C.put_i(i, k, (uint32_t)L.tn);
+    C.put_i(i, k, (uint32_t)L.iter);
+    C.put_i(i, k, (uint32_t)L.attempts);
+    C.put_i(i, k, (uint32_t)s);
+    C.put_i(i, k, (uint32_t)(s >> 32));
+}
+
+// Restores carried electron k; returns its index.  The target and laser at the
+// state are evaluated next (dX = dP = 0 at clock tn + tfr).
+template <int DIM, int PHASE>
+DFS_HD uint64_t restore_carry(Lane<DIM, PHASE>& L, const Carry& C, int64_t k) {
+    int i = 0;
+    for (int d = 0; d < DIM; ++d) {
+        L.X[d] = C.take(i, k);
+        L.Pv[d] = C.take(i, k);
+        L.dX[d] = df_f(0.0f);
+        L.dP[d] = df_f(0.0f);
+    }
+    L.PH = C.take(i, k);
+    L.tfr = L.fi = C.take(i, k);
+    L.dtprop = L.dt = C.take(i, k);
+    L.dtmax = C.take(i, k);
+    L.lqold = C.take(i, k);
+    L.dtmin = C.w(i++, k);
+    L.tn = L.ni = (int)C.take_i(i, k);
+    L.iter = (int)C.take_i(i, k);
+    L.attempts = (int)C.take_i(i, k);
+    const uint64_t lo = C.take_i(i, k);
+    const uint64_t hi = C.take_i(i, k);
+    L.accept = true;
+    L.last = false;
+    L.q11 = df_f(1.0f);
+    return lo | (hi << 32);
 }
 
 template <int DIM, int PHASE>

@@ -264,9 +264,12 @@ struct DFParams {
     float t_snap;         // 100 ulp of t_final: a step ending closer than this ends the solve
     float2 Z, Ip, sc, a1, b1, a2, b2, a3, b3, a2b2;
     int max_iters;
-    int threads, blocks;  // launch shape (persistent grid)
+    int threads, blocks;    // launch shape of the start-up pass (persistent grid)
+    int blocks_main;        // blocks of the main pass (threads each)
     int64_t max_n;
+    float* carry;           // kDfCarryWords x max_n words: electrons passed to the main pass
 };
+constexpr int kDfCarryWords = 32;        // words of one carried electron (at most 29 used)
 constexpr int kDfTablePerPeriod = 1024;  // table intervals per shortest laser period
 constexpr int kDfTableF4 = 7;            // float4 per table interval
 // Chebyshev nodes of a field-table piece and the values of T_0..T_7 there
@@ -276,13 +279,16 @@ struct DfTableNodes {
 };
 int launch_field_table_df(const DJob& J, double T0, double h, int n_int, const DfTableNodes& nodes, float4* tab,
                           cudaStream_t s);
-// Work-stealing double-float Tsit5 solve of the survivors; writes out.final_state
-// (FP64), out.status and out.steps, for launch_collect_fp64.
+// Work-stealing double-float Tsit5 solve of the survivors in two passes (an
+// electron's first steps, whose error estimates need stage differences, then the
+// rest); writes out.final_state (FP64), out.status and out.steps, for
+// launch_collect_fp64.  work: three counters (start-up queue, carried electrons,
+// main-pass queue).
 int launch_integrate_df(const DFParams& P, InitSoA soa, const double* t, const int64_t* idx,
-                        const unsigned long long* count, unsigned long long* queue, TrajOut out,
+                        const unsigned long long* count, unsigned long long* work, TrajOut out,
                         cudaStream_t s);
-// Resident blocks per SM of a double-float integrator variant (threads per block given).
-int df_blocks_per_sm(int dim, int phase, int tgt, int threads);
+// Resident blocks per SM of a double-float integrator pass (main: the main pass).
+int df_blocks_per_sm(int dim, int phase, int tgt, bool main, int threads);
 
 // Deterministic deposit: stable radix sort of (key, survivor) and segmented sums.
 struct DepositScratch {

@@ -1,7 +1,9 @@
 // integrate_df.cu -- the double-float integrator: persistent, warp-cooperative,
 // work-stealing Tsit5 on the FP32 pipe with every stage value, sum, error
-// estimate and controller power a double-float pair (dfloat.h), each stage
-// formed as a difference from the accepted state (df_solve.cuh).
+// estimate and controller power a double-float pair (dfloat.h).  Two passes: a
+// start-up pass over an electron's first steps, whose stages are formed as
+// differences from the accepted state (df_solve.cuh), and a main pass, every
+// stage evaluated directly, over the electrons the start-up hands on.
 //
 // It restates the plain FP64 solve of integrate_fp64.cu step for step, so it
 // takes the FP64 path's step sequence and its final states agree with the FP64
@@ -15,13 +17,18 @@
 // Schedule.  A warp advances its lanes stage by stage in lock-step: a counter
 // st = 1..6 shared by the warp selects the Tsit5 stage every stepping lane
 // evaluates, and each turn of the loop makes exactly one right-hand-side
-// evaluation, so the kernel holds one copy of that (long) double-float code and
-// the instruction cache keeps it.  The stage differences of the attempt live in
+// evaluation site, so the kernel holds one copy of that (long) double-float code
+// and the instruction cache keeps it.  The stage differences of the attempt live in
 // shared memory (6 slots per lane).  At each attempt boundary (st = 1) lanes that
 // finished take new electrons from a global queue (warp-aggregated atomicAdd); a
 // new electron spends the first two turns on its starting step and joins the
 // stepping lanes at the next boundary.  The laser table at the end of the
-// attempt (stage 5) serves stage 6 and the new accepted state too.
+// attempt (stage 5) serves stage 6 and the new accepted state too, whose target
+// terms are stage 6's.  The start-up pass hands an electron on at the first
+// boundary where it needs no differences (to a list, warp-aggregated atomicAdd);
+// a main-pass lane that takes one spends one turn evaluating its state.  Since
+// ~90% of the attempts run in the main pass, no warp there carries the longer
+// difference code for one lane, and it is not compiled into that pass.
 //
 // Field table.  F(t) is one function of time for every electron, tabulated once
 // per job in FP64: pieces of width h = T_min/1024 (T_min the shortest laser
@@ -46,19 +53,30 @@ __device__ const float g_df_rcpc[2 * kLogTabN] = {ETRAJ_DF_RCPC_TABLE};
 namespace {
 
 constexpr int kDfThreads = 128;
+// Resident 128-thread blocks per SM the passes' register budgets are set for (168
+// and 128 registers a thread; a few hundred bytes spill).  On the argon headline
+// job (4.0e6 electrons) the budgets (1, 1), (2, 3), (3, 4), (4, 4) and (4, 5) took
+// 139, 104, 99, 103 and 107 ms, with identical results.
+constexpr int kDfMinBlocksStart = 3;
+constexpr int kDfMinBlocksMain = 4;
 
 template <int DIM, int PHASE>
 constexpr int slot_floats() {
     return 6 * dfs::Lane<DIM, PHASE>::KW;
 }
 
-enum LaneMode { kFree = 0, kInit0 = 1, kInit1 = 2, kWait = 3, kStep = 4 };
+enum LaneMode { kFree = 0, kBase = 1, kInit1 = 2, kWait = 3, kStep = 4 };
 
-template <int DIM, int PHASE, int TGT>
-__global__ void __launch_bounds__(kDfThreads)
+// MAIN = false: the start-up pass, from the initial conditions (the starting
+// step's two evaluations, then attempts whose stages are differences) to each
+// electron's first attempt that needs no differences, where it is carried over;
+// MAIN = true: the main pass over the carried electrons, every stage direct.
+// work[0] and work[2] are the passes' queues, work[1] counts carried electrons.
+template <int DIM, int PHASE, int TGT, bool MAIN>
+__global__ void __launch_bounds__(kDfThreads, MAIN ? kDfMinBlocksMain : kDfMinBlocksStart)
 k_integrate_df(const __grid_constant__ DFParams P, InitSoA soa, const double* __restrict__ tsamp,
                const int64_t* __restrict__ idx, const unsigned long long* __restrict__ count,
-               unsigned long long* __restrict__ queue, TrajOut out) {
+               unsigned long long* __restrict__ work, TrajOut out) {
     using LaneT = dfs::Lane<DIM, PHASE>;
     constexpr int KW = LaneT::KW;
     constexpr int N = LaneT::N;
@@ -72,12 +90,16 @@ k_integrate_df(const __grid_constant__ DFParams P, InitSoA soa, const double* __
     __syncthreads();
     const dfs::Tabs T{s_exp2, s_log2c, s_rcpc};
     const dfs::Slots<KW> ks{s_slots + threadIdx.x, (int)blockDim.x};
+    const dfs::Carry C{P.carry, P.max_n};
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned lt_mask = (1u << lane) - 1u;
-    const unsigned long long n_traj = *count;
+    unsigned long long* queue = work + (MAIN ? 2 : 0);
+    unsigned long long* n_carried = work + 1;
+    const unsigned long long n_traj = MAIN ? *n_carried : *count;
 
     LaneT L = {};
+    dfs::TAt B;  // the target's terms at the accepted state (start-up: for the differences)
     int mode = kFree;
     unsigned long long s = 0;
     bool drained = false;
@@ -94,8 +116,22 @@ k_integrate_df(const __grid_constant__ DFParams P, InitSoA soa, const double* __
 
     for (int st = 1;; st = (st == 6) ? 1 : st + 1) {
         if (st == 1) {
-            // ---- attempt boundary: start the next attempts, refill free lanes ----------
+            // ---- attempt boundary: hand over, start the next attempts, refill ------------
             if (mode == kWait) mode = kStep;
+            if (!MAIN) {
+                const bool leave = (mode == kStep) && !dfs::precise(L);
+                const unsigned lm = __ballot_sync(FULL, leave);
+                if (lm) {
+                    const int leader = __ffs(lm) - 1;
+                    unsigned long long k0 = 0ull;
+                    if (lane == leader) k0 = atomicAdd(n_carried, (unsigned long long)__popc(lm));
+                    k0 = __shfl_sync(FULL, k0, leader);
+                    if (leave) {
+                        dfs::save_carry(L, C, (int64_t)(k0 + __popc(lm & lt_mask)), s);
+                        mode = kFree;
+                    }
+                }
+            }
             if (mode == kStep) {
                 const int status = dfs::prologue(L, P);
                 if (status) finish(status);
@@ -108,69 +144,65 @@ k_integrate_df(const __grid_constant__ DFParams P, InitSoA soa, const double* __
                 base = __shfl_sync(FULL, base, leader);
                 drained = base + (unsigned long long)__popc(freem) >= n_traj;
                 if (mode == kFree) {
-                    s = base + __popc(freem & lt_mask);
-                    if (s < n_traj) {
-                        const int64_t g = idx ? idx[s] : (int64_t)s;
-                        double x0[DIM], p0[DIM];
-                        x0[0] = soa.x[g];
-                        x0[1] = soa.y[g];
-                        p0[0] = soa.kx[g];
-                        p0[1] = soa.ky[g];
-                        if (DIM == 3) {
-                            x0[2] = 0.0;
-                            p0[2] = soa.kz[g];
+                    const unsigned long long k = base + __popc(freem & lt_mask);
+                    if (k < n_traj) {
+                        if (MAIN) {
+                            s = dfs::restore_carry(L, C, (int64_t)k);
+                        } else {
+                            s = k;
+                            const int64_t g = idx ? idx[s] : (int64_t)s;
+                            double x0[DIM], p0[DIM];
+                            x0[0] = soa.x[g];
+                            x0[1] = soa.y[g];
+                            p0[0] = soa.kx[g];
+                            p0[1] = soa.ky[g];
+                            if (DIM == 3) {
+                                x0[2] = 0.0;
+                                p0[2] = soa.kz[g];
+                            }
+                            dfs::load(L, P, x0, p0, LaneT::HASPH ? soa.phase[g] : 0.0, tsamp[soa.batch[g]]);
                         }
-                        dfs::load(L, P, x0, p0, LaneT::HASPH ? soa.phase[g] : 0.0, tsamp[soa.batch[g]]);
-                        mode = kInit0;
+                        mode = kBase;
                     }
                 }
             }
             if (__ballot_sync(FULL, mode != kFree) == 0u) break;
         }
         // ---- the inputs of this turn's evaluation ------------------------------------------
-        if (mode == kStep) {
-            switch (st) {
-                case 1: dfs::stage_in<1>(L, ks); break;
-                case 2: dfs::stage_in<2>(L, ks); break;
-                case 3: dfs::stage_in<3>(L, ks); break;
-                case 4: dfs::stage_in<4>(L, ks); break;
-                case 5: dfs::stage_in<5>(L, ks); break;
-                default: dfs::stage_in<6>(L, ks); break;
-            }
-        }
-        // ---- one stage evaluation: the laser table and the target's change from the
-        //      accepted state ---------------------------------------------------------------
-        bool base = (mode == kInit0);  // evaluate the target directly at the accepted state
-        if (mode == kStep || mode == kInit1) {
-            dfs::FieldAt F;
+        if (mode == kStep) dfs::stage_in(L, ks, st);
+        // ---- one evaluation: the laser table, and the target's terms at the new point
+        //      directly (an accepted state: a new electron's, stage 6's; every stage of
+        //      the main pass) and/or as the change from the accepted state (start-up) ------
+        if (mode == kStep || mode == kInit1 || mode == kBase) {
             const bool step6 = (mode == kStep && st == 6);
+            dfs::FieldAt F;
             if (step6) F = L.F5;  // stage 6 is at stage 5's time
             else dfs::field_at(P, L.ni, L.fi, F);
+            const bool diff = !MAIN && mode != kBase;
             dfs::TAt Tl;
-            df dKT[DIM], dkph;
-            dfs::target_step<DIM, PHASE, TGT>(P, T.exp2, L.X, L.Pv, L.B, L.kph0, L.dX, L.dP, Tl, dKT, dkph);
-            dfs::set_diff(L, ks, (mode == kInit1) ? 1 : st, F, dKT, dkph);
-            if (mode == kInit1) {
-                dfs::init_second(L, P, ks, T);
-                mode = kWait;
-            } else if (st == 5) {
-                L.F5 = F;
-            } else if (step6) {
-                const int status = dfs::epilogue(L, P, ks, T);
-                if (status) finish(status < 0 ? 0 : status);
-                else base = L.accept;
+            df KT[DIM], dKT[DIM], dkph, kph;
+            dfs::target_eval<DIM, PHASE, TGT, !MAIN>(P, T.exp2, L, B, diff, !diff || step6, Tl, KT, dKT, dkph, kph);
+            if (mode == kBase) {
+                if (!MAIN) B = Tl;
+                dfs::set_base(L, F, KT, kph);
+                mode = (!MAIN && dfs::init_first(L, P)) ? kInit1 : kWait;
+            } else {
+                dfs::set_diff(L, ks, (mode == kInit1) ? 1 : st, F, dKT, dkph);
+                if (mode == kInit1) {
+                    dfs::init_second(L, P, ks, T);
+                    mode = kWait;
+                } else if (st == 5) {
+                    L.F5 = F;
+                } else if (step6) {
+                    const int status = dfs::epilogue(L, P, ks, T);
+                    if (status) {
+                        finish(status < 0 ? 0 : status);
+                    } else if (L.accept) {
+                        if (!MAIN) B = Tl;
+                        dfs::set_base(L, L.F5, KT, kph);
+                    }
+                }
             }
-        }
-        // ---- the target at a new accepted state (a new electron's, or the end of an
-        //      accepted step) ------------------------------------------------------------------
-        if (base) {
-            dfs::FieldAt F;
-            if (mode == kInit0) dfs::field_at(P, L.ni, L.fi, F);
-            else F = L.F5;
-            df KT[DIM], kph;
-            dfs::target_at<DIM, PHASE, TGT>(P, T.exp2, L.X, L.Pv, L.B, KT, kph);
-            dfs::set_base(L, F, kph);
-            if (mode == kInit0) mode = dfs::init_first(L, P) ? kInit1 : kWait;
         }
     }
 }
@@ -184,19 +216,22 @@ __global__ void k_field_table_df(const __grid_constant__ DJob J, double T0, doub
 
 template <int DIM, int PHASE, int TGT>
 int launch_df_t(const DFParams& P, InitSoA soa, const double* t, const int64_t* idx, const unsigned long long* count,
-                unsigned long long* queue, TrajOut out, cudaStream_t s) {
+                unsigned long long* work, TrajOut out, cudaStream_t s) {
     const size_t smem = (size_t)slot_floats<DIM, PHASE>() * sizeof(float) * (size_t)P.threads;
-    cudaMemsetAsync(queue, 0, sizeof(unsigned long long), s);
-    k_integrate_df<DIM, PHASE, TGT><<<P.blocks, P.threads, smem, s>>>(P, soa, t, idx, count, queue, out);
-    return 1;
+    cudaMemsetAsync(work, 0, 3 * sizeof(unsigned long long), s);
+    k_integrate_df<DIM, PHASE, TGT, false><<<P.blocks, P.threads, smem, s>>>(P, soa, t, idx, count, work, out);
+    k_integrate_df<DIM, PHASE, TGT, true><<<P.blocks_main, P.threads, smem, s>>>(P, soa, t, idx, count, work, out);
+    return 2;
 }
 
 template <int DIM, int PHASE, int TGT>
-int blocks_t(int threads) {
+int blocks_t(bool main, int threads) {
     const size_t smem = (size_t)slot_floats<DIM, PHASE>() * sizeof(float) * (size_t)threads;
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_integrate_df<DIM, PHASE, TGT>, threads, smem) !=
-        cudaSuccess) {
+    const cudaError_t e =
+        main ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_integrate_df<DIM, PHASE, TGT, true>, threads, smem)
+             : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_integrate_df<DIM, PHASE, TGT, false>, threads, smem);
+    if (e != cudaSuccess) {
         cudaGetLastError();
         return 1;
     }
@@ -232,12 +267,14 @@ int launch_field_table_df(const DJob& J, double T0, double h, int n_int, const D
                                              : FN<3, ETRAJ_PHASE_SCTS, ETRAJ_TARGET_SAE> ARGS;
 
 int launch_integrate_df(const DFParams& P, InitSoA soa, const double* t, const int64_t* idx,
-                        const unsigned long long* count, unsigned long long* queue, TrajOut out, cudaStream_t s) {
+                        const unsigned long long* count, unsigned long long* work, TrajOut out, cudaStream_t s) {
     const int dim = P.dim, phase = P.phase, tgt = P.tgt;
-    ETRAJ_DF_DISPATCH(launch_df_t, (P, soa, t, idx, count, queue, out, s))
+    ETRAJ_DF_DISPATCH(launch_df_t, (P, soa, t, idx, count, work, out, s))
 }
 
-int df_blocks_per_sm(int dim, int phase, int tgt, int threads) { ETRAJ_DF_DISPATCH(blocks_t, (threads)) }
+int df_blocks_per_sm(int dim, int phase, int tgt, bool main, int threads) {
+    ETRAJ_DF_DISPATCH(blocks_t, (main, threads))
+}
 
 #undef ETRAJ_DF_DISPATCH
 

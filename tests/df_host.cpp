@@ -2,7 +2,9 @@
 // (etraj.jl_gb300/csrc/df_solve.cuh, the code the device kernel runs) for
 // tests/test_df_host.py, which checks it against the FP64 oracle on the CPU.
 // One electron after another: load, the starting step's two evaluations, then
-// prologue, six stages and epilogue per attempt, as a lane of the kernel does.
+// prologue, six stages and epilogue per attempt, as a lane of the kernel does
+// (stage 6's direct target terms become the next accepted state's), with the
+// hand-over from the start-up pass to the main pass at the same boundary.
 #include <vector>
 
 #include "df_solve.cuh"
@@ -26,46 +28,54 @@ void solve_all(const DFParams& P, int64_t n, const double* init, double* final_s
         double x0[3] = {r[0], r[1], 0.0}, p0[3] = {0.0, 0.0, 0.0};
         for (int d = 0; d < DIM; ++d) p0[d] = r[DIM + d];
         const double t0 = r[2 * DIM], ph0 = LaneT::HASPH ? r[rows - 1] : 0.0;
-        float slots[6 * KW];
+        float slots[6 * KW], carry[kDfCarryWords];
         const dfs::Slots<KW> ks{slots, 1};
+        const dfs::Carry Cw{carry, 1};
         LaneT L = {};
-        dfs::load(L, P, x0, p0, ph0, t0);
+        dfs::TAt B, Tl;
         dfs::FieldAt F;
-        df KT[DIM], dKT[DIM], kph = df{0.0f, 0.0f};
-        dfs::TAt Tl;
+        df KT[DIM], dKT[DIM], dkph, kph;
+        // start-up pass: the starting step, then attempts with stage differences
+        dfs::load(L, P, x0, p0, ph0, t0);
         dfs::field_at(P, L.ni, L.fi, F);
-        dfs::target_at<DIM, PHASE, TGT>(P, T.exp2, L.X, L.Pv, L.B, KT, kph);
-        dfs::set_base(L, F, kph);
+        dfs::target_eval<DIM, PHASE, TGT, true>(P, T.exp2, L, B, false, true, Tl, KT, dKT, dkph, kph);
+        B = Tl;
+        dfs::set_base(L, F, KT, kph);
         if (dfs::init_first(L, P)) {
             dfs::field_at(P, L.ni, L.fi, F);
-            dfs::target_step<DIM, PHASE, TGT>(P, T.exp2, L.X, L.Pv, L.B, L.kph0, L.dX, L.dP, Tl, dKT, kph);
-            dfs::set_diff(L, ks, 1, F, dKT, kph);
+            dfs::target_eval<DIM, PHASE, TGT, true>(P, T.exp2, L, B, true, false, Tl, KT, dKT, dkph, kph);
+            dfs::set_diff(L, ks, 1, F, dKT, dkph);
             dfs::init_second(L, P, ks, T);
         }
         int st = 0;
+        bool main = false;
         while (true) {
+            if (!main && !dfs::precise(L)) {
+                // hand-over to the main pass, through the carry words as on the device
+                dfs::save_carry(L, Cw, 0, (uint64_t)i);
+                L = LaneT{};
+                dfs::restore_carry(L, Cw, 0);
+                dfs::field_at(P, L.ni, L.fi, F);
+                dfs::target_eval<DIM, PHASE, TGT, false>(P, T.exp2, L, B, false, true, Tl, KT, dKT, dkph, kph);
+                dfs::set_base(L, F, KT, kph);
+                main = true;
+            }
             st = dfs::prologue(L, P);
             if (st) break;
             for (int s = 1; s <= 6; ++s) {
-                switch (s) {
-                    case 1: dfs::stage_in<1>(L, ks); break;
-                    case 2: dfs::stage_in<2>(L, ks); break;
-                    case 3: dfs::stage_in<3>(L, ks); break;
-                    case 4: dfs::stage_in<4>(L, ks); break;
-                    case 5: dfs::stage_in<5>(L, ks); break;
-                    default: dfs::stage_in<6>(L, ks); break;
-                }
+                dfs::stage_in(L, ks, s);
                 if (s == 6) F = L.F5;  // stage 6 is at stage 5's time
                 else dfs::field_at(P, L.ni, L.fi, F);
-                dfs::target_step<DIM, PHASE, TGT>(P, T.exp2, L.X, L.Pv, L.B, L.kph0, L.dX, L.dP, Tl, dKT, kph);
-                dfs::set_diff(L, ks, s, F, dKT, kph);
+                dfs::target_eval<DIM, PHASE, TGT, true>(P, T.exp2, L, B, !main, main || s == 6, Tl, KT, dKT, dkph,
+                                                        kph);
+                dfs::set_diff(L, ks, s, F, dKT, dkph);
                 if (s == 5) L.F5 = F;
             }
             st = dfs::epilogue(L, P, ks, T);
             if (st) break;
             if (L.accept) {
-                dfs::target_at<DIM, PHASE, TGT>(P, T.exp2, L.X, L.Pv, L.B, KT, kph);
-                dfs::set_base(L, L.F5, kph);
+                B = Tl;
+                dfs::set_base(L, L.F5, KT, kph);
             }
         }
         status[i] = st < 0 ? 0 : st;
