@@ -122,3 +122,32 @@ def test_python_mirror_rejects_what_the_reference_rejects():
         et.HydrogenLikeAtom(Ip=-0.5, Z=1)
     with pytest.raises(KeyError):
         et.get_atom("Xe", 2)
+
+
+def test_julia_binding_structs_are_generated_and_match_c(tmp_path):
+    """The Julia structs of the ccall binding are the generator's
+    output for include/etraj.h, and their layout is the C compiler's."""
+    from etraj_gb300 import julia_structs as J
+
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    assert J.julia_structs() in text
+    layout = J.julia_layout()
+    parsed = J.parse_header()
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "etraj.h"', "int main(void){"]
+    for st, _ in J.STRUCTS:
+        lines.append('printf("%s %%zu\\n", sizeof(%s));' % (st, st))
+        for f, _, _, _ in parsed[st]:
+            lines.append('printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (st, f, st, f))
+    lines.append("return 0;}")
+    src = tmp_path / "jprobe.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "jprobe"
+    subprocess.run(["gcc", "-I" + os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = dict(l.rsplit(" ", 1) for l in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                        check=True).stdout.split("\n") if l)
+    for st, _ in J.STRUCTS:
+        size, offs = layout[st]
+        assert int(out[st]) == size, st
+        assert [f for f, _, _, _ in parsed[st]] == list(offs), st
+        for f, o in offs.items():
+            assert int(out["%s.%s" % (st, f)]) == o, (st, f)
