@@ -6,24 +6,37 @@ the source says; the explicit fma() calls in detmath.h stay fused.  The same
 flags are used on x86-64 and aarch64.
 """
 import os
+import re
 import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboracle.so")
-SOURCES = ["oracle_physics.c", "oracle_sampler.c", "oracle_solve.c"]
-HEADERS = ["oracle.h", "oracle_internal.h", "oracle_sampler.h",
-           os.path.join("..", "etraj.jl_gb300", "csrc", "detmath.h"),
-           os.path.join("..", "include", "etraj.h")]
+SOURCES = ["oracle_physics.c", "oracle_sampler.c", "oracle_solve.c", "oracle_spa_ref.c"]
+
+
+def _headers():
+    """Every header the sources reach through quoted #includes (the oracle's own
+    and those it shares with the device code), so that an edit to any of them
+    rebuilds the library."""
+    seen, todo = set(), [os.path.join(HERE, s) for s in SOURCES]
+    while todo:
+        path = todo.pop()
+        for inc in re.findall(r'^\s*#\s*include\s+"([^"]+)"', open(path).read(), flags=re.M):
+            dep = os.path.normpath(os.path.join(os.path.dirname(path), inc))
+            if dep not in seen and os.path.exists(dep):
+                seen.add(dep)
+                todo.append(dep)
+    return sorted(seen)
 
 
 def _stale():
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
-    deps = SOURCES + HEADERS + [os.path.basename(__file__)]
-    return any(os.path.getmtime(os.path.join(HERE, d)) > t for d in deps)
+    deps = [os.path.join(HERE, s) for s in SOURCES] + _headers() + [os.path.abspath(__file__)]
+    return any(os.path.getmtime(d) > t for d in deps)
 
 
 def build(force=False, verbose=False):

@@ -72,6 +72,9 @@ double oracle_hartree_asymp_coeff(int Z, double Ip, int l);
  * process-wide switch (default on) used to show the skip changes nothing */
 int oracle_sae_skip_exact(const etraj_target* target);
 void oracle_set_sae_skip(int enable);
+/* SPA candidates from the independent restatement (oracle_spa_ref.c: C library
+ * functions, its own solver and quadrature) instead of the device's twin */
+void oracle_set_spa_independent(int on);
 void oracle_rhs(const etraj_job* job, double t, const double* u, double* du);
 void oracle_detmath(int fn, int64_t n, const double* x, const double* y, double* out);
 void oracle_tsit5_tableau(double* c, double* a, double* btilde);

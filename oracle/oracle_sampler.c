@@ -303,7 +303,7 @@ void o_batch_prepare(const o_sampler* S, int64_t b, o_batch* B) {
 
 /* Sum over m' of C * D^l_{m' m} * Y_{l m'}(k_ts rotated to the field frame),
  * the numerator of pre() (ADKSampler.jl:243-265). */
-static dm_cplx o_pre_numerator(const o_sampler* S, const o_batch* B, dm_cplx kx, dm_cplx ky, dm_cplx kz) {
+dm_cplx o_pre_numerator(const o_sampler* S, const o_batch* B, dm_cplx kx, dm_cplx ky, dm_cplx kz) {
     /* new_k = conj(k_ts) . axis (LinearAlgebra.dot conjugates its first argument) */
     dm_cplx ckx = dm_cconj(kx), cky = dm_cconj(ky), ckz = dm_cconj(kz);
     dm_cplx nkx = dm_cadd(dm_cadd(dm_cscale(ckx, 0.0), dm_cscale(cky, 0.0)), dm_cscale(ckz, 1.0));
@@ -497,6 +497,11 @@ void o_mc_point(const o_sampler* S, int64_t b, int64_t i, double* kd0, double* k
     }
 }
 
+/* which SPA candidate the sampler runs: the twin of the device's (spa.h, 0) or
+ * the independent restatement of oracle_spa_ref.c (1) */
+static int g_spa_independent = 0;
+void oracle_set_spa_independent(int on) { g_spa_independent = on; }
+
 int64_t o_sample_batch(const o_sampler* S, int64_t b, double* init, int64_t capacity) {
     static __thread o_batch B;  /* about 8 KB with the molecular tables: off the stack */
     o_batch_prepare(S, b, &B);
@@ -512,7 +517,8 @@ int64_t o_sample_batch(const o_sampler* S, int64_t b, double* init, int64_t capa
         } else {
             o_mc_point(S, b, i, &kd0, &kz0);
         }
-        const int kept = spa ? o_candidate_spa(S, &B, kd0, kz0, row)
+        const int kept = spa ? (g_spa_independent ? o_candidate_spa_ref(S, &B, kd0, kz0, row)
+                                                  : o_candidate_spa(S, &B, kd0, kz0, row))
                              : S->wfat ? o_candidate_wfat(S, &B, kd0, kz0, row) : o_candidate(S, &B, kd0, kz0, row);
         if (kept) {
             if (count < capacity) memcpy(init + count * S->rows, row, sizeof(double) * (size_t)S->rows);

@@ -44,6 +44,8 @@ void o_sampler_free(o_sampler* S);
 void o_batch_prepare(const o_sampler* S, int64_t b, o_batch* B);
 int o_candidate(const o_sampler* S, const o_batch* B, double kd0, double kz0, double* row);
 int o_candidate_spa(const o_sampler* S, const o_batch* B, double kd0, double kz0, double* row);
+int o_candidate_spa_ref(const o_sampler* S, const o_batch* B, double kd0, double kz0, double* row);
+dm_cplx o_pre_numerator(const o_sampler* S, const o_batch* B, dm_cplx kx, dm_cplx ky, dm_cplx kz);
 int o_candidate_wfat(const o_sampler* S, const o_batch* B, double kd0, double kz0, double* row);
 void o_mc_point(const o_sampler* S, int64_t b, int64_t i, double* kd0, double* kz0);
 int64_t o_sample_batch(const o_sampler* S, int64_t b, double* init, int64_t capacity);

@@ -51,6 +51,7 @@ def lib():
             "oracle_rhs": (None, [_JP, C.c_double, _DP, _DP]),
             "oracle_sae_skip_exact": (C.c_int, [C.c_void_p]),
             "oracle_set_sae_skip": (None, [C.c_int]),
+            "oracle_set_spa_independent": (None, [C.c_int]),
             "oracle_detmath": (None, [C.c_int, C.c_int64, _DP, _DP, _DP]),
             "oracle_tsit5_tableau": (None, [_DP, _DP, _DP]),
         }
@@ -202,6 +203,17 @@ def sae_skip_exact(target_c):
 
 def set_sae_skip(enable):
     lib().oracle_set_sae_skip(1 if enable else 0)
+
+
+class spa_independent:
+    """Within the block the oracle's SPA candidates come from the independent
+    restatement (oracle_spa_ref.c) instead of the device's twin."""
+
+    def __enter__(self):
+        lib().oracle_set_spa_independent(1)
+
+    def __exit__(self, *a):
+        lib().oracle_set_spa_independent(0)
 
 
 def rhs(job, t, u):
