@@ -13,7 +13,7 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboracle.so")
-SOURCES = ["oracle_physics.c", "oracle_sampler.c", "oracle_solve.c", "oracle_spa_ref.c"]
+SOURCES = ["oracle_physics.c", "oracle_sampler.c", "oracle_solve.c", "oracle_spa_ref.c", "oracle_mol_ref.c"]
 
 
 def _headers():

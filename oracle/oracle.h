@@ -75,6 +75,10 @@ void oracle_set_sae_skip(int enable);
 /* SPA candidates from the independent restatement (oracle_spa_ref.c: C library
  * functions, its own solver and quadrature) instead of the device's twin */
 void oracle_set_spa_independent(int on);
+/* molecular prefactor numerators and WFAT rates from the independent
+ * restatement (oracle_mol_ref.c) instead of the device's twin (mol.h) */
+void oracle_set_mol_independent(int on);
+void oracle_mol_wfat_G_ref(const etraj_target* T, int nxi, int m, double theta, double chi, double* out);
 void oracle_rhs(const etraj_job* job, double t, const double* u, double* du);
 void oracle_detmath(int fn, int64_t n, const double* x, const double* y, double* out);
 void oracle_tsit5_tableau(double* c, double* a, double* btilde);

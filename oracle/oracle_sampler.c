@@ -303,13 +303,20 @@ void o_batch_prepare(const o_sampler* S, int64_t b, o_batch* B) {
 
 /* Sum over m' of C * D^l_{m' m} * Y_{l m'}(k_ts rotated to the field frame),
  * the numerator of pre() (ADKSampler.jl:243-265). */
+/* which molecular rate pieces the sampler runs: the twin of the device's
+ * (mol.h, 0) or the independent restatement of oracle_mol_ref.c (1) */
+static int g_mol_independent = 0;
+void oracle_set_mol_independent(int on) { g_mol_independent = on; }
+
 dm_cplx o_pre_numerator(const o_sampler* S, const o_batch* B, dm_cplx kx, dm_cplx ky, dm_cplx kz) {
     /* new_k = conj(k_ts) . axis (LinearAlgebra.dot conjugates its first argument) */
     dm_cplx ckx = dm_cconj(kx), cky = dm_cconj(ky), ckz = dm_cconj(kz);
     dm_cplx nkx = dm_cadd(dm_cadd(dm_cscale(ckx, 0.0), dm_cscale(cky, 0.0)), dm_cscale(ckz, 1.0));
     dm_cplx nky = dm_cadd(dm_cadd(dm_cscale(ckx, B->ny[0]), dm_cscale(cky, B->ny[1])), dm_cscale(ckz, B->ny[2]));
     dm_cplx nkz = dm_cadd(dm_cadd(dm_cscale(ckx, B->nz[0]), dm_cscale(cky, B->nz[1])), dm_cscale(ckz, B->nz[2]));
-    if (S->mol) return mol_numerator(&S->T, B->cd, S->Pmol, nkx, nky, nkz);
+    if (S->mol)
+        return g_mol_independent ? o_mol_numerator_ref(S, B, nkx, nky, nkz)
+                                 : mol_numerator(&S->T, B->cd, S->Pmol, nkx, nky, nkz);
     dm_cplx acc = dm_c(0.0, 0.0);
     for (int mp = -S->l; mp <= S->l; ++mp) {
         dm_cplx Y = dm_cmul(S->Plm[mp + S->l], o_sph_sum(S->l, mp, nkx, nky, nkz));
@@ -466,7 +473,8 @@ int o_candidate_wfat(const o_sampler* S, const o_batch* B, double kd0, double kz
     const double r0 = (S->Ip + (kd0 * kd0 + kz0 * kz0) / 2.0) / F;
     const double x0 = r0 * B->cphi;
     const double y0 = r0 * B->sphi;
-    const double rate = mol_wfat_rate(S->nxi, S->mmax, B->g2, B->A, S->kappa, F, kd0, kz0, S->dkdt);
+    const double rate = g_mol_independent ? o_wfat_rate_ref(S, B, kd0, kz0)
+                                          : mol_wfat_rate(S->nxi, S->mmax, B->g2, B->A, S->kappa, F, kd0, kz0, S->dkdt);
     if (dm_isnan(rate) || rate < S->cutoff) return 0;
     int k = 0;
     row[k++] = x0;

@@ -46,6 +46,8 @@ int o_candidate(const o_sampler* S, const o_batch* B, double kd0, double kz0, do
 int o_candidate_spa(const o_sampler* S, const o_batch* B, double kd0, double kz0, double* row);
 int o_candidate_spa_ref(const o_sampler* S, const o_batch* B, double kd0, double kz0, double* row);
 dm_cplx o_pre_numerator(const o_sampler* S, const o_batch* B, dm_cplx kx, dm_cplx ky, dm_cplx kz);
+dm_cplx o_mol_numerator_ref(const o_sampler* S, const o_batch* B, dm_cplx nkx, dm_cplx nky, dm_cplx nkz);
+double o_wfat_rate_ref(const o_sampler* S, const o_batch* B, double kd, double kz);
 int o_candidate_wfat(const o_sampler* S, const o_batch* B, double kd0, double kz0, double* row);
 void o_mc_point(const o_sampler* S, int64_t b, int64_t i, double* kd0, double* kz0);
 int64_t o_sample_batch(const o_sampler* S, int64_t b, double* init, int64_t capacity);

@@ -48,6 +48,9 @@ def lib():
             "oracle_target_eval": (None, [C.POINTER(abi.Target), C.c_int64, _DP, _DP, _DP]),
             "oracle_hartree_asymp_coeff": (C.c_double, [C.c_int, C.c_double, C.c_int]),
             "oracle_mol_wfat_G": (None, [C.POINTER(abi.Target), C.c_int, C.c_int, C.c_double, C.c_double, _DP]),
+            "oracle_mol_wfat_G_ref": (None, [C.POINTER(abi.Target), C.c_int, C.c_int, C.c_double, C.c_double,
+                                             _DP]),
+            "oracle_set_mol_independent": (None, [C.c_int]),
             "oracle_rhs": (None, [_JP, C.c_double, _DP, _DP]),
             "oracle_sae_skip_exact": (C.c_int, [C.c_void_p]),
             "oracle_set_sae_skip": (None, [C.c_int]),
@@ -243,7 +246,21 @@ def tsit5_tableau():
     return c, a.reshape(7, 6), bt
 
 
-def mol_wfat_G(target, nxi, m, theta, chi):
+def mol_wfat_G(target, nxi, m, theta, chi, independent=False):
+    """G_{n_xi m}(theta, chi) from the device's twin (mol.h) or, with independent,
+    from oracle_mol_ref.c."""
     out = np.zeros(2)
-    lib().oracle_mol_wfat_G(C.byref(target), nxi, m, theta, chi, _p(out))
+    f = lib().oracle_mol_wfat_G_ref if independent else lib().oracle_mol_wfat_G
+    f(C.byref(target), nxi, m, theta, chi, _p(out))
     return complex(out[0], out[1])
+
+
+class mol_independent:
+    """Within the block the oracle's molecular prefactor numerators and WFAT
+    rates come from the independent restatement (oracle_mol_ref.c)."""
+
+    def __enter__(self):
+        lib().oracle_set_mol_independent(1)
+
+    def __exit__(self, *a):
+        lib().oracle_set_mol_independent(0)
