@@ -9,10 +9,16 @@ rtol 1e-6; coherent 1000 x 1000 momentum grid spanning +-2 a.u.
 
 A step is one whole job: sampling, integration, collection and the
 deterministic deposit.  `value` is effective trajectories per second of the
-FP32-bulk path with all buffers resident on the device; `e2e` is the same
-metric through the C ABI's etraj_submit / etraj_wait with host output buffers
-(time samples copied in and the spectrum copied back every step).  The FP64 plain path is run on the same job for the speed ratio and
-the PMD error (relative L2 of |A|^2 against the FP64 result).
+timed path with all buffers resident on the device: by default the
+double-float path (precision fp32_df: Tsit5 stages, field and force as
+double-float pairs on the FP32 pipe, FP64 sampling, collection and deposit),
+which keeps the FP64 path's step sequence and so its momentum distribution
+(PMD); --precision fp32_bulk times the plain-FP32 bulk path instead, which is
+~50x faster again but changes step sequences.  `e2e` is the same metric
+through the C ABI's etraj_submit / etraj_wait with host output buffers (time
+samples copied in and the spectrum copied back every step).  The FP64 plain
+path is run on the same job for the speed ratio and the PMD error (relative L2
+of |A|^2 against the FP64 result); the other FP32 path is reported beside it.
 
 python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 Under torchrun each rank runs its own Monte-Carlo shard (seed = rank):
@@ -101,10 +107,22 @@ WORKLOADS = {
 # 2*(1+2+3+4+5+6)*5 = 210; error estimate 5*(2*7+6) = 100; compensated update
 # 5*8 = 40; clock, controller and bookkeeping ~40.  Total 702 per step attempt.
 FLOPS_PER_STEP_SAE_2D_SCTS = 702
-# DRAM bytes (read + write) of the integrator's round-0 launch per electron on this
-# workload, from one ncu capture of a 2e6-candidate case (24.91 MB for 8.17e5
+# DRAM bytes (read + write) of the bulk integrator's round-0 launch per electron on
+# this workload, from one ncu capture of a 2e6-candidate case (24.91 MB for 8.17e5
 # electrons); traffic grows with the electrons.
 INTEGRATOR_DRAM_BYTES_PER_ELECTRON = 30.48
+# The double-float integrator (start-up and main pass) on the same workload, from one
+# ncu capture of both passes on a 4e5-candidate case (400 time samples: 161,722
+# electrons, 6,489,342 step attempts): FP32 thread instructions
+# (smsp__sass_thread_inst_executed_op_fp32_pred_on: 4.07e9 start-up + 4.463e10
+# main; 71 % FADD, 19 % FFMA, 7 % FMUL) per step attempt, and DRAM bytes (read +
+# write, 14.52 MB + 16.71 MB) per electron.  At that size the carry buffer between
+# the passes (116 B per electron) stays in L2; at full size it adds about that much
+# per electron again.  FMA-pipe issue (sm__inst_executed_pipe_fma, warp
+# instructions against 4 per SM and cycle) was 35.9 % (start-up) and 40.8 % (main).
+DF_FP32_INST_PER_STEP = 7505
+DF_DRAM_BYTES_PER_ELECTRON = 193.1
+DF_FMA_PIPE_ISSUE_NCU = {"start_up": 0.359, "main": 0.408}
 
 
 def rank_env():
@@ -245,8 +263,9 @@ def main():
                          "SPA workload and the small ADK workload")
     ap.add_argument("--t-num", type=int, default=None,
                     help="time samples (default: the workload's full size)")
-    ap.add_argument("--precision", default="fp32_bulk", choices=["fp32_bulk", "fp64"],
-                    help="path timed as `value` (fp64 profiles the plain kernel)")
+    ap.add_argument("--precision", default="fp32_df", choices=["fp32_df", "fp32_bulk", "fp64"],
+                    help="path timed as `value` (fp32_df: the double-float path that keeps the FP64 "
+                         "step sequence; fp32_bulk: plain FP32; fp64 profiles the plain kernel)")
     ap.add_argument("--no-multi-instance", action="store_true",
                     help="skip the 64-instance batched intensity scan")
     ap.add_argument("--no-serving", action="store_true",
@@ -276,10 +295,13 @@ def main():
     # one Monte-Carlo shard per rank (seed = rank), weight 1/world in a merge
     job, shard_w = shards.shard_job(maker(args.precision, seed=0, t_num=args.t_num), rank, world)
     job64, _ = shards.shard_job(maker("fp64", seed=0, t_num=args.t_num), rank, world)
+    other = {"fp32_df": "fp32_bulk", "fp32_bulk": "fp32_df"}.get(args.precision)
+    job_other = shards.shard_job(maker(other, seed=0, t_num=args.t_num), rank, world)[0] if other else None
     grid = job.grid_size
 
-    # accuracy: FP32-bulk against the FP64 plain path on the same sampled electrons
-    acc = accuracy_report(eng, job, job64) if not args.no_fp64_compare else None
+    # accuracy: the timed path (and the other FP32 path) against the FP64 plain path
+    # on the same sampled electrons
+    acc = accuracy_report(eng, job, job64, job_other) if not args.no_fp64_compare else None
     tstats = trajectory_stats(eng, job, job64) if not args.no_fp64_compare else None
 
     def sync_all():
@@ -323,7 +345,7 @@ def main():
     else:
         t_slowest, value = t_local, sum(effs) / t_local
 
-    # kernel-level timing of the bulk integrator for the roofline
+    # kernel-level timing of the integrator for the roofline
     stages = stage_times(eng, job)
     kern_ms = stages["integrate"]
 
@@ -371,15 +393,42 @@ def main():
         clocks = clk.summary()
         sm_mhz = clocks["sm_mhz"] or peaks.get("sm_max_mhz", 2070.0)
         n_sm = torch.cuda.get_device_properties(dev).multi_processor_count
-        fp32_peak = n_sm * 128 * 2 * (peaks.get("sm_max_mhz", 2070.0) * 1e6) / 1e12
+        sm_max = peaks.get("sm_max_mhz", 2070.0)
         steps_per_job = steps_total / args.steps
-        flops = steps_per_job * FLOPS_PER_STEP_SAE_2D_SCTS
-        # the flop count per step is the headline workload's (2D SAE SCTS)
-        achieved = flops / (kern_ms / 1e3) / 1e12 if (kern_ms and headline) else None
+        eff_mean = statistics.mean(effs)
+        if args.precision == "fp32_df":
+            # FP32-pipe issue: thread instructions per second against 128 lanes x SMs x clock
+            per_step = DF_FP32_INST_PER_STEP
+            achieved = (steps_per_job * per_step / (kern_ms / 1e3) / 1e12
+                        if (kern_ms and headline and per_step) else None)
+            roof = {"bound": "fp32_issue", "achieved": achieved, "peak": n_sm * 128 * sm_max * 1e6 / 1e12,
+                    "unit": "T FP32-pipe thread instructions/s",
+                    "traffic": (DF_DRAM_BYTES_PER_ELECTRON * eff_mean)
+                    if (headline and DF_DRAM_BYTES_PER_ELECTRON) else None,
+                    "kernel": "k_integrate_df (start-up + main pass)", "kernel_ms": kern_ms,
+                    "fp32_inst_per_step_attempt": per_step, "step_attempts_per_job": steps_per_job,
+                    "fma_pipe_issue_frac_ncu": DF_FMA_PIPE_ISSUE_NCU,
+                    "peak_source": "nominal FP32 issue: %d SMs x 128 lanes x %d MHz (no measured FP32 "
+                                   "peak is provided)" % (n_sm, sm_max)}
+        else:
+            flops = steps_per_job * FLOPS_PER_STEP_SAE_2D_SCTS
+            # the flop count per step is the headline workload's (2D SAE SCTS)
+            achieved = flops / (kern_ms / 1e3) / 1e12 if (kern_ms and headline) else None
+            roof = {"bound": "fp32", "achieved": achieved, "peak": n_sm * 128 * 2 * sm_max * 1e6 / 1e12,
+                    "unit": "TFLOP/s",
+                    "traffic": (INTEGRATOR_DRAM_BYTES_PER_ELECTRON * eff_mean) if headline else None,
+                    "kernel": "k_integrate_bulk" if args.precision == "fp32_bulk" else "k_integrate_fp64",
+                    "kernel_ms": kern_ms, "flops_per_step_attempt": FLOPS_PER_STEP_SAE_2D_SCTS,
+                    "step_attempts_per_job": steps_per_job,
+                    "peak_source": "nominal FP32 peak: %d SMs x 128 lanes x 2 x %d MHz (no measured "
+                                   "FP32 peak is provided)" % (n_sm, sm_max)}
+        roof["frac"] = (roof["achieved"] / roof["peak"]) if roof["achieved"] else None
+        dtype = {"fp32_df": "f32 pairs (double-float) stages + f64 sampling/collection/deposit",
+                 "fp32_bulk": "f32 stages + f64 phase/deposit", "fp64": "f64"}[args.precision]
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * t_slowest / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 stages + f64 collection/deposit",
+            "scaling": "weak", "vs_baseline": None, "dtype": dtype,
             "data": "synthetic",
             "config": {"workload": workload_text, "effective_trajectories_per_step": statistics.mean(effs),
                        "candidates_per_step": args.t_num * kt_per_t,
@@ -387,8 +436,9 @@ def main():
                        "parallelism": "weak: one Monte-Carlo shard per GPU (seed = rank)"},
             "precision": args.precision,
             "fp64_plain": acc and acc["fp64_plain"],
-            "speedup_fp32_bulk_vs_fp64": acc and value / world / acc["fp64_plain"]["value"],
+            "speedup_vs_fp64": acc and value / world / acc["fp64_plain"]["value"],
             "pmd_rel_l2_vs_fp64": acc and acc["pmd_rel_l2_vs_fp64"],
+            "pmd_gate_1e-3_met": acc and acc["pmd_rel_l2_vs_fp64"] <= 1e-3,
             "accuracy": acc,
             "trajectory_stats": tstats,
             "merged_shards": merged,
@@ -397,19 +447,15 @@ def main():
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * (args.t_num + 2),
                     "d2h_bytes_per_step": 8 * grid + 64},
             "gpu_launches": launches,
-            "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                         "frac": (achieved / fp32_peak) if achieved else None, "traffic": (INTEGRATOR_DRAM_BYTES_PER_ELECTRON * statistics.mean(effs)) if headline else None,
-                         "kernel": "k_integrate_bulk", "kernel_ms": kern_ms,
-                         "flops_per_step_attempt": FLOPS_PER_STEP_SAE_2D_SCTS,
-                         "step_attempts_per_job": steps_per_job,
-                         "peak_source": "nominal FP32 peak: %d SMs x 128 lanes x 2 x %d MHz (no measured "
-                                        "FP32 peak is provided)" % (n_sm, peaks.get("sm_max_mhz", 2070))},
+            "roofline": roof,
             "clocks": clocks,
             "wall_s": t_wall,
         }
         if not args.no_multi_instance and world == 1:
             line["multi_instance"] = multi_instance_report(eng)
-            line["autotune"] = autotune_report(eng, job, multi_instance_jobs()[0])
+            # the autotuner shapes the bulk integrator: tuned against fixed on the bulk job
+            job_bulk = job if args.precision == "fp32_bulk" else maker("fp32_bulk", seed=0, t_num=args.t_num)
+            line["autotune"] = autotune_report(eng, job_bulk, multi_instance_jobs()[0])
             line["graphs"] = graphs_report(lambda n: maker(args.precision, seed=rank, t_num=n or args.t_num))
         if not args.no_serving and world == 1:
             line["serving"] = serving_report()
@@ -422,10 +468,11 @@ def main():
     return 0
 
 
-def accuracy_report(eng, job, job64):
+def accuracy_report(eng, job, job64, job_other=None):
     """PMD error of the timed path against the FP64 plain path on the same electrons,
     next to the FP64 path's own sensitivity to its tolerance (rtol 1e-6 vs 1e-7), at
-    the full 1000 x 1000 resolution and after rebinning to 100 x 100 and 20 x 20."""
+    the full 1000 x 1000 resolution and after rebinning to 100 x 100 and 20 x 20;
+    job_other (the other FP32 path) gets its speed (5 runs) and PMD error beside it."""
     res64, spec64, _ = eng.run(job64, want_spectrum=True)
     res, spec, _ = eng.run(job, want_spectrum=True)
     j7 = job64.copy()
@@ -453,6 +500,18 @@ def accuracy_report(eng, job, job64):
     for f in (10, 50):
         out["pmd_rel_l2_vs_fp64_rebin%d" % f] = l2(rebin(spec, f), rebin(spec64, f))
         out["fp64_rtol1e-7_vs_rtol1e-6_rebin%d" % f] = l2(rebin(spec64b, f), rebin(spec64, f))
+    if job_other is not None:
+        eng.run(job_other, want_spectrum=False)
+        ms = []
+        for _ in range(5):
+            r, _, _ = eng.run(job_other, want_spectrum=False)
+            ms.append(r.elapsed_ms)
+        r, so, _ = eng.run(job_other, want_spectrum=True)
+        name = {abi.PRECISION_FP32_BULK: "fp32_bulk", abi.PRECISION_FP32_DF: "fp32_df"}[job_other.precision]
+        out[name] = {
+            "value": r.num_effective_traj / (min(ms) / 1e3), "unit": UNIT, "ms_per_step": min(ms),
+            "pmd_rel_l2_vs_fp64": l2(so, spec64), "pmd_rel_l2_vs_fp64_rebin50": l2(rebin(so, 50), rebin(spec64, 50)),
+            "speedup_vs_fp64": res64.elapsed_ms / min(ms)}
     return out
 
 
@@ -479,7 +538,8 @@ def trajectory_stats(eng, job, job64):
                 "max": int(s.max()), "log2_bins": [int(x) for x in bins]}
 
     return {"frac_rmin_below_5": float(np.mean(rmin < 5.0)) if rmin.size else None,
-            "steps_fp64": hist(s64), "steps_bulk": hist(s32)}
+            "steps_fp64": hist(s64), "steps_timed_path": hist(s32),
+            "step_counts_differing_from_fp64": int(np.sum(s32 != s64)) if s32.shape == s64.shape else None}
 
 
 def serving_requests(n=512, rate=20.0, seed=2024):
@@ -686,7 +746,7 @@ STAGES = ("sample", "compact", "field_table", "integrate", "collect", "deposit")
 
 def stage_times(eng, job):
     """Per-stage device times of one job (mean of 3 runs) from the library's own
-    events on its stream: the integrator entry is the bulk kernel's launch alone."""
+    events on its stream: the integrator entry is its kernels' launches alone."""
     import ctypes as C
 
     acc = [[] for _ in STAGES]

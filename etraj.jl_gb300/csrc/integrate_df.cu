@@ -27,7 +27,7 @@
 // terms are stage 6's.  The start-up pass hands an electron on at the first
 // boundary where it needs no differences (to a list, warp-aggregated atomicAdd);
 // a main-pass lane that takes one spends one turn evaluating its state.  Since
-// ~90% of the attempts run in the main pass, no warp there carries the longer
+// ~95% of the attempts run in the main pass, no warp there carries the longer
 // difference code for one lane, and it is not compiled into that pass.
 //
 // Field table.  F(t) is one function of time for every electron, tabulated once
@@ -55,8 +55,9 @@ namespace {
 constexpr int kDfThreads = 128;
 // Resident 128-thread blocks per SM the passes' register budgets are set for (168
 // and 128 registers a thread; a few hundred bytes spill).  On the argon headline
-// job (4.0e6 electrons) the budgets (1, 1), (2, 3), (3, 4), (4, 4) and (4, 5) took
-// 139, 104, 99, 103 and 107 ms, with identical results.
+// job (4.0e6 electrons) the integrator took 93.8, 93.5, 96.9 and 98.8 ms with the
+// budgets (3, 4), (2, 4), (4, 4) and (3, 5), with identical results; without
+// launch bounds (up to 251 registers) it took 139 ms.
 constexpr int kDfMinBlocksStart = 3;
 constexpr int kDfMinBlocksMain = 4;
 
