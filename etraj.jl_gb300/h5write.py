@@ -1,10 +1,11 @@
 """Writer of the reference's output files (TrajectorySimulation.jl:502-546).
 
 `write_output!` stores, at the top level of a JLD2 file (or an HDF5 file
-with `output_fmt=:h5`), the datasets params_text, px, py[, pz],
-momentum_spec, ion_prob, ion_prob_uncollected and num_effective_traj.  This
-module writes the same names with numpy only (no libhdf5), as the HDF5 subset
-JLD2 itself writes (published HDF5 File Format Specification 3.0):
+with `output_fmt=:h5`), the datasets info (written when the file is created,
+:237), params_text, params (JLD2 only), px, py[, pz], momentum_spec, ion_prob,
+ion_prob_uncollected and num_effective_traj.  This module writes the same names
+with numpy and zlib only (no libhdf5), as the HDF5 subset JLD2 itself writes
+(published HDF5 File Format Specification 3.0):
 
   - a version-2 superblock; for `.jld2` behind JLD2's 512-byte identification
     block, with the base address after it, as JLD2 does;
@@ -14,18 +15,28 @@ JLD2 itself writes (published HDF5 File Format Specification 3.0):
   - each dataset as a version-2 object header with the four messages JLD2
     writes: fill value (version 3, flags 0x09), dataspace (version 2),
     datatype (version 3: IEEE little-endian float64, signed 64-bit integer, or
-    a null-padded UTF-8 fixed-length string) and data layout (version 4:
+    null-padded UTF-8 fixed-length strings) and data layout (version 4:
     compact for small data, contiguous otherwise);
+  - a compressed dataset (`output_compress`, which the reference applies to
+    momentum_spec only) as one chunk: data layout version 4 with the
+    single-chunk index and its filtered size, and a version-2 filter pipeline
+    message: deflate (filter 1, zlib format) as JLD2's `compress=true`, and for
+    :h5 the byte shuffle (filter 2) before deflate at level 6, as HDF5.jl's
+    `shuffle=true, deflate=6`;
+  - a nested mapping as a group (an object header of links, like the root);
   - every superblock and object header closed by its Jenkins lookup3
     checksum (Bob Jenkins' `hashlittle`, initval 0), as HDF5 requires.
 
 Arrays are written with their dimensions reversed and their data in Julia's
 column-major order, so HDF5.jl and JLD2 read back the Julia array.  The
-reference's `params` entry (a Julia object) has no counterpart here, and the
-data is written uncompressed (`output_compress` would need chunked layouts
-and a filter pipeline).
+reference's `params` entry is a serialized Julia object (an OrderedDict of
+Symbols, tuples and the laser and target structs, whose JLD2 form names Julia
+types); here it is a group of plain datasets with the same keys and values
+(symbols as strings, tuples as arrays, the laser and target as groups of
+their `Serialize` fields), which HDF5 and JLD2 readers open without eTraj.
 """
 import struct
+import zlib
 
 import numpy as np
 
@@ -93,13 +104,20 @@ def _ohdr(messages):
     return head + struct.pack("<I", lookup3(head))
 
 
+def _strings(vals):
+    raw = [v.encode("utf-8") for v in vals]
+    n = max([len(r) for r in raw] + [1])
+    return bytes([0x33, 0x11, 0x00, 0x00]) + struct.pack("<I", n), b"".join(r.ljust(n, b"\x00") for r in raw)
+
+
 def _encode(value):
-    """(datatype message body, dataspace message body, raw bytes) of a value."""
+    """(datatype message body, dataspace message body, raw bytes, element size) of a value."""
     if isinstance(value, str):
-        raw = value.encode("utf-8")
-        n = max(len(raw), 1)
-        dtype = bytes([0x33, 0x11, 0x00, 0x00]) + struct.pack("<I", n)
-        return dtype, bytes([2, 0, 0, 0]), raw.ljust(n, b"\x00")
+        dtype, raw = _strings([value])
+        return dtype, bytes([2, 0, 0, 0]), raw, len(raw)
+    if isinstance(value, (list, tuple)) and value and all(isinstance(v, str) for v in value):
+        dtype, raw = _strings(list(value))
+        return dtype, bytes([2, 1, 0, 1]) + struct.pack("<Q", len(value)), raw, len(raw) // len(value)
     arr = np.asarray(value)
     if arr.dtype.kind in "iub":
         dtype, arr = _I64, arr.astype("<i8")
@@ -112,43 +130,80 @@ def _encode(value):
     else:
         dims = arr.shape[::-1]  # HDF5's row-major dims of a column-major Julia array
         space = bytes([2, arr.ndim, 0, 1]) + b"".join(struct.pack("<Q", d) for d in dims)
-    return dtype, space, arr.ravel(order="F").tobytes()
+    return dtype, space, arr.ravel(order="F").tobytes(), 8
 
 
-def write(path, items, jld2=True):
-    """Writes the (name, value) pairs of `items` (str, int, float or numpy
-    arrays) as top-level datasets of a new file at `path`."""
+def _filters(shuffle, esize, level):
+    """Filter pipeline message (version 2) body: [shuffle,] deflate."""
+    f = []
+    if shuffle:
+        f.append(struct.pack("<HHH", 2, 0x0001, 1) + struct.pack("<I", esize))
+    f.append(struct.pack("<HHH", 1, 0x0001, 1) + struct.pack("<I", level))
+    return bytes([2, len(f)]) + b"".join(f)
+
+
+def _shuffled(raw, esize):
+    """HDF5's byte shuffle: byte k of every element, for k = 0 .. esize-1."""
+    if esize <= 1:
+        return raw
+    return np.frombuffer(raw, np.uint8).reshape(-1, esize).T.tobytes()
+
+
+def write(path, items, jld2=True, compress=()):
+    """Writes the (name, value) pairs of `items` as top-level datasets of a new
+    file at `path`.  Values: str, int, float, numpy arrays, lists of str, or a
+    dict of such values (a group, nested).  Names in `compress` are written as
+    one deflated chunk (with the byte shuffle in front for HDF5 files)."""
     block = b""
     if jld2:
         ident = b"HDF5-based Julia Data Format, version 0.1.1\x00 (etraj-gb300)\x00"
         block = ident.ljust(512, b"\x00")
     base = len(block)
     out = bytearray(48)  # superblock, filled at the end
-    links = []
 
     def here():
         return len(out)
 
-    for name, value in items:
-        dtype, space, raw = _encode(value)
-        if len(raw) <= _COMPACT_MAX:
+    def dataset(name, value):
+        dtype, space, raw, esize = _encode(value)
+        msgs = [_msg(0x05, bytes([3, 0x09])), _msg(0x01, space), _msg(0x03, dtype, flags=1)]
+        if name in compress and len(raw) > 0 and space[1] > 0:
+            packed = zlib.compress(_shuffled(raw, esize) if not jld2 else raw, 6)
+            addr = here()
+            out.extend(packed)
+            rank = space[1]
+            dims = struct.unpack_from("<%dQ" % rank, space, 4)
+            layout = bytes([4, 2, 0x02, rank + 1, 8]) + b"".join(struct.pack("<Q", d) for d in dims)
+            layout += struct.pack("<Q", esize) + bytes([1]) + struct.pack("<QI", len(packed), 0)
+            layout += struct.pack("<Q", addr)
+            msgs.append(_msg(0x0B, _filters(not jld2, esize, 6), flags=1))
+        elif len(raw) <= _COMPACT_MAX:
             layout = bytes([4, 0]) + struct.pack("<H", len(raw)) + raw
         else:
             addr = here()
-            out += raw
+            out.extend(raw)
             layout = bytes([4, 1]) + struct.pack("<QQ", addr, len(raw))
-        hdr_addr = here()
-        out += _ohdr([_msg(0x05, bytes([3, 0x09])), _msg(0x01, space), _msg(0x03, dtype, flags=1),
-                      _msg(0x08, layout)])
-        links.append((name, hdr_addr))
-    msgs = [_msg(0x02, bytes([0, 0]) + struct.pack("<QQ", UNDEF, UNDEF)), _msg(0x0A, bytes([0, 0]))]
-    for name, addr in links:
-        nb = name.encode("utf-8")
-        if len(nb) > 255:
-            raise ValueError("dataset name too long")
-        msgs.append(_msg(0x06, bytes([1, 0x10, 0x01, len(nb)]) + nb + struct.pack("<Q", addr)))
-    root = here()
-    out += _ohdr(msgs)
+        msgs.append(_msg(0x08, layout))
+        hdr = here()
+        out.extend(_ohdr(msgs))
+        return hdr
+
+    def group(entries):
+        links = []
+        for name, value in entries:
+            addr = group(list(value.items())) if isinstance(value, dict) else dataset(name, value)
+            links.append((name, addr))
+        msgs = [_msg(0x02, bytes([0, 0]) + struct.pack("<QQ", UNDEF, UNDEF)), _msg(0x0A, bytes([0, 0]))]
+        for name, addr in links:
+            nb = name.encode("utf-8")
+            if len(nb) > 255:
+                raise ValueError("dataset name too long")
+            msgs.append(_msg(0x06, bytes([1, 0x10, 0x01, len(nb)]) + nb + struct.pack("<Q", addr)))
+        hdr = here()
+        out.extend(_ohdr(msgs))
+        return hdr
+
+    root = group(list(items))
     eof = len(out)
     sb = _SIG + bytes([2, 8, 8, 0]) + struct.pack("<QQQQ", base, UNDEF, eof, root)
     out[0:48] = sb + struct.pack("<I", lookup3(sb))

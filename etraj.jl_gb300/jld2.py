@@ -264,9 +264,11 @@ class JLD2File:
         if key in self._objs:
             return self._objs[key]
         msgs = self._messages(addr)
-        dtype = dspace = layout = None
+        dtype = dspace = layout = pipeline = None
         links = {}
         for mtype, mflags, body in msgs:
+            if mtype == 0x0B:
+                pipeline = body
             if mtype == 0x03:
                 dtype = self._shared_dtype(body) if mflags & 0x02 else self._dtype(body)[0]
             elif mtype == 0x01:
@@ -285,7 +287,7 @@ class JLD2File:
             self._objs[key] = val
             return val
         count = int(np.prod(dspace)) if dspace else 1
-        raw = self._layout_data(layout, dtype.size * count)
+        raw = self._layout_data(layout, dtype.size * count, pipeline)
         vals = self._decode(dtype, raw, count)
         if dspace == ():
             val = vals[0]
@@ -296,7 +298,44 @@ class JLD2File:
         self._objs[key] = val
         return val
 
-    def _layout_data(self, body, nbytes):
+    @staticmethod
+    def _filters(body):
+        """(id, client data) of a filter pipeline message (version 1 or 2)."""
+        ver, n = body[0], body[1]
+        p = 8 if ver == 1 else 2
+        out = []
+        for _ in range(n):
+            fid = struct.unpack_from("<H", body, p)[0]
+            p += 2
+            nlen = 0
+            if ver == 1 or fid >= 256:
+                nlen = struct.unpack_from("<H", body, p)[0]
+                p += 2
+            _flags, ncd = struct.unpack_from("<HH", body, p)
+            p += 4
+            if nlen:
+                p += (nlen + 7) // 8 * 8 if ver == 1 else nlen
+            cd = struct.unpack_from("<%dI" % ncd, body, p)
+            p += 4 * ncd
+            if ver == 1 and ncd % 2:
+                p += 4
+            out.append((fid, cd))
+        return out
+
+    def _unfilter(self, data, pipeline):
+        """Undoes the filters of a chunk, last first: deflate (1) and byte shuffle (2)."""
+        import zlib
+        for fid, cd in reversed(self._filters(pipeline)):
+            if fid == 1:
+                data = zlib.decompress(data)
+            elif fid == 2:
+                k = cd[0] if cd else 1
+                data = np.frombuffer(data, np.uint8).reshape(k, -1).T.tobytes() if k > 1 else data
+            else:
+                raise ValueError("filter %d is not supported" % fid)
+        return data
+
+    def _layout_data(self, body, nbytes, pipeline=None):
         ver = body[0]
         if ver not in (3, 4):
             raise ValueError("data layout version %d" % ver)
@@ -310,7 +349,21 @@ class JLD2File:
                 return b"\x00" * nbytes
             p = self._abs(addr)
             return self.buf[p:p + size]
-        raise ValueError("chunked datasets are not supported")
+        if cls == 2 and ver == 4:  # chunked: the single-chunk index only
+            flags, rank, enc = body[2], body[3], body[4]
+            p = 5 + rank * enc
+            if body[p] != 1:
+                raise ValueError("chunk index type %d is not supported" % body[p])
+            p += 1
+            size = None
+            if flags & 0x02:
+                size, _mask = struct.unpack_from("<QI", body, p)
+                p += 12
+            addr = struct.unpack_from("<Q", body, p)[0]
+            q = self._abs(addr)
+            data = self.buf[q:q + (size if size is not None else nbytes)]
+            return self._unfilter(data, pipeline) if pipeline is not None else data
+        raise ValueError("this chunked layout is not supported")
 
     def _link(self, body):
         ver, flags = body[0], body[1]

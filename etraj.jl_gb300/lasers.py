@@ -112,6 +112,13 @@ class _CosNLaser(MonochromaticLaser):
         self.cep = float(cep)
         self.t_shift = float(t_shift)
 
+    def Serialize(self):
+        """The laser's parameters in the order of Serialize (Cos4Laser.jl:192-204,
+        Cos2Laser.jl:192-204)."""
+        return {"type": type(self).__name__, "peak_int": self.peak_int, "wave_len": self.wave_len,
+                "cyc_num": self.cyc_num, "ellip": self.ellip, "azi": self.azi, "cep": self.cep,
+                "t_shift": self.t_shift}
+
     def CycNum(self):
         return self.cyc_num
 
@@ -164,6 +171,12 @@ class GaussianLaser(MonochromaticLaser):
         self.cep = float(cep)
         self.t_shift = float(t_shift)
 
+    def Serialize(self):
+        """The laser's parameters in the order of Serialize (GaussianLaser.jl:200-212)."""
+        return {"type": "GaussianLaser", "peak_int": self.peak_int, "wave_len": self.wave_len,
+                "spread_cyc_num": self.spread_cyc_num, "ellip": self.ellip, "azi": self.azi, "cep": self.cep,
+                "t_shift": self.t_shift}
+
     def SpreadCycNum(self):
         return self.spread_cyc_num
 
@@ -193,6 +206,11 @@ class BichromaticLaser(Laser):
         if i == 2:
             return self.laser2
         raise IndexError("Index of the laser should be either 1 or 2.")
+
+    def Serialize(self):
+        """Serialize (BichromaticLaser.jl:101-109): the two lasers' and the delay."""
+        return {"type": "BichromaticLaser", "laser1": self.laser1.Serialize(), "laser2": self.laser2.Serialize(),
+                "delay21": self.delay}
 
     def Laser1(self):
         return self.laser1

@@ -388,7 +388,7 @@ def perform_traj_simulation(*, init_cond_method, laser, target, dimension, sampl
 
     Returns a dict with the keys of the reference's output file, and writes
     that file when `output_path` is given: `output_fmt` :jld2 (the default) or
-    :h5 as write_output! does (h5write.py; uncompressed), or "npz".  As in the
+    :h5 as write_output! does (h5write.py; momentum_spec deflated when output_compress), or "npz".  As in the
     reference (:199-215) an existing file is not overwritten (a time-stamped
     name is used instead) and the extension is appended when missing.  Extra
     keywords: `precision` ("fp64", "fp32_df" or "fp32_bulk"), `seed` (Monte-Carlo
@@ -418,12 +418,12 @@ def perform_traj_simulation(*, init_cond_method, laser, target, dimension, sampl
         "ion_prob_uncollected": res.ion_prob_uncollected,
         "num_effective_traj": res.num_effective_traj,
         "num_failed_traj": res.num_failed_traj,
-        "params_text": _params_text(locals()),
     }
     if dimension == 3:
         out["pz"] = _axis(final_p_max[2], final_p_num[2])
     if amp is not None:
         out["amplitude"] = (amp[0::2] + 1j * amp[1::2]).reshape(shape, order="F")
+    path = None
     if output_path:
         import os
         import time
@@ -434,29 +434,103 @@ def perform_traj_simulation(*, init_cond_method, laser, target, dimension, sampl
         ext = "." + fmt
         if not path.endswith(ext):
             path += ext
+    params = _params(locals())
+    out["params"] = params
+    out["params_text"] = _yaml(params)
+    if path:
         if fmt == "npz":
-            (np.savez_compressed if output_compress else np.savez)(path, **out)
+            flat = {k: v for k, v in out.items() if k != "params"}
+            (np.savez_compressed if output_compress else np.savez)(path, **flat)
         else:
-            # the names and order of write_output! (TrajectorySimulation.jl:508-543)
+            # the names and order of write_output! (TrajectorySimulation.jl:237, 508-543)
             from . import h5write
-            items = [("params_text", out["params_text"]), ("px", out["px"]), ("py", out["py"])]
+            items = [("info", "Trajectory simulation output generated by etraj-gb300"),
+                     ("params_text", out["params_text"])]
+            if fmt == "jld2":
+                items.append(("params", params))
+            items += [("px", out["px"]), ("py", out["py"])]
             if dimension == 3:
                 items.append(("pz", out["pz"]))
             items += [("momentum_spec", out["momentum_spec"]), ("ion_prob", float(out["ion_prob"])),
                       ("ion_prob_uncollected", float(out["ion_prob_uncollected"])),
                       ("num_effective_traj", int(out["num_effective_traj"]))]
-            h5write.write(path + "!", items, jld2=(fmt == "jld2"))
+            h5write.write(path + "!", items, jld2=(fmt == "jld2"),
+                          compress=("momentum_spec",) if output_compress else ())
             os.replace(path + "!", path)
         out["output_path"] = path
     return out
 
 
-def _params_text(kw):
-    keys = ["init_cond_method", "sample_t_intv", "sample_t_num", "sample_monte_carlo",
-            "sample_cutoff_limit", "traj_phase_method", "traj_rtol", "traj_t_final",
-            "final_p_max", "final_p_num", "ss_kd_max", "ss_kd_num", "ss_kz_max", "ss_kz_num",
-            "mc_kt_num", "mc_kd_max", "mc_kz_max", "rate_prefix", "precision", "seed"]
-    lines = ["%s: %r" % (k, kw[k]) for k in keys if k in kw]
-    lines.append("laser: %r" % (kw.get("laser"),))
-    lines.append("target: %r" % (getattr(kw.get("target"), "__dict__", None),))
+def _params(kw):
+    """The effective parameters that TrajectorySimulation.jl:275-296 packs into
+    `params`, in its order: symbols as strings, the laser and target as their
+    Serialize dicts; the method's sample ranges, rate_prefix for the ADK / SPA /
+    SPANE family and mol_orbit_ridx for molecules."""
+    method = _sym(kw["init_cond_method"])
+    p = {"init_cond_method": method, "laser": kw["laser"].Serialize(), "target": kw["target"].Serialize(),
+         "sample_t_intv": tuple(float(x) for x in kw["sample_t_intv"]), "sample_t_num": int(kw["sample_t_num"]),
+         "sample_monte_carlo": bool(kw["sample_monte_carlo"]),
+         "sample_cutoff_limit": float(kw["sample_cutoff_limit"]),
+         "traj_phase_method": _sym(kw["traj_phase_method"]), "traj_rtol": float(kw["traj_rtol"]),
+         "traj_t_final": float(kw["traj_t_final"]), "output_fmt": kw["fmt"], "output_path": kw["path"] or "",
+         "final_p_max": tuple(float(x) for x in kw["final_p_max"]),
+         "final_p_num": tuple(int(x) for x in kw["final_p_num"])}
+    three = int(kw["dimension"]) == 3
+    if not kw["sample_monte_carlo"]:
+        p["ss_kd_max"], p["ss_kd_num"] = float(kw["ss_kd_max"]), int(kw["ss_kd_num"])
+        if three:
+            p["ss_kz_max"], p["ss_kz_num"] = float(kw["ss_kz_max"]), int(kw["ss_kz_num"])
+    else:
+        p["mc_kd_max"], p["mc_kt_num"] = float(kw["mc_kd_max"]), int(kw["mc_kt_num"])
+        if three:
+            p["mc_kz_max"] = float(kw["mc_kz_max"])
+    if method.endswith(("ADK", "SPA", "SPANE", "SFA", "SFAAE")):
+        rp = kw["rate_prefix"]
+        p["rate_prefix"] = _sym(rp) if isinstance(rp, str) else [_sym(x) for x in rp]
+    if getattr(kw["target"], "MolEnergyLevels", None) is not None:
+        p["mol_orbit_ridx"] = int(kw["mol_orbit_ridx"])
+    return p
+
+
+def _jl_float(x):
+    """A float as Julia prints it: the shortest digits that round-trip, in
+    scientific notation (mantissa with a decimal point, bare exponent) outside
+    [1e-4, 1e6)."""
+    x = float(x)
+    if x != x:
+        return "NaN"
+    if x in (float("inf"), float("-inf")):
+        return "Inf" if x > 0 else "-Inf"
+    if x == 0.0 or 1e-4 <= abs(x) < 1e6:
+        r = repr(x)
+        return r if "." in r else r + ".0"
+    m, e = np.format_float_scientific(x, unique=True, trim="0").split("e")
+    return "%se%d" % (m, int(e))
+
+
+def _yaml_scalar(v):
+    if isinstance(v, (bool, np.bool_)):
+        return "true" if v else "false"
+    if isinstance(v, (int, np.integer)):
+        return str(int(v))
+    if isinstance(v, (float, np.floating)):
+        return _jl_float(v)
+    return str(v)
+
+
+def _yaml(d, indent=0):
+    """Block-style YAML of the params dict (the params_text entry, YAML.write at
+    TrajectorySimulation.jl:507)."""
+    pad = "  " * indent
+    lines = []
+    for k, v in d.items():
+        if isinstance(v, dict):
+            lines.append("%s%s:" % (pad, k))
+            lines.append(_yaml(v, indent + 1))
+        elif isinstance(v, (list, tuple, np.ndarray)):
+            lines.append("%s%s:" % (pad, k))
+            for x in np.asarray(v, dtype=object).ravel(order="F"):
+                lines.append("%s  - %s" % (pad, _yaml_scalar(x)))
+        else:
+            lines.append("%s%s: %s" % (pad, k, _yaml_scalar(v)))
     return "\n".join(lines)

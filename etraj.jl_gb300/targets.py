@@ -84,6 +84,12 @@ class HydrogenLikeAtom(SAEAtomBase):
         self.soft_core = float(soft_core)
         self.name = name
 
+    def Serialize(self):
+        """The atom's parameters in the order of Serialize (HydrogenLikeAtom.jl:166-180)."""
+        return {"type": "HydrogenLikeAtom", "Ip": self.Ip, "nucl_charge": self.nucl_charge, "l": self.l,
+                "m": self.m, "asymp_coeff": self.asymp_coeff, "soft_core": self.soft_core,
+                "quan_ax_θ": self.quan_ax_θ, "quan_ax_ϕ": self.quan_ax_ϕ, "name": self.name}
+
     def to_c(self):
         t = abi.Target()
         t.kind = abi.TARGET_HYDROGEN_LIKE
@@ -113,6 +119,13 @@ class SAEAtom(SAEAtomBase):
         self.a1, self.b1, self.a2, self.b2, self.a3, self.b3 = map(float, (a1, b1, a2, b2, a3, b3))
         self.soft_core = float(soft_core)
         self.name = name
+
+    def Serialize(self):
+        """The atom's parameters in the order of Serialize (SAEAtom.jl:193-212)."""
+        return {"type": "SAEAtom", "Ip": self.Ip, "nucl_charge": self.nucl_charge, "l": self.l, "m": self.m,
+                "asymp_coeff": self.asymp_coeff, "quan_ax_θ": self.quan_ax_θ, "quan_ax_ϕ": self.quan_ax_ϕ,
+                "a1": self.a1, "b1": self.b1, "a2": self.a2, "b2": self.b2, "a3": self.a3, "b3": self.b3,
+                "soft_core": self.soft_core, "name": self.name}
 
     def to_c(self):
         t = abi.Target()
@@ -393,6 +406,13 @@ class GenericMolecule(MoleculeBase):
             t.asymp_coeff_lm = abi.dptr(arr)
             t.asymp_lmax = Cm.shape[0] - 1
         return t, keep
+
+    def Serialize(self):
+        """The molecule's parameters in the order of Serialize (GenericMolecule.jl:620-633)."""
+        return {"type": "GenericMolecule", "atoms": list(self.atoms),
+                "atom_coords": np.asarray(self.atom_coords, dtype=float), "charge": self.charge,
+                "spin": self.spin, "name": self.name, "rot_α": self.rot_α, "rot_β": self.rot_β,
+                "rot_γ": self.rot_γ}
 
     def __repr__(self):
         return "[GenericMolecule] %s" % self.name

@@ -253,8 +253,12 @@ def test_gpu_perform_traj_simulation_writes_the_reference_file(eng, tmp_path, fm
     ext = "." + fmt[1:]
     assert out["output_path"] == path + ext
     d = et.jld2.load(out["output_path"])
-    assert set(d) == {"params_text", "px", "py", "pz", "momentum_spec", "ion_prob", "ion_prob_uncollected",
-                      "num_effective_traj"}
+    names = ["info", "params_text"] + (["params"] if fmt == ":jld2" else []) + [
+        "px", "py", "pz", "momentum_spec", "ion_prob", "ion_prob_uncollected", "num_effective_traj"]
+    assert list(d) == names
+    if fmt == ":jld2":
+        assert d["params"]["init_cond_method"] == "ADK" and d["params"]["laser"]["type"] == "Cos4Laser"
+        assert tuple(d["params"]["final_p_num"]) == (40, 30, 6)
     assert np.array_equal(d["momentum_spec"], out["momentum_spec"]) and d["momentum_spec"].shape == (40, 30, 6)
     assert np.array_equal(d["px"], out["px"]) and np.array_equal(d["pz"], out["pz"])
     assert d["ion_prob"] == out["ion_prob"] and d["num_effective_traj"] == out["num_effective_traj"]
