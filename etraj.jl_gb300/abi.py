@@ -137,6 +137,7 @@ SIGNATURES = [
     ("etraj_set_bulk_tile", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                       C.c_int]),
     ("etraj_set_straggler_repack", C.c_int, [C.c_void_p, C.c_int]),
+    ("etraj_set_static_assignment", C.c_int, [C.c_void_p, C.c_int]),
     ("etraj_set_keep_final_states", C.c_int, [C.c_void_p, C.c_int]),
     ("etraj_dump_final_states", C.c_int, [C.c_void_p, C.c_uint64, _DP, _DP, _I32P]),
     ("etraj_dump_step_counts", C.c_int, [C.c_void_p, C.c_uint64, _I32P]),

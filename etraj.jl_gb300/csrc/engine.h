@@ -197,6 +197,7 @@ struct BulkParams {
     int n_int;          // field-table intervals
     int table_in_smem;  // 1: stage the table in shared memory
     int threads, blocks_per_sm, refill_min;
+    int static_assign;  // 1: one electron per lane, no queue, no rounds (the plain kernel's schedule)
     int occ;            // register budget of the build: 2 (<= 128 per thread) or 3 (<= 85)
     int64_t max_n;      // upper bound of the electron count (grid sizing)
     const BulkInst* inst;  // multi-instance launch: n_inst instances (else nullptr, 0)

@@ -255,6 +255,7 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
     float mK1 = 0.0f, mph1 = 0.0f;  // and their term magnitudes
     int tn = 0, iter = 0, attempts = 0, rs = 0;  // rs: step attempts in this round
     bool drained = false;                         // the queue was found empty
+    bool taken = false;                           // static assignment: the lane's electron was taken
     float tfr = 0.0f, dth = 0.0f, dthp = 0.0f, dthmax = 0.0f, lqold = LOG2_QOLDINIT, q11 = 1.0f;
     bool accept = false, active = false, need = true;
     unsigned long long s = 0;
@@ -266,8 +267,14 @@ k_integrate_bulk(const __grid_constant__ BulkParams P, InitSoA soa, const double
         if (needm && (__popc(needm) >= P.refill_min || actm == 0u)) {
             const int leader = __ffs(needm) - 1;
             unsigned long long base = 0ull;
-            if (lane == leader) base = atomicAdd(queue, (unsigned long long)__popc(needm));
-            base = __shfl_sync(FULL, base, leader);
+            if (P.static_assign) {
+                // electron blockIdx.x * blockDim.x + threadIdx.x, then nothing more
+                base = taken ? n_traj : (unsigned long long)blockIdx.x * blockDim.x + (threadIdx.x & ~31u);
+                taken = true;
+            } else {
+                if (lane == leader) base = atomicAdd(queue, (unsigned long long)__popc(needm));
+                base = __shfl_sync(FULL, base, leader);
+            }
             drained = drained || (base + (unsigned long long)__popc(needm) > n_traj);
             if (need) {
                 need = false;
@@ -804,7 +811,21 @@ int launch_bulk_t(const BulkParams& P, InitSoA soa, const double* t, const int64
     const int64_t lanes_per_block = (int64_t)P.threads * 4;
     const int64_t want = (P.max_n + lanes_per_block - 1) / lanes_per_block;
     const int64_t cap = (int64_t)sm_count * P.blocks_per_sm;
-    const int blocks = (int)(want < 1 ? 1 : (want < cap ? want : cap));
+    int blocks = (int)(want < 1 ? 1 : (want < cap ? want : cap));
+    if (P.static_assign) {
+        // one electron per lane: a grid over all of them, one launch
+        const int64_t nb = (P.max_n + P.threads - 1) / P.threads;
+        blocks = (int)(nb < 1 ? 1 : nb);
+        cudaMemsetAsync(queue, 0, sizeof(unsigned long long) * 2, s);
+        BulkParams Q = P;
+        Q.park_buf = nullptr;
+        Q.park_in = nullptr;
+        Q.park_out = nullptr;
+        Q.park_budget = 0;
+        Q.park_out_count = queue + 1;
+        kern<<<blocks, P.threads, smem, s>>>(Q, soa, t, idx, count, queue, out);
+        return 1;
+    }
     // queue[2r]: the work counter of round r; queue[2r+1]: electrons parked in round r
     const int rounds = P.park_buf ? kBulkRounds : 1;
     cudaMemsetAsync(queue, 0, sizeof(unsigned long long) * 2 * rounds, s);

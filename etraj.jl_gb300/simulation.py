@@ -211,6 +211,10 @@ class Engine:
             self._check(st)
         return t.value, b.value, r.value, st == abi.OK
 
+    def set_static_assignment(self, enable):
+        """Bulk path: one electron per lane and no work stealing (for comparison)."""
+        self._check(self.lib.etraj_set_static_assignment(self.ctx, 1 if enable else 0))
+
     def set_straggler_repack(self, enable):
         """Bulk path: run the integrator in rounds that repack long-running electrons."""
         self._check(self.lib.etraj_set_straggler_repack(self.ctx, 1 if enable else 0))

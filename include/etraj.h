@@ -285,11 +285,14 @@ int etraj_server_stats(etraj_server* srv, int64_t* running, int64_t* queued, siz
 const char* etraj_server_last_error(const etraj_server* srv);
 
 /* ---- CUDA graphs ------------------------------------------------------------------
- * No counterpart in the reference.  With etraj_set_graphs(ctx, 1) the kernel
- * sequence of a job (prologue to deposit) is captured into a CUDA graph and
- * replayed for the following jobs whose launch parameters are identical
- * (same job, same buffers, same bulk launch shape), e.g. repeated runs of one
- * configuration; any other job is captured anew.  Off by default. */
+ * No counterpart in the reference.  On by default: the kernel sequence of a job
+ * (prologue to deposit), or of a multi-instance batch (etraj_run_batch: every
+ * instance's sampling, one integrator launch, the deposit, the per-instance
+ * reductions and the weighted sum), runs directly the first time; when the
+ * same launch parameters come again (same jobs, same buffers, same launch
+ * shape) it is captured into a CUDA graph and replayed from then on.  Jobs
+ * that do not repeat never pay for a capture.  etraj_set_graphs(ctx, 0) turns
+ * it off and frees the graphs. */
 int etraj_set_graphs(etraj_ctx* ctx, int enable);
 
 /* ---- autotuner --------------------------------------------------------------------
@@ -325,6 +328,14 @@ int etraj_set_bulk_tile(etraj_ctx* ctx, int dimension, int phase, int target, in
  * one launch.  Each electron's arithmetic does not depend on where it runs, so
  * results are the same bits either way. */
 int etraj_set_straggler_repack(etraj_ctx* ctx, int enable);
+
+/* Static assignment (off by default): the bulk integrator of a job launches one
+ * lane per electron and each lane integrates its electron and stops, as the
+ * plain one-thread-per-trajectory kernel does -- no queue, no refill, no
+ * rounds.  A warp then runs until its slowest electron is done.  It exists to
+ * measure what work stealing gains at the same precision; results are the same
+ * bits either way. */
+int etraj_set_static_assignment(etraj_ctx* ctx, int enable);
 
 
 /* ---- per-trajectory final states ---------------------------------------------------

@@ -204,6 +204,31 @@ def test_rounds_with_parking_keep_every_bit():
     off.close()
 
 
+def test_static_assignment_keeps_every_bit():
+    """One electron per lane with no work stealing and no rounds (the plain
+    kernel's schedule) gives the same bits as the work-stealing schedule, on the
+    uneven-step recollision workload (SPA, bichromatic, 3D, QTMC)."""
+    from test_gpu_full_size import recollision_job
+    job = recollision_job(t_num=300)
+    job.precision = abi.PRECISION_FP32_BULK
+    ws = et.Engine(device=0)
+    st = et.Engine(device=0)
+    st.set_static_assignment(True)
+    for e in (ws, st):
+        e.keep_final_states(True)
+    r1, s1, a1 = ws.run(job, want_amplitude=True)
+    r2, s2, a2 = st.run(job, want_amplitude=True)
+    n = r1.num_effective_traj
+    assert n == r2.num_effective_traj > 1000
+    assert r1.num_steps == r2.num_steps and r1.ion_prob == r2.ion_prob
+    assert np.array_equal(s1, s2) and np.array_equal(a1, a2)
+    p1, f1, t1 = ws.dump_final_states(n)
+    p2, f2, t2 = st.dump_final_states(n)
+    assert np.array_equal(p1, p2) and np.array_equal(f1, f2) and np.array_equal(t1, t2)
+    ws.close()
+    st.close()
+
+
 SPA_CASES = [
     dict(method="SPA", dim=3, mc=True, laser="bichrom", phase="QTMC", nt=40, nkd=12, nkz=12, prefix=["Pre", "Jac"]),
     dict(method="SPA", dim=2, target="Ar", laser="cos2", phase="SCTS", ellip=1.0, mc=True, nt=60, nkd=200, nkz=1),

@@ -17,6 +17,7 @@ def test_graph_replay_matches_direct_launches():
     b.precision = abi.PRECISION_FP32_BULK
     jobs.append(b)
     direct = et.Engine(device=0)
+    direct.set_graphs(False)
     ref = [direct.run(j, want_amplitude=True) for j in jobs]
     direct.close()
     g = et.Engine(device=0)
@@ -29,4 +30,23 @@ def test_graph_replay_matches_direct_launches():
     import ctypes as C
     buf = (C.c_double * 8)()
     assert g.lib.etraj_stage_times(g.ctx, buf, 8) == 6 and buf[3] > 0.0
+    g.close()
+
+
+def test_batch_graph_replay_matches_direct_launches():
+    """A multi-instance batch runs directly, is captured the second time and
+    replayed the third, each time with the direct run's bits."""
+    import bench
+    jobs, w = bench.multi_instance_jobs(n=6, seed=3)
+    direct = et.Engine(device=0)
+    direct.set_graphs(False)
+    ref, wref = direct.run_batch(jobs, want_spectrum=True, weights=w)
+    direct.close()
+    g = et.Engine(device=0)
+    for _ in range(3):
+        outs, wsum = g.run_batch(jobs, want_spectrum=True, weights=w)
+        assert np.array_equal(wsum, wref)
+        for (r, s, _), (r0, s0, _) in zip(outs, ref):
+            assert r.num_effective_traj == r0.num_effective_traj and r.ion_prob == r0.ion_prob
+            assert np.array_equal(s, s0)
     g.close()
