@@ -13,10 +13,10 @@
 // ion_prob_uncollected are 256-ary trees over trajectory order, each node
 // summed left to right from 0.0.
 //
-// Roofline: HBM bound.  Per trajectory and pass: read 4 B key (histogram),
-// read 8 B + write 8 B (scatter); the per-bin pass reads 8 B of the sorted
-// pair plus 16 B of contribution and 8 + 16 B per bin; passes =
-// ceil(bits(grid+1)/9), each on at most 9 key bits.
+// Roofline: HBM bound.  Per trajectory: read 4 B key once for the digit counts
+// of every pass, then per pass read 8 B + write 8 B (one onesweep kernel); the
+// per-bin pass reads 8 B of the sorted pair plus 16 B of contribution and 8 +
+// 16 B per bin; passes = ceil(bits(grid+1)/9), each on at most 9 key bits.
 
 #include "engine.h"
 
@@ -30,164 +30,168 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kMaxDigitBits = 9;           // a pass sorts on up to 9 key bits
 constexpr int kMaxDigits = 1 << kMaxDigitBits;
 
-// Digit counts of one tile for a pass over `bits` key bits from `shift`,
-// digit-major: hist[d nblocks + block].
-__global__ void __launch_bounds__(kThreads)
-k_radix_hist(const uint32_t* __restrict__ keys, const unsigned long long* __restrict__ count, int shift,
-             int bits, int64_t nblocks, uint32_t* __restrict__ hist) {
-    __shared__ uint32_t h[kMaxDigits];
-    const int64_t n = (int64_t)*count;
-    const int nd = 1 << bits;
-    const uint32_t mask = (uint32_t)nd - 1u;
-    for (int d = threadIdx.x; d < nd; d += kThreads) h[d] = 0u;
-    __syncthreads();
-    const int64_t base = (int64_t)blockIdx.x * kTile;
-    for (int r = 0; r < kRounds; ++r) {
-        int64_t i = base + (int64_t)r * kThreads + threadIdx.x;
-        if (i < n) atomicAdd(&h[(keys[i] >> shift) & mask], 1u);
-    }
-    __syncthreads();
-    for (int d = threadIdx.x; d < nd; d += kThreads) hist[(int64_t)d * nblocks + blockIdx.x] = h[d];
+constexpr int kMaxPasses = 4;              // keys of up to 36 bits
+constexpr int kSub = kTile / kWarps;       // keys per warp and tile
+
+// Width and first bit of pass p of a sort over `bits` key bits in `npass` passes.
+__host__ __device__ inline void pass_digits(int bits, int npass, int p, int* w, int* shift) {
+    int sh = 0;
+    for (int q = 0; q < p; ++q) sh += bits / npass + ((q < bits % npass) ? 1 : 0);
+    *w = bits / npass + ((p < bits % npass) ? 1 : 0);
+    *shift = sh;
 }
 
-// ---- exclusive scan of a uint32 array (reduce, scan partials, scan) --------
-constexpr int kScanThreads = 1024;
-constexpr int kScanItems = 4;
-constexpr int kScanChunk = kScanThreads * kScanItems;
+// ---- onesweep LSD radix sort (Adinets & Merrill 2022) -------------------------------
+// One read of the keys counts the digits of every pass (k_onesweep_hist), one
+// block turns each pass's counts into digit offsets (k_onesweep_scan), and each
+// pass is one kernel that sorts tile after tile: a tile counts its digits, posts
+// them, takes the sum of the earlier tiles' counts per digit by decoupled
+// look-back, and scatters its keys stably.  Launches per sort: 2 + passes.
 
-__device__ __forceinline__ uint32_t block_scan_excl(uint32_t v, uint32_t* total) {
-    __shared__ uint32_t ws[32];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    uint32_t x = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
-    }
-    if (lane == 31) ws[warp] = x;
+// Digit counts of every pass: ghist[p kMaxDigits + d].
+__global__ void __launch_bounds__(kThreads)
+k_onesweep_hist(const uint32_t* __restrict__ keys, const unsigned long long* __restrict__ count, int bits,
+                int npass, uint32_t* __restrict__ ghist) {
+    __shared__ uint32_t h[kMaxPasses][kMaxDigits];
+    const int64_t n = (int64_t)*count;
+    for (int i = threadIdx.x; i < kMaxPasses * kMaxDigits; i += kThreads) (&h[0][0])[i] = 0u;
     __syncthreads();
-    if (warp == 0) {
-        uint32_t w = (lane < nw) ? ws[lane] : 0u;
+    int w[kMaxPasses], sh[kMaxPasses];
+    for (int p = 0; p < npass; ++p) pass_digits(bits, npass, p, &w[p], &sh[p]);
+    for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kThreads) {
+        const uint32_t k = keys[i];
+        for (int p = 0; p < npass; ++p) atomicAdd(&h[p][(k >> sh[p]) & ((1u << w[p]) - 1u)], 1u);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < npass * kMaxDigits; i += kThreads) {
+        const uint32_t v = (&h[0][0])[i];
+        if (v) atomicAdd(&ghist[i], v);
+    }
+}
+
+// Exclusive prefix of each pass's digit counts (one block of kMaxDigits threads).
+__global__ void __launch_bounds__(kMaxDigits)
+k_onesweep_scan(const uint32_t* __restrict__ ghist, int npass, uint32_t* __restrict__ base) {
+    __shared__ uint32_t ws[kMaxDigits / 32];
+    const int d = threadIdx.x, lane = d & 31, warp = d >> 5;
+    for (int p = 0; p < npass; ++p) {
+        const uint32_t v = ghist[p * kMaxDigits + d];
+        uint32_t x = v;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
-            if (lane >= o) w += y;
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
         }
-        if (lane < nw) ws[lane] = w;
-    }
-    __syncthreads();
-    uint32_t r = ((warp > 0) ? ws[warp - 1] : 0u) + x - v;
-    if (total) *total = ws[nw - 1];
-    __syncthreads();
-    return r;
-}
-
-__global__ void __launch_bounds__(kScanThreads)
-k_scan_reduce(const uint32_t* __restrict__ a, int64_t n, uint32_t* __restrict__ part) {
-    const int64_t base = (int64_t)blockIdx.x * kScanChunk + (int64_t)threadIdx.x * kScanItems;
-    uint32_t c = 0;
-#pragma unroll
-    for (int k = 0; k < kScanItems; ++k) c += (base + k < n) ? a[base + k] : 0u;
-    c = __reduce_add_sync(0xffffffffu, c);
-    __shared__ uint32_t ws[32];
-    if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = c;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        uint32_t s = 0;
-        for (int w = 0; w < kScanThreads / 32; ++w) s += ws[w];
-        part[blockIdx.x] = s;
-    }
-}
-
-__global__ void __launch_bounds__(kScanThreads) k_scan_partials(uint32_t* __restrict__ part, int64_t np) {
-    __shared__ uint32_t carry;
-    if (threadIdx.x == 0) carry = 0u;
-    __syncthreads();
-    for (int64_t off = 0; off < np; off += blockDim.x) {
-        int64_t i = off + threadIdx.x;
-        uint32_t v = (i < np) ? part[i] : 0u, tot;
-        uint32_t ex = block_scan_excl(v, &tot);
-        if (i < np) part[i] = carry + ex;
+        if (lane == 31) ws[warp] = x;
         __syncthreads();
-        if (threadIdx.x == 0) carry += tot;
+        uint32_t off = 0u;
+        for (int q = 0; q < warp; ++q) off += ws[q];
+        base[p * kMaxDigits + d] = off + x - v;
         __syncthreads();
     }
 }
 
-__global__ void __launch_bounds__(kScanThreads)
-k_scan_apply(uint32_t* __restrict__ a, int64_t n, const uint32_t* __restrict__ part) {
-    const int64_t base = (int64_t)blockIdx.x * kScanChunk + (int64_t)threadIdx.x * kScanItems;
-    uint32_t v[kScanItems], c = 0;
-#pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        v[k] = (base + k < n) ? a[base + k] : 0u;
-        c += v[k];
-    }
-    uint32_t run = part[blockIdx.x] + block_scan_excl(c, nullptr);
-#pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        if (base + k < n) a[base + k] = run;
-        run += v[k];
-    }
+// Posts of the look-back: a 64-bit word per (tile, digit), the count in the low 32
+// bits and above them 2p+1 ("this tile's count") or 2p+2 ("the count of this and
+// every earlier tile") for pass p, so one region, cleared once per sort, serves
+// every pass.  A wait gives up after kLookbackSpins polls (the tiles it waits for
+// belong to blocks of the same cooperative grid that took their tiles earlier,
+// so it never should) and raises *err.
+constexpr int kLookbackSpins = 1 << 22;
+
+__device__ __forceinline__ unsigned long long load_post(const unsigned long long* p) {
+    return *(const volatile unsigned long long*)p;
 }
 
-// Stable scatter of one digit (`bits` <= 9 key bits from `shift`).  Warp w of a block owns the tile's keys
-// [w kSub, (w + 1) kSub): it first counts its digits (ranks within a round of
-// 32 keys come from __match_any_sync, and only the warp's leader lanes write
-// its row of counts), one prefix over the warps then turns the rows into each
-// warp's first position per digit (after the block's offset from the scan), and
-// the warp writes its keys in index order, advancing its own offsets.  Keys
-// land in index order within each digit, as a stable sort needs, with three
-// block barriers per tile.
-constexpr int kSub = kTile / kWarps;  // keys per warp and tile
 __global__ void __launch_bounds__(kThreads)
-k_radix_scatter(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin,
-                uint32_t* __restrict__ kout, uint32_t* __restrict__ vout,
-                const unsigned long long* __restrict__ count, int shift, int bits, int64_t nblocks,
-                const uint32_t* __restrict__ offs) {
+k_onesweep_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
+                uint32_t* __restrict__ vout, const unsigned long long* __restrict__ count, int pass, int shift,
+                int bits, const uint32_t* __restrict__ base, unsigned long long* __restrict__ post,
+                unsigned int* __restrict__ tile_ctr, unsigned long long* __restrict__ err) {
     __shared__ uint32_t wc[kWarps][kMaxDigits];
+    __shared__ uint32_t toff[kMaxDigits];
+    __shared__ uint32_t s_tile;
     const int64_t n = (int64_t)*count;
+    const int64_t ntiles = (n + kTile - 1) / kTile;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const unsigned lt_mask = (1u << lane) - 1u;
     const uint32_t nd = 1u << bits, mask = nd - 1u;
-    for (uint32_t d = threadIdx.x; d < nd; d += kThreads)
-        for (int w = 0; w < kWarps; ++w) wc[w][d] = 0u;
-    __syncthreads();
-    const int64_t sub = (int64_t)blockIdx.x * kTile + (int64_t)warp * kSub;
-    for (int r = 0; r < kSub / 32; ++r) {
-        const int64_t i = sub + r * 32 + lane;
-        const uint32_t d = (i < n) ? (kin[i] >> shift) & mask : nd;
-        const unsigned peers = __match_any_sync(0xffffffffu, d);
-        if (d < nd && lane == __ffs(peers) - 1) wc[warp][d] += __popc(peers);
-    }
-    __syncthreads();
-    for (uint32_t d = threadIdx.x; d < nd; d += kThreads) {
-        uint32_t run = offs[(int64_t)d * nblocks + blockIdx.x];
-        for (int w = 0; w < kWarps; ++w) {
-            const uint32_t c = wc[w][d];
-            wc[w][d] = run;
-            run += c;
+    const unsigned long long f_own = (unsigned long long)(2 * pass + 1) << 32;
+    const unsigned long long f_inc = (unsigned long long)(2 * pass + 2) << 32;
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(tile_ctr, 1u);
+        for (uint32_t d = threadIdx.x; d < nd; d += kThreads)
+            for (int w = 0; w < kWarps; ++w) wc[w][d] = 0u;
+        __syncthreads();
+        const int64_t tile = (int64_t)s_tile;
+        if (tile >= ntiles) break;
+        // digit counts of each warp's part of the tile
+        const int64_t sub = tile * kTile + (int64_t)warp * kSub;
+        for (int r = 0; r < kSub / 32; ++r) {
+            const int64_t i = sub + r * 32 + lane;
+            const uint32_t d = (i < n) ? (kin[i] >> shift) & mask : nd;
+            const unsigned peers = __match_any_sync(0xffffffffu, d);
+            if (d < nd && lane == __ffs(peers) - 1) wc[warp][d] += __popc(peers);
         }
-    }
-    __syncthreads();
-    for (int r = 0; r < kSub / 32; ++r) {
-        const int64_t i = sub + r * 32 + lane;
-        const bool valid = i < n;
-        uint32_t key = 0u, val = 0u, d = nd;
-        if (valid) {
-            key = kin[i];
-            val = vin ? vin[i] : (uint32_t)i;
-            d = (key >> shift) & mask;
+        __syncthreads();
+        // post the tile's counts, sum the earlier tiles', post the running total
+        for (uint32_t d = threadIdx.x; d < nd; d += kThreads) {
+            uint32_t run = 0u;
+            for (int w = 0; w < kWarps; ++w) {
+                const uint32_t c = wc[w][d];
+                wc[w][d] = run;
+                run += c;
+            }
+            unsigned long long* mine = post + tile * kMaxDigits + d;
+            atomicExch(mine, (tile == 0 ? f_inc : f_own) | run);
+            uint32_t excl = 0u;
+            if (tile > 0) {
+                int64_t t = tile - 1;
+                int spins = 0;
+                while (t >= 0) {
+                    const unsigned long long v = load_post(post + t * kMaxDigits + d);
+                    const unsigned long long f = v & 0xFFFFFFFF00000000ull;
+                    if (f == f_inc) {
+                        excl += (uint32_t)v;
+                        break;
+                    }
+                    if (f == f_own) {
+                        excl += (uint32_t)v;
+                        --t;
+                        continue;
+                    }
+                    if (++spins > kLookbackSpins) {
+                        atomicExch(err, 1ull);
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+                atomicExch(mine, f_inc | (unsigned long long)(excl + run));
+            }
+            toff[d] = base[d] + excl;
         }
-        const unsigned peers = __match_any_sync(0xffffffffu, d);
-        const uint32_t pos = valid ? wc[warp][d] + __popc(peers & lt_mask) : 0u;
-        __syncwarp();
-        if (valid && lane == __ffs(peers) - 1) wc[warp][d] += __popc(peers);
-        __syncwarp();
-        if (valid) {
-            kout[pos] = key;
-            vout[pos] = val;
+        __syncthreads();
+        // stable scatter: each warp writes its keys in index order
+        for (int r = 0; r < kSub / 32; ++r) {
+            const int64_t i = sub + r * 32 + lane;
+            const bool valid = i < n;
+            uint32_t key = 0u, val = 0u, d = nd;
+            if (valid) {
+                key = kin[i];
+                val = vin ? vin[i] : (uint32_t)i;
+                d = (key >> shift) & mask;
+            }
+            const unsigned peers = __match_any_sync(0xffffffffu, d);
+            const uint32_t pos = valid ? toff[d] + wc[warp][d] + __popc(peers & lt_mask) : 0u;
+            __syncwarp();
+            if (valid && lane == __ffs(peers) - 1) wc[warp][d] += __popc(peers);
+            __syncwarp();
+            if (valid && (int64_t)pos < n) {  // (pos >= n only after a look-back gave up)
+                kout[pos] = key;
+                vout[pos] = val;
+            }
         }
+        __syncthreads();
     }
 }
 
@@ -350,7 +354,8 @@ __global__ void k_copy_count(const unsigned long long* __restrict__ count, Count
 }
 
 int64_t tiles_for(int64_t n) { return (n + kTile - 1) / kTile; }
-int64_t scan_parts_for(int64_t n) { return (n + kScanChunk - 1) / kScanChunk; }
+// digit counts and offsets of every pass, one tile counter per pass (+ padding)
+constexpr int kOnesweepAuxWords = 2 * kMaxPasses * kMaxDigits + 64;
 
 int64_t tree_size(int64_t n) {
     int64_t s = 0, m = n;
@@ -367,35 +372,68 @@ int key_bits(int64_t grid) {
     return b;
 }
 
+// Blocks of k_onesweep_pass that fit on the device at once (its grid: the
+// look-back waits only for tiles taken earlier, by blocks of the same
+// co-resident, cooperative grid).
+int onesweep_blocks() {
+    static int cached[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return 152;
+    }
+    if (!cached[dev]) {
+        int per_sm = 0, sms = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_onesweep_pass, kThreads, 0) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || per_sm < 1 ||
+            sms < 1) {
+            cudaGetLastError();
+            return 152;
+        }
+        cached[dev] = per_sm * sms;
+    }
+    return cached[dev];
+}
+
 // Stable LSD radix sort of (key, index) pairs on the low `bits` key bits, in as
 // few passes of at most kMaxDigitBits as cover them (20 bits: 7 + 7 + 6; 25:
-// 9 + 8 + 8).  Wider digits would save the 20-bit case a pass, but two
-// 1024-digit passes measured slower than three narrow ones (larger histogram
-// scans, writes spread over more runs).  The order is the same for any split: by key, then by index.  The
-// sorted pairs are left in the buffers *kout, *vout point to.
+// 9 + 8 + 8).  The order is the same for any split: by key, then by index.
+// The sorted pairs are left in the buffers *kout, *vout point to.  `post` holds
+// kMaxDigits words per tile, `aux` the digit counts, offsets and tile counters
+// (kOnesweepAuxWords), `err` is raised by a look-back that gives up.
 int radix_sort(const uint32_t* keys, const unsigned long long* count, int64_t max_n, int bits,
-               uint32_t* const kbuf[2], uint32_t* const vbuf[2], uint32_t* hist, uint32_t* scan_tmp,
-               const uint32_t** kout, const uint32_t** vout, cudaStream_t s) {
+               uint32_t* const kbuf[2], uint32_t* const vbuf[2], unsigned long long* post, uint32_t* aux,
+               unsigned long long* err, const uint32_t** kout, const uint32_t** vout, cudaStream_t s) {
     const int64_t nb = tiles_for(max_n);
     const int npass = (bits + kMaxDigitBits - 1) / kMaxDigitBits;
+    uint32_t* ghist = aux;
+    uint32_t* base = aux + kMaxPasses * kMaxDigits;
+    unsigned int* tile_ctr = aux + 2 * kMaxPasses * kMaxDigits;
+    cudaMemsetAsync(aux, 0, sizeof(uint32_t) * kOnesweepAuxWords, s);
+    cudaMemsetAsync(post, 0, sizeof(unsigned long long) * (size_t)nb * kMaxDigits, s);
+    int hblocks = onesweep_blocks();
+    if ((int64_t)hblocks > nb) hblocks = (int)nb;
+    k_onesweep_hist<<<hblocks, kThreads, 0, s>>>(keys, count, bits, npass, ghist);
+    k_onesweep_scan<<<1, kMaxDigits, 0, s>>>(ghist, npass, base);
+    int launches = 2;
     const uint32_t* kin = keys;
     const uint32_t* vin = nullptr;
-    int which = 0, launches = 0;
-    for (int p = 0, shift = 0; p < npass; ++p) {
-        const int w = bits / npass + ((p < bits % npass) ? 1 : 0);
-        const int64_t hist_n = ((int64_t)1 << w) * nb;
-        const int64_t parts = scan_parts_for(hist_n);
-        k_radix_hist<<<(unsigned)nb, kThreads, 0, s>>>(kin, count, shift, w, nb, hist);
-        k_scan_reduce<<<(unsigned)parts, kScanThreads, 0, s>>>(hist, hist_n, scan_tmp);
-        k_scan_partials<<<1, kScanThreads, 0, s>>>(scan_tmp, parts);
-        k_scan_apply<<<(unsigned)parts, kScanThreads, 0, s>>>(hist, hist_n, scan_tmp);
-        k_radix_scatter<<<(unsigned)nb, kThreads, 0, s>>>(kin, vin, kbuf[which], vbuf[which], count, shift, w, nb,
-                                                           hist);
-        launches += 5;
-        kin = kbuf[which];
-        vin = vbuf[which];
+    int which = 0;
+    const int grid = (int)std::min<int64_t>(nb, onesweep_blocks());
+    for (int p = 0; p < npass; ++p) {
+        int w = 0, shift = 0;
+        pass_digits(bits, npass, p, &w, &shift);
+        uint32_t* ko = kbuf[which];
+        uint32_t* vo = vbuf[which];
+        const uint32_t* bp = base + p * kMaxDigits;
+        unsigned int* tc = tile_ctr + p;
+        void* args[] = {(void*)&kin, (void*)&vin, (void*)&ko, (void*)&vo, (void*)&count, (void*)&p,
+                        (void*)&shift, (void*)&w, (void*)&bp, (void*)&post, (void*)&tc, (void*)&err};
+        cudaLaunchCooperativeKernel((const void*)k_onesweep_pass, dim3(grid), dim3(kThreads), args, 0, s);
+        ++launches;
+        kin = ko;
+        vin = vo;
         which ^= 1;
-        shift += w;
     }
     *kout = kin;
     *vout = vin;
@@ -406,11 +444,10 @@ int radix_sort(const uint32_t* keys, const unsigned long long* count, int64_t ma
 
 size_t deposit_scratch_bytes(int64_t max_n) {
     int64_t nb = tiles_for(max_n > 0 ? max_n : 1);
-    int64_t hist = (int64_t)kMaxDigits * nb;
     size_t bytes = 0;
     bytes += 4 * (size_t)max_n * sizeof(uint32_t) + 4 * 256;  // keys a/b, vals a/b
-    bytes += (size_t)hist * sizeof(uint32_t) + 256;
-    bytes += (size_t)(scan_parts_for(hist) + 64) * sizeof(uint32_t) + 256;
+    bytes += (size_t)nb * kMaxDigits * sizeof(unsigned long long) + 256;
+    bytes += (size_t)kOnesweepAuxWords * sizeof(uint32_t) + 256;
     bytes += 2 * (size_t)tree_size(max_n) * sizeof(double) + 512;
     return bytes;
 }
@@ -420,13 +457,12 @@ void deposit_scratch_carve(void* base, int64_t max_n, DepositScratch* d) {
     char* p = (char*)base;
     size_t off = 0;
     int64_t nb = tiles_for(max_n > 0 ? max_n : 1);
-    int64_t hist = (int64_t)kMaxDigits * nb;
     d->keys_a = (uint32_t*)(p + off); off = align(off + (size_t)max_n * 4);
     d->keys_b = (uint32_t*)(p + off); off = align(off + (size_t)max_n * 4);
     d->vals_a = (uint32_t*)(p + off); off = align(off + (size_t)max_n * 4);
     d->vals_b = (uint32_t*)(p + off); off = align(off + (size_t)max_n * 4);
-    d->hist = (uint32_t*)(p + off); off = align(off + (size_t)hist * 4);
-    d->scan_tmp = (uint32_t*)(p + off); off = align(off + (size_t)(scan_parts_for(hist) + 64) * 4);
+    d->post = (unsigned long long*)(p + off); off = align(off + (size_t)nb * kMaxDigits * 8);
+    d->aux = (uint32_t*)(p + off); off = align(off + (size_t)kOnesweepAuxWords * 4);
     int64_t ts = tree_size(max_n);
     d->tree_a = (double*)(p + off); off = align(off + (size_t)ts * 8);
     d->tree_b = (double*)(p + off);
@@ -446,7 +482,8 @@ int launch_deposit(const DJob& J, const TrajOut& out, const unsigned long long* 
         uint32_t* kbuf[2] = {d.keys_a, d.keys_b};
         uint32_t* vbuf[2] = {d.vals_a, d.vals_b};
         const uint32_t *kin = nullptr, *vin = nullptr;
-        launches += radix_sort(out.key, count, max_n, key_bits(grid), kbuf, vbuf, d.hist, d.scan_tmp, &kin, &vin, s);
+        launches += radix_sort(out.key, count, max_n, key_bits(grid), kbuf, vbuf, d.post, d.aux,
+                               &counters->sort_err, &kin, &vin, s);
         launches += launch_bin_sums(kin, vin, count, max_n, grid, out.c_re, out.c_im, coherent, spec_re,
                                     spec_im, s);
         // canonical 256-ary trees for ion_prob and ion_prob_uncollected
@@ -678,7 +715,7 @@ int launch_weighted_sum(const double* mspec, int n_inst, int64_t grid, const dou
 // of (bin, electron), per-bin sums in electron order, |A|^2) on caller-owned
 // inputs and outputs, with its sort scratch in one fixed device array declared
 // below.  The array's size is fixed at build time (kNoallocMaxN contributions,
-// about 10 MiB) and every GPU that loads this library holds it until the
+// about 10.5 MiB) and every GPU that loads this library holds it until the
 // process exits.  Keys above the grid are taken as the grid ("not deposited")
 // before the sort, so a bad key can neither alias a bin nor leave the sort's
 // key range.
@@ -690,12 +727,10 @@ namespace {
 
 constexpr int64_t kNoallocMaxN = (int64_t)1 << 19;
 constexpr int64_t kNoallocTiles = (kNoallocMaxN + kTile - 1) / kTile;
-constexpr int64_t kNoallocHist = (int64_t)kMaxDigits * kNoallocTiles;
-constexpr int64_t kNoallocParts = (kNoallocHist + kScanChunk - 1) / kScanChunk;
-// layout: clamped keys | keys_a | keys_b | vals_a | vals_b | hist | scan partials | count
-constexpr size_t kNoallocOffHist = (size_t)5 * kNoallocMaxN * sizeof(uint32_t);
-constexpr size_t kNoallocOffParts = kNoallocOffHist + (size_t)kNoallocHist * sizeof(uint32_t);
-constexpr size_t kNoallocOffCount = (kNoallocOffParts + (size_t)(kNoallocParts + 64) * sizeof(uint32_t) + 255) & ~(size_t)255;
+// layout: clamped keys | keys_a | keys_b | vals_a | vals_b | look-back posts | aux | count, error flag
+constexpr size_t kNoallocOffPost = (size_t)5 * kNoallocMaxN * sizeof(uint32_t);
+constexpr size_t kNoallocOffAux = kNoallocOffPost + (size_t)kNoallocTiles * kMaxDigits * sizeof(unsigned long long);
+constexpr size_t kNoallocOffCount = (kNoallocOffAux + (size_t)kOnesweepAuxWords * sizeof(uint32_t) + 255) & ~(size_t)255;
 constexpr size_t kNoallocBytes = kNoallocOffCount + 256;
 
 constexpr int kMaxDevices = 64;
@@ -770,9 +805,10 @@ extern "C" int etraj_deposit_noalloc(int64_t n, const uint32_t* key, const doubl
     uint32_t* kclamp = (uint32_t*)p;
     uint32_t* kbuf[2] = {(uint32_t*)p + kNoallocMaxN, (uint32_t*)p + 2 * kNoallocMaxN};
     uint32_t* vbuf[2] = {(uint32_t*)p + 3 * kNoallocMaxN, (uint32_t*)p + 4 * kNoallocMaxN};
-    uint32_t* hist = (uint32_t*)(p + kNoallocOffHist);
-    uint32_t* parts = (uint32_t*)(p + kNoallocOffParts);
+    unsigned long long* post = (unsigned long long*)(p + kNoallocOffPost);
+    uint32_t* aux = (uint32_t*)(p + kNoallocOffAux);
     unsigned long long* count = (unsigned long long*)(p + kNoallocOffCount);
+    unsigned long long* err = count + 1;
     // the outputs start at zero; the scratch keeps the previous call's contents and
     // every part of it that is read is written first (count, histograms, sorted pairs)
     cudaMemsetAsync(spec_re, 0, (size_t)grid * sizeof(double), s);
@@ -783,7 +819,7 @@ extern "C" int etraj_deposit_noalloc(int64_t n, const uint32_t* key, const doubl
         int cblocks = (int)((n + 255) / 256);
         if (cblocks > sms * 8) cblocks = sms * 8;
         k_clamp_keys<<<cblocks, 256, 0, s>>>(key, n, (uint32_t)grid, kclamp);
-        radix_sort(kclamp, count, n, key_bits(grid), kbuf, vbuf, hist, parts, &kin, &vin, s);
+        radix_sort(kclamp, count, n, key_bits(grid), kbuf, vbuf, post, aux, err, &kin, &vin, s);
         launch_bin_sums(kin, vin, count, n, grid, c_re, c_im, coherent, spec_re, spec_im, s);
     }
     int fblocks = (int)((grid + 255) / 256);

@@ -294,7 +294,11 @@ DFS_HD df half_sq(const df* p) {
 }
 
 // The target's terms evaluated directly at state (X, Pm); KT = coef X; kph the phase rate.
-template <int DIM, int PHASE, int TGT>
+// Beyond r2_far (an SAE electron far from the core) every exp(-b_i r) is exactly
+// 0, so br = num = Z and coef = -y^3 Z: the same bits the full formulas give
+// there (adding an exact zero to a normalized pair changes nothing), without r
+// and the brackets -- unless NEED_R (the start-up pass, whose differences read r).
+template <int DIM, int PHASE, int TGT, bool NEED_R = true>
 DFS_HD void target_at(const DFParams& P, const float* exptab, const df* X, const df* Pm, TAt& T, df* KT, df& kph) {
     T.r2 = df_add(df_sqr(X[0]), df_sqr(X[1]));
     if (DIM == 3) T.r2 = df_add(T.r2, df_sqr(X[2]));
@@ -302,6 +306,10 @@ DFS_HD void target_at(const DFParams& P, const float* exptab, const df* X, const
     T.y3 = df_mul(df_sqr(T.y), T.y);
     if (TGT == ETRAJ_TARGET_HYDROGEN_LIKE) {
         T.coef = df_neg(df_mul(d2(P.Z), T.y3));
+    } else if (!NEED_R && T.r2.hi > P.r2_far) {
+        T.e1 = T.e2 = T.e3 = df{0.0f, 0.0f};
+        T.br = T.num = d2(P.Z);
+        T.coef = df_neg(df_mul(T.y3, T.br));
     } else {
         T.r = df_sqrt(T.r2);
         T.e1 = sae_exp(d2(P.b1), T.r, exptab);
@@ -499,6 +507,17 @@ DFS_HD void set_diff(const Lane<DIM, PHASE>& L, const Slots<KW>& k, int l, const
     if (Lane<DIM, PHASE>::HASPH) k.set(l, DIM, dkph);
 }
 
+// The main pass keeps each stage's whole derivative instead: K_l = KT - F (the
+// momentum rows, formed as set_base forms K_0) and the phase rate, into slot l.
+template <int DIM, int PHASE, int KW>
+DFS_HD void set_full(const Lane<DIM, PHASE>& L, const Slots<KW>& k, int l, const FieldAt& F, const df* KT,
+                     df kph) {
+    k.set(l, 0, df_sub(KT[0], df_add(c0_df(F.c0x), F.qx)));
+    k.set(l, 1, df_sub(KT[1], df_add(c0_df(F.c0y), F.qy)));
+    if (DIM == 3) k.set(l, 2, KT[2]);
+    if (Lane<DIM, PHASE>::HASPH) k.set(l, DIM, kph);
+}
+
 // sqrt(sum_j (v_j / sk_j)^2 / N)
 template <int N>
 DFS_HD df rms_ratio(const df* v, const df* sk) {
@@ -626,14 +645,16 @@ struct Acc {
 
 // The increments and clock of stage st (1..6; 6 is the new state):
 // dP = dt ((sum_l A_l) K_0 + sum_l A_l dK_l) and
-// dX = (sum_l A_l) dt p0 + dt^2 ((sum_l (A A)_l) K_0 + sum_l (A A)_l dK_l).
+// dX = (sum_l A_l) dt p0 + dt^2 ((sum_l (A A)_l) K_0 + sum_l (A A)_l dK_l);
+// with FULL slots (the main pass) the same sums over K_0 .. K_{st-1}.
 // st is the same for every stepping lane of a warp, so the coefficients are
 // uniform constant-memory reads and one copy of the code serves all stages.
-template <int DIM, int PHASE, int KW>
+template <bool FULL, int DIM, int PHASE, int KW>
 DFS_HD void stage_in(Lane<DIM, PHASE>& L, const Slots<KW>& k, int st) {
     const df adt = df_mul(DFS_T RA[st], L.dt);
     for (int d = 0; d < DIM; ++d) {
-        Acc sa(df_mul(DFS_T RA[st], L.K0[d])), saa(df_mul(DFS_T RAA[st], L.K0[d]));
+        Acc sa(df_mul(FULL ? DFS_T A[st][0] : DFS_T RA[st], L.K0[d])),
+            saa(df_mul(FULL ? DFS_T AA[st][0] : DFS_T RAA[st], L.K0[d]));
         for (int l = 1; l < st; ++l) {
             const df kl = k.get(l, d);
             sa.add(DFS_T A[st][l], kl);
@@ -673,8 +694,8 @@ DFS_HD void target_eval(const DFParams& P, const float* exptab, const Lane<DIM, 
             Xl[d] = df_add(L.X[d], L.dX[d]);
             Pl[d] = df_add(L.Pv[d], L.dP[d]);
         }
-        target_at<DIM, PHASE, TGT>(P, exptab, Xl, Pl, T, KT, kph);
-        if (!ok) {
+        target_at<DIM, PHASE, TGT, DIFF>(P, exptab, Xl, Pl, T, KT, kph);
+        if (!ok && DIFF) {  // (the main pass keeps whole derivatives, set_full)
             for (int d = 0; d < DIM; ++d) dKT[d] = df_sub(KT[d], L.KT0[d]);
             dkph = df_sub(kph, L.kph0);
         }
@@ -686,25 +707,29 @@ DFS_HD void target_eval(const DFParams& P, const float* exptab, const Lane<DIM, 
 // status > 0 on failure (3 Unstable, 4 DtNaN), 0 to go on; after an accepted step
 // that goes on (L.accept) the caller makes stage 6's direct target terms the new
 // state's (set_base with the laser table L.F5).
-template <int DIM, int PHASE, int KW>
+template <bool FULL, int DIM, int PHASE, int KW>
 DFS_HD int epilogue(Lane<DIM, PHASE>& L, const DFParams& P, const Slots<KW>& k, const Tabs& T) {
     constexpr bool HASPH = Lane<DIM, PHASE>::HASPH;
     constexpr int N = Lane<DIM, PHASE>::N;
     df dPH = df{0.0f, 0.0f};
     if (HASPH) {
-        Acc a(df_mul(DFS_T RA[6], L.kph0));
+        Acc a(df_mul(FULL ? DFS_T A[6][0] : DFS_T RA[6], L.kph0));
 #pragma unroll
         for (int l = 1; l < 6; ++l) a.add(DFS_T A[6][l], k.get(l, DIM));
         dPH = df_mul(L.dt, a.get());
     }
     const df PHn = df_add(L.PH, dPH);
     // RMS of the error estimate over the scales abstol + rtol max(|u_prev|, |u_new|);
-    // the weights of K_0 (sum bt, sum bt A) are 0
+    // the weights of K_0 (sum bt, sum bt A) are 0 on differences
     df acc = df{0.0f, 0.0f};
     df Xn[DIM], Pn[DIM];
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
         Acc ex, ep;
+        if (FULL) {
+            ex = Acc(df_mul(DFS_T BTA[0], L.K0[d]));
+            ep = Acc(df_mul(DFS_T BT[0], L.K0[d]));
+        }
 #pragma unroll
         for (int l = 1; l < 7; ++l) {
             const df kl = k.get(l, d);
@@ -721,6 +746,7 @@ DFS_HD int epilogue(Lane<DIM, PHASE>& L, const DFParams& P, const Slots<KW>& k, 
     }
     if (HASPH) {
         Acc ef;
+        if (FULL) ef = Acc(df_mul(DFS_T BT[0], L.kph0));
 #pragma unroll
         for (int l = 1; l < 7; ++l) ef.add(DFS_T BT[l], k.get(l, DIM));
         const df scf = df_fma(df_max(df_abs(L.PH), df_abs(PHn)), d2(P.rtol), dfc(kAbstol));

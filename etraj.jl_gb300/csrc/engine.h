@@ -150,6 +150,7 @@ struct Counters {
     unsigned long long n_failed;
     unsigned long long n_ionized;
     unsigned long long n_steps;
+    unsigned long long sort_err;  // nonzero: a look-back wait of the deposit's sort gave up
 };
 
 // ---- launchers (all stream-ordered; each returns the number of kernel launches) ----
@@ -157,8 +158,12 @@ int launch_batch_prepare(const DJob& J, const double* t, DBatch* batches, cudaSt
 // Samples the candidates of time samples [b0, b0+nb) (flag and SoA indexed by
 // b * n_cand + i).
 int launch_sample_range(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
-                        const DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
+                        DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
                         cudaStream_t s);
+// The FP64 SPA sampler's FP32 pre-pass (atoms): fills batches[b].spa and sets
+// flag = 0 for the candidates whose FP32 rate is more than 1e4 below the cutoff.
+int launch_spa_prefilter(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
+                         DBatch* batches, uint8_t* flag, int sm_count, cudaStream_t s);
 // FP32 variant of the same kernel for the bulk path (sampler_fp32.cu); used
 // when the rate cutoff keeps every kept rate in FP32's normal range.
 // Its SPA variant first fills batches[b].spa of the batches it samples.
@@ -264,6 +269,7 @@ struct DFParams {
     float2 rtol;
     float t_snap;         // 100 ulp of t_final: a step ending closer than this ends the solve
     float2 Z, Ip, sc, a1, b1, a2, b2, a3, b3, a2b2;
+    float r2_far;         // SAE: r^2 beyond which every exp(-b_i r) of the potential is 0
     int max_iters;
     int threads, blocks;    // launch shape of the start-up pass (persistent grid)
     int blocks_main;        // blocks of the main pass (threads each)
@@ -294,9 +300,9 @@ int df_blocks_per_sm(int dim, int phase, int tgt, bool main, int threads);
 // Deterministic deposit: stable radix sort of (key, survivor) and segmented sums.
 struct DepositScratch {
     uint32_t *keys_a, *keys_b, *vals_a, *vals_b;
-    uint32_t* hist;       // 256 * nblocks
-    uint32_t* scan_tmp;   // scan partials
-    double* tree_a;       // canonical-sum partials
+    unsigned long long* post;  // the sort's look-back posts: 512 per tile of 4096 keys
+    uint32_t* aux;             // digit counts, digit offsets, tile counters
+    double* tree_a;            // canonical-sum partials
     double* tree_b;
 };
 size_t deposit_scratch_bytes(int64_t max_n);

@@ -170,7 +170,7 @@ k_integrate_df(const __grid_constant__ DFParams P, InitSoA soa, const double* __
             if (__ballot_sync(FULL, mode != kFree) == 0u) break;
         }
         // ---- the inputs of this turn's evaluation ------------------------------------------
-        if (mode == kStep) dfs::stage_in(L, ks, st);
+        if (mode == kStep) dfs::stage_in<MAIN>(L, ks, st);
         // ---- one evaluation: the laser table, and the target's terms at the new point
         //      directly (an accepted state: a new electron's, stage 6's; every stage of
         //      the main pass) and/or as the change from the accepted state (start-up) ------
@@ -188,14 +188,15 @@ k_integrate_df(const __grid_constant__ DFParams P, InitSoA soa, const double* __
                 dfs::set_base(L, F, KT, kph);
                 mode = (!MAIN && dfs::init_first(L, P)) ? kInit1 : kWait;
             } else {
-                dfs::set_diff(L, ks, (mode == kInit1) ? 1 : st, F, dKT, dkph);
+                if (MAIN) dfs::set_full(L, ks, st, F, KT, kph);
+                else dfs::set_diff(L, ks, (mode == kInit1) ? 1 : st, F, dKT, dkph);
                 if (mode == kInit1) {
                     dfs::init_second(L, P, ks, T);
                     mode = kWait;
                 } else if (st == 5) {
                     L.F5 = F;
                 } else if (step6) {
-                    const int status = dfs::epilogue(L, P, ks, T);
+                    const int status = dfs::epilogue<MAIN>(L, P, ks, T);
                     if (status) {
                         finish(status < 0 ? 0 : status);
                     } else if (L.accept) {

@@ -116,6 +116,13 @@ inline void prepare_df_params(const DJob& J, double tmin, int64_t max_n, DFParam
     D.a2 = df_split2(T_.a2); D.b2 = df_split2(T_.b2);
     D.a3 = df_split2(T_.a3); D.b3 = df_split2(T_.b3);
     D.a2b2 = df_split2(T_.a2 * T_.b2);
+    // beyond r^2 = r2_far every b_i r exceeds the exponentials' skip bound (50) by a
+    // margin that rounding cannot close, so each exp(-b_i r) is taken as 0 there
+    {
+        const double bmin = std::min(T_.b1, std::min(T_.b2, T_.b3));
+        const double rf = 50.0 / bmin;
+        D.r2_far = (bmin > 0.0) ? (float)(rf * rf * (1.0 + 1.0 / 1024.0)) : INFINITY;
+    }
     D.max_iters = kBulkMaxIters;
     D.max_n = max_n;
 }

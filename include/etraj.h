@@ -382,7 +382,7 @@ int etraj_stage_times(etraj_ctx* ctx, double* ms, int n);
  * Work is queued on cuda_stream (NULL = legacy default stream); the call
  * returns without synchronizing.  The sort scratch is one fixed device array
  * of the library, sized for at most 524288 (2^19) contributions per call
- * (about 10 MiB, held by every GPU that loads the library until the process
+ * (about 10.5 MiB, held by every GPU that loads the library until the process
  * exits); larger n returns ETRAJ_ERR_INVALID_ARGUMENT.  That array comes into
  * being when the library's device code is loaded on a device, which with
  * CUDA's lazy module loading can be this entry point's first call: make that

@@ -63,15 +63,17 @@ void solve_all(const DFParams& P, int64_t n, const double* init, double* final_s
             st = dfs::prologue(L, P);
             if (st) break;
             for (int s = 1; s <= 6; ++s) {
-                dfs::stage_in(L, ks, s);
+                if (main) dfs::stage_in<true>(L, ks, s);
+                else dfs::stage_in<false>(L, ks, s);
                 if (s == 6) F = L.F5;  // stage 6 is at stage 5's time
                 else dfs::field_at(P, L.ni, L.fi, F);
                 dfs::target_eval<DIM, PHASE, TGT, true>(P, T.exp2, L, B, !main, main || s == 6, Tl, KT, dKT, dkph,
                                                         kph);
-                dfs::set_diff(L, ks, s, F, dKT, dkph);
+                if (main) dfs::set_full(L, ks, s, F, KT, kph);
+                else dfs::set_diff(L, ks, s, F, dKT, dkph);
                 if (s == 5) L.F5 = F;
             }
-            st = dfs::epilogue(L, P, ks, T);
+            st = main ? dfs::epilogue<true>(L, P, ks, T) : dfs::epilogue<false>(L, P, ks, T);
             if (st) break;
             if (L.accept) {
                 B = Tl;
