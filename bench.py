@@ -113,16 +113,16 @@ FLOPS_PER_STEP_SAE_2D_SCTS = 702
 INTEGRATOR_DRAM_BYTES_PER_ELECTRON = 30.48
 # The double-float integrator (start-up and main pass) on the same workload, from one
 # ncu capture of both passes on a 4e5-candidate case (400 time samples: 161,722
-# electrons, 6,489,342 step attempts): FP32 thread instructions
-# (smsp__sass_thread_inst_executed_op_fp32_pred_on: 4.07e9 start-up + 4.463e10
-# main; 71 % FADD, 19 % FFMA, 7 % FMUL) per step attempt, and DRAM bytes (read +
-# write, 14.52 MB + 16.71 MB) per electron.  At that size the carry buffer between
+# electrons, 6,489,343 step attempts): FP32 thread instructions
+# (smsp__sass_thread_inst_executed_op_fp32_pred_on: 4.07e9 start-up + 3.928e10
+# main; 68 % FADD, 21 % FFMA, 8 % FMUL) per step attempt, and DRAM bytes (read +
+# write, 14.53 MB + 16.04 MB) per electron.  At that size the carry buffer between
 # the passes (116 B per electron) stays in L2; at full size it adds about that much
 # per electron again.  FMA-pipe issue (sm__inst_executed_pipe_fma, warp
-# instructions against 4 per SM and cycle) was 35.9 % (start-up) and 40.8 % (main).
-DF_FP32_INST_PER_STEP = 7505
-DF_DRAM_BYTES_PER_ELECTRON = 193.1
-DF_FMA_PIPE_ISSUE_NCU = {"start_up": 0.359, "main": 0.408}
+# instructions against 4 per SM and cycle) was 35.3 % (start-up) and 41.5 % (main).
+DF_FP32_INST_PER_STEP = 6680
+DF_DRAM_BYTES_PER_ELECTRON = 189.0
+DF_FMA_PIPE_ISSUE_NCU = {"start_up": 0.353, "main": 0.415}
 
 
 def rank_env():
@@ -722,7 +722,8 @@ def autotune_report(eng, job, batch_jobs):
             row[tag + "_integrate_ms"] = statistics.mean(vals) if vals else None
         j0 = job if name == "headline" else batch_jobs[0]
         t, b, r, tuned = eng.bulk_tile(j0.dimension, j0.traj_phase_method, j0.target.kind, name != "headline")
-        row["tile"] = {"threads": t, "blocks_per_sm": b, "refill_min": r, "tuned": tuned}
+        chunk, _ = eng.bulk_step_chunk(j0.dimension, j0.traj_phase_method, j0.target.kind, name != "headline")
+        row["tile"] = {"threads": t, "blocks_per_sm": b, "refill_min": r, "step_chunk": chunk, "tuned": tuned}
         out[name] = row
     fixed.close()
     return out

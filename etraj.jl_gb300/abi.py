@@ -27,6 +27,7 @@ SAMPLER_ADK, SAMPLER_SPANE, SAMPLER_SPA, SAMPLER_WFAT = 0, 1, 2, 3
 PREFIX_PRE, PREFIX_PRECC, PREFIX_JAC = 1, 2, 4
 PHASE_CTMC, PHASE_QTMC, PHASE_SCTS = 0, 1, 2
 PRECISION_FP64, PRECISION_FP32_BULK, PRECISION_FP32_DF = 0, 1, 2
+PROPOSAL_UNIFORM, PROPOSAL_ADK_GAUSS = 0, 1
 
 
 class MonoLaser(C.Structure):
@@ -66,7 +67,7 @@ class Job(C.Structure):
                 ("ss_kz_max", C.c_double), ("ss_kz_num", C.c_int64),
                 ("mc_kt_num", C.c_int64), ("mc_kd_max", C.c_double), ("mc_kz_max", C.c_double),
                 ("sample_cutoff_limit", C.c_double), ("seed", C.c_uint64),
-                ("laser", Laser), ("target", Target)]
+                ("laser", Laser), ("target", Target), ("mc_kt_proposal", C.c_int32), ("reserved2", C.c_int32)]
 
     @property
     def rows(self):
@@ -136,6 +137,8 @@ SIGNATURES = [
     ("etraj_bulk_tile", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, _I32P, _I32P, _I32P]),
     ("etraj_set_bulk_tile", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                       C.c_int]),
+    ("etraj_bulk_step_chunk", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int)]),
+    ("etraj_set_bulk_step_chunk", C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int]),
     ("etraj_set_straggler_repack", C.c_int, [C.c_void_p, C.c_int]),
     ("etraj_set_static_assignment", C.c_int, [C.c_void_p, C.c_int]),
     ("etraj_set_keep_final_states", C.c_int, [C.c_void_p, C.c_int]),

@@ -34,7 +34,7 @@ using namespace etraj;
 
 namespace etraj {
 int launch_sample_range(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
-                        const DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
+                        DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
                         cudaStream_t s);
 }
 
@@ -144,6 +144,12 @@ int validate_job(const etraj_job* job, std::string& err) {
     if (job->precision != ETRAJ_PRECISION_FP64 && job->precision != ETRAJ_PRECISION_FP32_BULK &&
         job->precision != ETRAJ_PRECISION_FP32_DF)
         return fail("unknown precision.");
+    if (job->mc_kt_proposal != ETRAJ_PROPOSAL_UNIFORM && job->mc_kt_proposal != ETRAJ_PROPOSAL_ADK_GAUSS)
+        return fail("unknown mc_kt_proposal.");
+    if (job->mc_kt_proposal == ETRAJ_PROPOSAL_ADK_GAUSS &&
+        (!job->sample_monte_carlo ||
+         (job->init_cond_method != ETRAJ_SAMPLER_ADK && job->init_cond_method != ETRAJ_SAMPLER_SPANE)))
+        return fail("mc_kt_proposal ADK_GAUSS applies to Monte-Carlo ADK and SPANE sampling only.");
     if (job->rate_prefix & ~7) return fail("[ADKSampler] Undefined tunneling rate prefix.");
     if ((job->rate_prefix & ETRAJ_PREFIX_PRE) && (job->rate_prefix & ETRAJ_PREFIX_PRECC))
         return fail("[ADKSampler] Rate prefixes [Pre] & [PreCC] conflict.");
@@ -358,6 +364,8 @@ void prepare_job(const etraj_job* job, HostJob& H) {
         double kd_span = (job->mc_kd_max > 0.0) ? 2.0 * job->mc_kd_max : 1.0;
         double kz_span = (job->mc_kz_max > 0.0) ? 2.0 * job->mc_kz_max : 1.0;
         J.dkdt = ((t_step * kd_span) * kz_span) / (double)job->mc_kt_num;
+        J.gauss = (job->mc_kt_proposal == ETRAJ_PROPOSAL_ADK_GAUSS) ? 1 : 0;
+        J.dkdt_base = (J.dim == 3 ? t_step : t_step * kz_span) / (double)job->mc_kt_num;
         J.n_cand = job->mc_kt_num;
         J.n_kd = 1;
         J.n_kz = 1;
@@ -426,6 +434,7 @@ struct PinnedBlock {
 // Launch shape of the bulk integrator.
 struct BulkTile {
     int threads, blocks_per_sm, refill_min, occ;
+    int chunk;  // step chunk: round 0's step budget per electron (round r: chunk 16^r)
 };
 
 }  // namespace
@@ -639,7 +648,8 @@ int alloc_outputs(etraj_ctx* ctx, const DJob& J, int64_t max_n, bool with_state,
 // range; SPA for atoms), the FP64 path and molecular SPA in FP64.
 int launch_sampler(int precision, const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
                    DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count, cudaStream_t s) {
-    const bool fp32 = precision == ETRAJ_PRECISION_FP32_BULK &&
+    // (a Gaussian-proposal job samples in FP64 on every path)
+    const bool fp32 = precision == ETRAJ_PRECISION_FP32_BULK && !J.gauss &&
                       (J.method == ETRAJ_SAMPLER_SPA ? !J.mol.on : J.cutoff >= kSample32MinCutoff);
     return fp32 ? launch_sample32_range(J, b0, nb, kd, kz, batches, soa, flag, sm_count, s)
                 : launch_sample_range(J, b0, nb, kd, kz, batches, soa, flag, sm_count, s);
@@ -785,10 +795,13 @@ bool find_tile(etraj_ctx* ctx, int key, BulkTile* t) {
     return true;
 }
 
-constexpr BulkTile kTileCandidates[] = {{256, 2, 4, 2}, {256, 2, 8, 2}, {256, 2, 2, 2}, {256, 2, 16, 2},
-                                        {128, 4, 4, 2}, {128, 4, 8, 2}, {128, 3, 4, 2}, {64, 8, 4, 2},
-                                        {256, 3, 4, 3}, {256, 3, 8, 3}, {128, 6, 4, 3}, {128, 6, 8, 3}};
-constexpr BulkTile kTileDefault = {256, 2, 4, 2};
+constexpr BulkTile kTileCandidates[] = {{256, 2, 4, 2, 1024}, {256, 2, 8, 2, 1024}, {256, 2, 2, 2, 1024},
+                                        {256, 2, 16, 2, 1024}, {128, 4, 4, 2, 1024}, {128, 4, 8, 2, 1024},
+                                        {128, 3, 4, 2, 1024}, {64, 8, 4, 2, 1024},   {256, 3, 4, 3, 1024},
+                                        {256, 3, 8, 3, 1024}, {128, 6, 4, 3, 1024}, {128, 6, 8, 3, 1024}};
+// step chunks the tuner tries once the shape is chosen (with rounds on)
+constexpr int kChunkCandidates[] = {256, 4096};
+constexpr BulkTile kTileDefault = {256, 2, 4, 2, 1024};
 
 // Stage events: inside a stream capture they become event-record nodes of the graph.
 void rec(etraj_ctx* ctx, cudaEvent_t e, cudaStream_t s) {
@@ -803,6 +816,7 @@ void apply_tile(BulkParams& B, const BulkTile& t) {
     B.blocks_per_sm = t.blocks_per_sm;
     B.refill_min = t.refill_min;
     B.occ = t.occ;
+    B.chunk0 = t.chunk > 0 ? t.chunk : 1024;
     const size_t tb = (size_t)B.n_int * 2 * sizeof(float4);
     B.table_in_smem = (B.n_inst == 0 && tb <= (size_t)96 * 1024 && tb * (size_t)t.blocks_per_sm <= (size_t)200 * 1024)
                           ? 1 : 0;
@@ -862,6 +876,35 @@ int tuned_bulk_launch(etraj_ctx* ctx, BulkParams& B, const InitSoA& soa, const d
             if (m < best) {
                 best = m;
                 bt = kTileCandidates[c];
+            }
+        }
+        // second stage: the step chunk of the rounds, with the chosen shape
+        if (B.park_buf) {
+            const int nk = (int)(sizeof kChunkCandidates / sizeof kChunkCandidates[0]);
+            for (int rep = 0; rep < 2; ++rep)
+                for (int c = 0; c < nk; ++c) {
+                    BulkParams Bc = B;
+                    Bc.max_iters = kTuneMaxIters;
+                    BulkTile tc = bt;
+                    tc.chunk = kChunkCandidates[c];
+                    apply_tile(Bc, tc);
+                    cudaEventRecord(evs[(size_t)(4 * c + 2 * rep)], s);
+                    *launches += launch_integrate_bulk(Bc, soa, t, idx, sub, work, out, ctx->sm_count, s);
+                    cudaEventRecord(evs[(size_t)(4 * c + 2 * rep + 1)], s);
+                }
+            e = cudaStreamSynchronize(s);
+            if (e != cudaSuccess) return cuda_err(ctx, e, "autotune");
+            const BulkTile shape = bt;
+            for (int c = 0; c < nk; ++c) {
+                float m0 = 0.f, m1 = 0.f;
+                cudaEventElapsedTime(&m0, evs[(size_t)(4 * c)], evs[(size_t)(4 * c + 1)]);
+                cudaEventElapsedTime(&m1, evs[(size_t)(4 * c + 2)], evs[(size_t)(4 * c + 3)]);
+                const float m = m0 < m1 ? m0 : m1;
+                if (m < best) {
+                    best = m;
+                    bt = shape;
+                    bt.chunk = kChunkCandidates[c];
+                }
             }
         }
         for (auto& ev_ : evs) ctx->event_pool.push_back(ev_);
@@ -1074,7 +1117,8 @@ int enqueue_kernels_maybe_graph(etraj_ctx* ctx, const etraj_job* job, const Host
     BulkTile t = kTileDefault;
     find_tile(ctx, tile_k, &t);
     const int extra[3] = {job->precision, t.threads * 1000 + t.blocks_per_sm * 10 + t.occ,
-                          t.refill_min * 4 + (ctx->repack ? 1 : 0) + (ctx->static_assign ? 2 : 0)};
+                          (t.refill_min * 4 + (ctx->repack ? 1 : 0) + (ctx->static_assign ? 2 : 0)) * 65536 +
+                              t.chunk};
     std::memcpy(k, extra, sizeof extra);
     k += sizeof extra;
     std::memcpy(k, &n_int, sizeof n_int);
@@ -1213,7 +1257,9 @@ int finish_job(etraj_ctx* ctx, JobRec& r) {
     r.res.num_steps = (int64_t)cnt->n_steps;
     r.res.num_kernel_launches = r.launches;
     r.res.elapsed_ms = ms;
+    const bool sort_failed = cnt->sort_err != 0;
     release_job(ctx, r);
+    if (sort_failed) return set_err(ctx, ETRAJ_ERR_CUDA, "deposit: a look-back wait of the radix sort gave up");
     return ETRAJ_OK;
 }
 
@@ -1351,8 +1397,8 @@ int run_batch(etraj_ctx* ctx, const etraj_job* jobs, int n, etraj_result* res, c
     // the device work of the batch, from the first sampling launch to the weighted sum
     auto enqueue = [&](int* nl) -> int {
         int launches = 0;
-        cudaEventRecord(ctx->ev0, s);
-        cudaEventRecord(ctx->stage_ev[0], s);
+        rec(ctx, ctx->ev0, s);
+        rec(ctx, ctx->stage_ev[0], s);
         for (int i = 0; i < n; ++i) {
             const DJob& J = H[(size_t)i].J;
             DBatch* bat = P.batches + toff[i];
@@ -1364,21 +1410,21 @@ int run_batch(etraj_ctx* ctx, const etraj_job* jobs, int n, etraj_result* res, c
             launches += launch_sampler(ETRAJ_PRECISION_FP32_BULK, J, 0, J.n_t, P.kd + koff[i], P.kz + zoff[i], bat, so,
                                        P.flag + c, ctx->sm_count, s);
         }
-        cudaEventRecord(ctx->stage_ev[1], s);
+        rec(ctx, ctx->stage_ev[1], s);
         launches += launch_compact(P.flag, N, P.idx, P.block_sums, compact_blocks(N) + 1, P.count, s);
-        cudaEventRecord(ctx->stage_ev[2], s);
+        rec(ctx, ctx->stage_ev[2], s);
         for (int i = 0; i < n; ++i) {
             const BulkParams& b = B[(size_t)i];
             launches += launch_field_table(H[(size_t)i].J, b.T0, 1.0 / b.inv_h_d, b.n_int, tab + tab_off[i], s);
         }
         ETRAJ_TRY(tuned_bulk_launch(ctx, M, P.soa, P.t, P.idx, P.count, P.work, P.out, &launches, ctx->stage_ev + 3));
         launches += launch_collect_bulk(H[0].J, P.soa, P.t, P.idx, P.count, P.out, N, ctx->sm_count, s, d_inst, n);
-        cudaEventRecord(ctx->stage_ev[5], s);
+        rec(ctx, ctx->stage_ev[5], s);
         launches += launch_deposit(Jgrid, P.out, P.count, N, P.dep, P.spec_re, P.spec_im, P.mspec, P.sums, P.counters, s);
         launches += launch_instance_reductions(P.out, P.idx, P.count, d_inst, n, d_seg, d_scr, d_isums, d_icnt, s);
         if (weights) launches += launch_weighted_sum(P.mspec, n, grid1, d_w, d_wout, s);
-        cudaEventRecord(ctx->stage_ev[6], s);
-        cudaEventRecord(ctx->ev1, s);
+        rec(ctx, ctx->stage_ev[6], s);
+        rec(ctx, ctx->ev1, s);
         *nl = launches;
         return ETRAJ_OK;
     };
@@ -1401,7 +1447,7 @@ int run_batch(etraj_ctx* ctx, const etraj_job* jobs, int n, etraj_result* res, c
         k += sizeof ptrs;
         BulkTile t = kTileDefault;
         find_tile(ctx, tile_key(M), &t);
-        const int extra[3] = {t.threads * 1000 + t.blocks_per_sm * 10 + t.occ, t.refill_min,
+        const int extra[3] = {t.threads * 1000 + t.blocks_per_sm * 10 + t.occ, t.refill_min * 65536 + t.chunk,
                               (ctx->static_assign ? 1 : 0) + (weights ? 2 : 0)};
         std::memcpy(k, extra, sizeof extra);
         if (ctx->bgexec && key == ctx->bgkey) {
@@ -1444,6 +1490,8 @@ int run_batch(etraj_ctx* ctx, const etraj_job* jobs, int n, etraj_result* res, c
     if (e != cudaSuccess) return cuda_err(ctx, e, "batch launch");
     std::vector<double> isums((size_t)2 * n);
     std::vector<Counters> icnt((size_t)n);
+    unsigned long long sort_err = 0ull;
+    cudaMemcpyAsync(&sort_err, &P.counters->sort_err, sizeof sort_err, cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(isums.data(), d_isums, isums.size() * 8, cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(icnt.data(), d_icnt, icnt.size() * sizeof(Counters), cudaMemcpyDeviceToHost, s);
     const bool coherent = (H[0].J.phase != ETRAJ_PHASE_CTMC);
@@ -1459,6 +1507,7 @@ int run_batch(etraj_ctx* ctx, const etraj_job* jobs, int n, etraj_result* res, c
     if (weights) cudaMemcpyAsync(wspec, d_wout, (size_t)grid1 * 8, cudaMemcpyDeviceToHost, s);
     e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return cuda_err(ctx, e, "etraj_run_batch");
+    if (sort_err) return set_err(ctx, ETRAJ_ERR_CUDA, "deposit: a look-back wait of the radix sort gave up");
     float ms = 0.f;
     cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
     for (int i = 0; i < n; ++i) {
@@ -2099,7 +2148,30 @@ int etraj_set_bulk_tile(etraj_ctx* ctx, int dimension, int phase, int target, in
         return ETRAJ_ERR_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> lk(ctx->mu);
     const int key = (multi ? 1000 : 0) + dimension * 100 + phase * 10 + target;
-    ctx->tiles[key] = BulkTile{threads, blocks_per_sm, refill_min, warps > 16 ? 3 : 2};
+    BulkTile old = kTileDefault;
+    find_tile(ctx, key, &old);
+    ctx->tiles[key] = BulkTile{threads, blocks_per_sm, refill_min, warps > 16 ? 3 : 2, old.chunk};
+    return ETRAJ_OK;
+}
+
+int etraj_bulk_step_chunk(etraj_ctx* ctx, int dimension, int phase, int target, int multi, int* steps) {
+    if (!ctx) return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    const int key = (multi ? 1000 : 0) + dimension * 100 + phase * 10 + target;
+    BulkTile t = kTileDefault;
+    const bool found = find_tile(ctx, key, &t);
+    if (steps) *steps = t.chunk;
+    return found ? ETRAJ_OK : ETRAJ_ERR_NOT_FOUND;
+}
+
+int etraj_set_bulk_step_chunk(etraj_ctx* ctx, int dimension, int phase, int target, int multi, int steps) {
+    if (!ctx || steps < 16 || steps > (1 << 16)) return ETRAJ_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ctx->mu);
+    const int key = (multi ? 1000 : 0) + dimension * 100 + phase * 10 + target;
+    BulkTile t = kTileDefault;
+    find_tile(ctx, key, &t);
+    t.chunk = steps;
+    ctx->tiles[key] = t;
     return ETRAJ_OK;
 }
 

@@ -98,12 +98,25 @@ k_onesweep_scan(const uint32_t* __restrict__ ghist, int npass, uint32_t* __restr
 // belong to blocks of the same cooperative grid that took their tiles earlier,
 // so it never should) and raises *err.
 constexpr int kLookbackSpins = 1 << 22;
+constexpr int kWindow = 16;  // posts a look-back step loads at once
 
 __device__ __forceinline__ unsigned long long load_post(const unsigned long long* p) {
     return *(const volatile unsigned long long*)p;
 }
 
-__global__ void __launch_bounds__(kThreads)
+// The lanes of the warp whose digit equals this lane's: one ballot per digit bit
+// (bits + 1 of them: an absent key carries the digit 2^bits).
+__device__ __forceinline__ unsigned digit_peers(uint32_t d, int bits) {
+    unsigned peers = 0xffffffffu;
+    for (int bit = 0; bit <= bits; ++bit) {
+        const bool on = (d >> bit) & 1u;
+        const unsigned b = __ballot_sync(0xffffffffu, on);
+        peers &= on ? b : ~b;
+    }
+    return peers;
+}
+
+__global__ void __launch_bounds__(kThreads, 3)
 k_onesweep_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ vin, uint32_t* __restrict__ kout,
                 uint32_t* __restrict__ vout, const unsigned long long* __restrict__ count, int pass, int shift,
                 int bits, const uint32_t* __restrict__ base, unsigned long long* __restrict__ post,
@@ -125,12 +138,22 @@ k_onesweep_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ v
         __syncthreads();
         const int64_t tile = (int64_t)s_tile;
         if (tile >= ntiles) break;
-        // digit counts of each warp's part of the tile
+        // the warp's part of the tile in registers, every load in flight at once
+        // (key r of the lane is element sub + 32 r + lane)
         const int64_t sub = tile * kTile + (int64_t)warp * kSub;
+        uint32_t kr[kSub / 32], vr[kSub / 32];
+#pragma unroll
         for (int r = 0; r < kSub / 32; ++r) {
             const int64_t i = sub + r * 32 + lane;
-            const uint32_t d = (i < n) ? (kin[i] >> shift) & mask : nd;
-            const unsigned peers = __match_any_sync(0xffffffffu, d);
+            kr[r] = (i < n) ? kin[i] : 0u;
+            vr[r] = (i < n) ? (vin ? vin[i] : (uint32_t)i) : 0u;
+        }
+        // digit counts of each warp's part of the tile
+#pragma unroll
+        for (int r = 0; r < kSub / 32; ++r) {
+            const int64_t i = sub + r * 32 + lane;
+            const uint32_t d = (i < n) ? (kr[r] >> shift) & mask : nd;
+            const unsigned peers = digit_peers(d, bits);
             if (d < nd && lane == __ffs(peers) - 1) wc[warp][d] += __popc(peers);
         }
         __syncthreads();
@@ -146,25 +169,39 @@ k_onesweep_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ v
             atomicExch(mine, (tile == 0 ? f_inc : f_own) | run);
             uint32_t excl = 0u;
             if (tile > 0) {
+                // walk back kWindow posts per round trip: all loads in flight at once,
+                // then the window's counts in order up to the first running total
                 int64_t t = tile - 1;
                 int spins = 0;
-                while (t >= 0) {
-                    const unsigned long long v = load_post(post + t * kMaxDigits + d);
-                    const unsigned long long f = v & 0xFFFFFFFF00000000ull;
-                    if (f == f_inc) {
-                        excl += (uint32_t)v;
-                        break;
+                bool done = false;
+                while (!done) {
+                    unsigned long long v[kWindow];
+#pragma unroll
+                    for (int j = 0; j < kWindow; ++j)
+                        v[j] = (t - j >= 0) ? load_post(post + (t - j) * kMaxDigits + d) : f_inc;
+                    int used = 0;
+#pragma unroll
+                    for (int j = 0; j < kWindow; ++j) {
+                        if (done || used < j) continue;  // stopped earlier in the window
+                        const unsigned long long f = v[j] & 0xFFFFFFFF00000000ull;
+                        if (f == f_inc) {
+                            excl += (uint32_t)v[j];
+                            done = true;
+                        } else if (f == f_own) {
+                            excl += (uint32_t)v[j];
+                            used = j + 1;
+                        }
                     }
-                    if (f == f_own) {
-                        excl += (uint32_t)v;
-                        --t;
-                        continue;
+                    if (!done) {
+                        t -= used;
+                        if (used < kWindow) {  // a post not there yet: wait a little
+                            if (++spins > kLookbackSpins) {
+                                atomicExch(err, 1ull);
+                                break;
+                            }
+                            __nanosleep(32);
+                        }
                     }
-                    if (++spins > kLookbackSpins) {
-                        atomicExch(err, 1ull);
-                        break;
-                    }
-                    __nanosleep(32);
                 }
                 atomicExch(mine, f_inc | (unsigned long long)(excl + run));
             }
@@ -172,16 +209,13 @@ k_onesweep_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ v
         }
         __syncthreads();
         // stable scatter: each warp writes its keys in index order
+#pragma unroll
         for (int r = 0; r < kSub / 32; ++r) {
             const int64_t i = sub + r * 32 + lane;
             const bool valid = i < n;
-            uint32_t key = 0u, val = 0u, d = nd;
-            if (valid) {
-                key = kin[i];
-                val = vin ? vin[i] : (uint32_t)i;
-                d = (key >> shift) & mask;
-            }
-            const unsigned peers = __match_any_sync(0xffffffffu, d);
+            const uint32_t key = kr[r], val = vr[r];
+            const uint32_t d = valid ? (key >> shift) & mask : nd;
+            const unsigned peers = digit_peers(d, bits);
             const uint32_t pos = valid ? toff[d] + wc[warp][d] + __popc(peers & lt_mask) : 0u;
             __syncwarp();
             if (valid && lane == __ffs(peers) - 1) wc[warp][d] += __popc(peers);

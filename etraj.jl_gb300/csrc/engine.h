@@ -108,6 +108,8 @@ struct DJob {
     int64_t n_t, n_kd, n_kz, n_cand, n_total;  // n_total = n_t * n_cand
     double Ip, Z, kappa, nstar, c, cc_base, e_pre, C, q_theta, q_phi;
     double cutoff, dkdt, mc_kd_max, mc_kz_max;
+    int gauss;         // Monte-Carlo ADK / SPANE: transverse momenta normal of the ADK width
+    double dkdt_base;  // gauss: step_t / mc_kt_num (times the kz span in 2D); dkdt = that / pdf
     double spa_omega;  // SPA initial guess' angular frequency (SPASampler.jl:160-166)
     uint64_t seed;
     double Plm[2 * (2 * kMaxL + 1)];
@@ -161,7 +163,7 @@ int launch_sample_range(const DJob& J, int64_t b0, int64_t nb, const double* kd,
                         DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
                         cudaStream_t s);
 // The FP64 SPA sampler's FP32 pre-pass (atoms): fills batches[b].spa and sets
-// flag = 0 for the candidates whose FP32 rate is more than 1e4 below the cutoff.
+// flag = 0 for the candidates whose FP32 rate is more than 100 times below the cutoff.
 int launch_spa_prefilter(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
                          DBatch* batches, uint8_t* flag, int sm_count, cudaStream_t s);
 // FP32 variant of the same kernel for the bulk path (sampler_fp32.cu); used
@@ -202,6 +204,7 @@ struct BulkParams {
     int n_int;          // field-table intervals
     int table_in_smem;  // 1: stage the table in shared memory
     int threads, blocks_per_sm, refill_min;
+    int chunk0;         // round 0's step budget per electron; round r's is chunk0 16^r (last: none)
     int static_assign;  // 1: one electron per lane, no queue, no rounds (the plain kernel's schedule)
     int occ;            // register budget of the build: 2 (<= 128 per thread) or 3 (<= 85)
     int64_t max_n;      // upper bound of the electron count (grid sizing)
@@ -216,8 +219,9 @@ struct BulkParams {
     float r_far;        // SAE: radius beyond which the exp(-b r) terms are dropped
     int max_iters;      // steps before an electron is given up (status 1)
     // Rounds: the integrator runs as kBulkRounds launches.  In round r, once
-    // the round's queue is empty, an electron that has taken kParkBudget[r]
-    // steps in the round writes its whole state to the park buffer and frees
+    // the round's queue is empty, an electron that has taken the round's step
+    // chunk (chunk0 16^r steps; the last round has none; 1024, 16384, 262144 by
+    // default) in the round writes its whole state to the park buffer and frees
     // its lane; round r+1 resumes the parked electrons packed densely (blocks
     // without parked work exit at once).  park_buf == nullptr: one launch.
     uint32_t* park_buf;   // 2 halves x park_cap entries x kParkWords words (word-major)
@@ -231,7 +235,6 @@ struct BulkParams {
 };
 constexpr int kParkWords = 33;   // words of one parked electron (3D with phase)
 constexpr int kBulkRounds = 4;
-constexpr int kParkBudget[kBulkRounds] = {1024, 16384, 262144, 0};
 constexpr int kBulkCounters = 2 * kBulkRounds;  // work counter and park count per round
 constexpr int kBulkMaxIters = 1000000;  // OrdinaryDiffEq's default maxiters
 int launch_field_table(const DJob& J, double T0, double h, int n_int, float4* tab, cudaStream_t s);

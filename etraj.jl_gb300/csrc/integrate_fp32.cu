@@ -832,7 +832,9 @@ int launch_bulk_t(const BulkParams& P, InitSoA soa, const double* t, const int64
     for (int r = 0; r < rounds; ++r) {
         BulkParams Q = P;
         const size_t half = (size_t)P.park_cap * kParkWords;
-        Q.park_budget = kParkBudget[r];
+        // the step chunk of round r: chunk0 16^r steps (1024, 16384, 262144 for the
+        // default chunk0 = 1024); the last round has none
+        Q.park_budget = (r + 1 < rounds) ? (P.chunk0 > 0 ? P.chunk0 : 1024) << (4 * r) : 0;
         Q.park_in = (r > 0) ? P.park_buf + (size_t)((r - 1) & 1) * half : nullptr;
         Q.park_in_count = (r > 0) ? queue + 2 * (r - 1) + 1 : nullptr;
         Q.park_out = (P.park_buf && r + 1 < rounds) ? P.park_buf + (size_t)(r & 1) * half : nullptr;

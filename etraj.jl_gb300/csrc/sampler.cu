@@ -272,6 +272,33 @@ __device__ dm_cplx pre_numerator(const DJob& J, const DBatch& B, int64_t b, dm_c
     return acc;
 }
 
+// A Gaussian-proposal Monte-Carlo point (etraj_mc_proposal ADK_GAUSS): kd (and, in
+// 3D, kz) normal with the ADK width sigma^2 = F / (2 kappa) at field strength F, by
+// Box-Muller from the candidate's two uniforms, and its weight dkdt = dkdt_base /
+// pdf(kd) [/ pdf(kz)].  The oracle's o_mc_point evaluates the same expressions.
+__device__ __forceinline__ void mc_gauss_point(const DJob& J, double F, double ua, double ub, double* kd0,
+                                               double* kz0, double* dkdt) {
+    const double sig = sqrt(F / (2.0 * J.kappa));
+    const double r = sqrt(-2.0 * dm_log(1.0 - ua));
+    double sn, cs;
+    dm_sincos(6.283185307179586 * ub, &sn, &cs);
+    const double z1 = r * cs, z2 = r * sn;
+    const double norm = sig * 2.5066282746310002;  // sigma sqrt(2 pi)
+    const double inv2s2 = 1.0 / (2.0 * (sig * sig));
+    double w = J.dkdt_base;
+    *kd0 = 0.0;
+    *kz0 = 0.0;
+    if (J.dim != 3 || J.mc_kd_max != 0.0) {
+        *kd0 = sig * z1;
+        w = w * (norm * dm_exp((*kd0 * *kd0) * inv2s2));
+    }
+    if (J.dim == 3 && J.mc_kz_max != 0.0) {
+        *kz0 = sig * z2;
+        w = w * (norm * dm_exp((*kz0 * *kz0) * inv2s2));
+    }
+    *dkdt = w;
+}
+
 __global__ void __launch_bounds__(256)
 k_sample(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double* __restrict__ kdv,
          const double* __restrict__ kzv, const DBatch* __restrict__ batches, InitSoA soa,
@@ -281,7 +308,7 @@ k_sample(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double* _
          q += (int64_t)gridDim.x * blockDim.x) {
         const int64_t bl = q / J.n_cand, i = q - bl * J.n_cand, b = b0 + bl;
         const DBatch& B = batches[b];
-        double kd0, kz0;
+        double kd0, kz0, dkdt = J.dkdt;
         if (!J.mc) {
             kd0 = kdv[i / J.n_kz];
             kz0 = kzv[i % J.n_kz];
@@ -289,13 +316,17 @@ k_sample(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double* _
             uint32_t c[4] = {(uint32_t)i, (uint32_t)((uint64_t)i >> 32), (uint32_t)b, 0x4B445A00u};
             philox4x32(c, J.seed);
             double ua = u53(c[0], c[1]), ub = u53(c[2], c[3]);
-            kd0 = ((ua - 0.5) * 2.0) * J.mc_kd_max;
-            if (J.dim == 3) {
-                kz0 = ((ub - 0.5) * 2.0) * J.mc_kz_max;
-                if (J.mc_kd_max == 0.0) kd0 = 0.0;
-                else if (J.mc_kz_max == 0.0) kz0 = 0.0;
+            if (J.gauss) {
+                mc_gauss_point(J, B.F, ua, ub, &kd0, &kz0, &dkdt);
             } else {
-                kz0 = 0.0;
+                kd0 = ((ua - 0.5) * 2.0) * J.mc_kd_max;
+                if (J.dim == 3) {
+                    kz0 = ((ub - 0.5) * 2.0) * J.mc_kz_max;
+                    if (J.mc_kd_max == 0.0) kd0 = 0.0;
+                    else if (J.mc_kz_max == 0.0) kz0 = 0.0;
+                } else {
+                    kz0 = 0.0;
+                }
             }
         }
         uint8_t keep = 0;
@@ -314,7 +345,9 @@ k_sample(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double* _
                 rate = mol_wfat_rate(J.mol.nxi, J.mol.mmax, tb, tb + nch, J.kappa, F, kd0, kz0, J.dkdt);
                 keep = (!(rate != rate) && !(rate < J.cutoff)) ? 1 : 0;
             }
-        } else if (!(fabs(kd0) < 1e-4)) {
+        } else if (!(fabs(kd0) < 1e-4) && !(fabs(kd0) > J.mc_kd_max && J.gauss) &&
+                   !(J.gauss && J.dim == 3 && fabs(kz0) > J.mc_kz_max)) {
+            // (a Gaussian draw outside +-mc_kd_max, +-mc_kz_max is dropped)
             const double Ip = J.Ip, F = B.F;
             kx0 = kd0 * (-B.sphi);
             ky0 = kd0 * B.cphi;
@@ -343,7 +376,7 @@ k_sample(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double* _
             if (!skip) {
                 double Xe = (kd0 * kd0 + kz0 * kz0) + 2.0 * Ip;
                 double E = dm_exp(-(Xe * sqrt(Xe)) / (3.0 * Fexp));
-                double r1 = sqrt(J.dkdt) * E;
+                double r1 = sqrt(dkdt) * E;
                 dm_cplx amp;
                 if (J.prefix & (ETRAJ_PREFIX_PRE | ETRAJ_PREFIX_PRECC)) {
                     dm_cplx kx, ky, kz = dm_c(kz0, 0.0);
@@ -369,7 +402,7 @@ k_sample(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double* _
                     amp = dm_cscale(amp, sqrt(jac));
                 }
                 rate = amp.re * amp.re + amp.im * amp.im;
-                double crit = spane ? rate / J.dkdt : rate;
+                double crit = spane ? rate / dkdt : rate;
                 keep = (!(rate != rate) && !(crit < J.cutoff)) ? 1 : 0;
                 if (keep && J.phase != ETRAJ_PHASE_CTMC) ph = dm_carg(amp);
             }
@@ -481,11 +514,13 @@ k_compact_scatter(const uint8_t* __restrict__ flag, int64_t n, const uint32_t* _
 __global__ void __launch_bounds__(128)
 k_sample_spa(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double* __restrict__ kdv,
              const double* __restrict__ kzv, const DBatch* __restrict__ batches, InitSoA soa,
-             uint8_t* __restrict__ flag) {
+             uint8_t* __restrict__ flag, int prefiltered) {
     const int64_t total = nb * J.n_cand;
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
          q += (int64_t)gridDim.x * blockDim.x) {
         const int64_t bl = q / J.n_cand, i = q - bl * J.n_cand, b = b0 + bl;
+        // a candidate the FP32 pre-pass found far below the cutoff (flag 0) keeps flag 0
+        if (prefiltered && flag[b * J.n_cand + i] == 0) continue;
         const DBatch& B = batches[b];
         double kd0, kz0;
         if (!J.mc) {
@@ -587,15 +622,19 @@ int launch_batch_prepare(const DJob& J, const double* t, DBatch* batches, cudaSt
 }
 
 int launch_sample_range(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
-                        const DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
+                        DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
                         cudaStream_t s) {
     if (J.method == ETRAJ_SAMPLER_SPA) {
+        // atoms: an FP32 pre-pass marks the candidates far below the cutoff, which
+        // the FP64 kernel then skips (molecules: every candidate in FP64)
+        const int pre = J.mol.on ? 0 : 1;
+        int launches = pre ? launch_spa_prefilter(J, b0, nb, kd, kz, batches, flag, sm_count, s) : 0;
         const int threads = 128;
         const int64_t want = (nb * J.n_cand + threads - 1) / threads;
         const int64_t cap = (int64_t)sm_count * 64;
         const int blocks = (int)(want < cap ? (want > 0 ? want : 1) : cap);
-        k_sample_spa<<<blocks, threads, 0, s>>>(J, b0, nb, kd, kz, batches, soa, flag);
-        return 1;
+        k_sample_spa<<<blocks, threads, 0, s>>>(J, b0, nb, kd, kz, batches, soa, flag, pre);
+        return launches + 1;
     }
     int threads = 256;
     int64_t want = (nb * J.n_cand + threads - 1) / threads;

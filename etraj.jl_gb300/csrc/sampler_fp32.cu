@@ -74,6 +74,12 @@ __device__ __forceinline__ void philox4x32(uint32_t c[4], uint64_t seed) {
     }
 }
 
+// the FP64 sampler's 53-bit uniform in [0, 1) from two draws (sampler.cu), for the
+// pre-pass that must see the FP64 sampler's own momenta
+__device__ __forceinline__ double u53(uint32_t a, uint32_t b) {
+    return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
+}
+
 // k-sum of the solid harmonic (shared_methods.jl:21) at complex (x, y, z).
 __device__ cf sph_sum(int l, int m, cf x, cf y, cf z) {
     const cf xp = cmk(x.re - y.im, x.im + y.re);
@@ -485,14 +491,63 @@ __global__ void k_spa32_bases(const __grid_constant__ DJob J, int64_t b0, int64_
     }
 }
 
+// The rate part of one SPA candidate in FP32 (the steps of SPASampler.jl:320-347):
+// the saddle point t_i, the momenta p, the action's quadrature, the prefactor and
+// the Jacobian, as the log-rate lr = log |amp|^2 and the phase arg.  Returns false
+// when the solve or the action's quadrature fails (the candidate is dropped).
+struct Spa32Rate {
+    float ti, px, py, lr, arg;
+};
+__device__ __forceinline__ bool spa32_rate(const DJob& J, const DBatch& DB, const SpaBase32& S, float kd0, float kz0,
+                                           Spa32Rate& R) {
+    const FBatch& B = DB.f;
+    const float Ip = J.fc.Ip, w = J.fc.spa_omega, e_half = J.fc.e_half;
+    const float wF = w / B.F;
+    const float guess = asinhf(wF * sqrtf(fmaf(kd0, kd0, kz0 * kz0) + 2.0f * Ip)) / w;
+    const float ti = spa32_solve(S, kd0, kz0, Ip, guess);
+    if (ti == 0.0f) return false;
+    cf Ax, Ay, Fx, Fy;
+    spa32_AF(S, ti, Ax, Ay, &Fx, &Fy);
+    float px, py;
+    spa32_pxy(kd0, Ax, Ay, px, py);
+    SpaQ32 Q{&S, px, py, kz0, Ip};
+    bool oks;
+    // S_tun = -int_{t_s}^{t_r} f dt = i int_0^{t_i} f(t_r + i tau) dtau
+    const cf Qs = spa32_quad_from(Q_ACTION, Q, spa32_rule(Q_ACTION, Q, 0.0f, ti, nullptr), oks);
+    if (!oks) return false;
+    // amplitude sqrt(dkdt) exp(i S_tun) [pre] [sqrt(jac)] = sqrt(dkdt) exp(-Q) [...],
+    // kept as its log-rate lr = log |amp|^2 - log dkdt and phase arg
+    float lr = -2.0f * Qs.re, arg = -Qs.im;
+    if (J.prefix & (ETRAJ_PREFIX_PRE | ETRAJ_PREFIX_PRECC)) {
+        const cf kx = cmk(px + Ax.re, Ax.im), ky = cmk(py + Ay.re, Ay.im);
+        const cf num = num32(J, B, kx, ky, kz0);
+        const float cpre = (J.prefix & ETRAJ_PREFIX_PRE) ? J.fc.c : B.c_cc;
+        const cf kF = cadd(cmul(kx, Fx), cmul(ky, Fy));
+        // (k_ts . F(t_s))^((n*+1)/2) as |z|^p cis(p arg z)
+        const float mag = powf(hypotf(kF.re, kF.im), e_half);
+        float sn, cs;
+        sincosf(e_half * atan2f(kF.im, kF.re), &sn, &cs);
+        const cf den = cmk(mag * cs, mag * sn);
+        const float dd = fmaf(den.re, den.re, den.im * den.im);
+        const cf nd = cscale(cmul(num, cconj(den)), cpre / dd);
+        lr += 2.0f * logf(hypotf(nd.re, nd.im));
+        arg += atan2f(nd.im, nd.re);
+    }
+    if (J.prefix & ETRAJ_PREFIX_JAC) lr += logf(spa32_jac(S, DB.spa[1], DB.spa[2], kd0, kz0, Ip, ti));
+    R.ti = ti;
+    R.px = px;
+    R.py = py;
+    R.lr = lr + J.fc.log_dkdt;
+    R.arg = arg;
+    return true;
+}
+
 __global__ void __launch_bounds__(128)
 k_sample_spa32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double* __restrict__ kdv,
                const double* __restrict__ kzv, const DBatch* __restrict__ batches, InitSoA soa,
                uint8_t* __restrict__ flag) {
     const int64_t total = nb * J.n_cand;
     const float Ip = J.fc.Ip, kd_max = J.fc.kd_max, kz_max = J.fc.kz_max;
-    const float w = J.fc.spa_omega, e_half = J.fc.e_half;
-    const float log_dkdt = J.fc.log_dkdt;
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
          q += (int64_t)gridDim.x * blockDim.x) {
         const int64_t bl = q / J.n_cand, i = q - bl * J.n_cand, b = b0 + bl;
@@ -521,65 +576,32 @@ k_sample_spa32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const dou
         // the batch is skipped when F(t_r) <= 1e-3 (SPASampler.jl:167-169)
         if (!(fabsf(kd0) < 1e-4f) && B.spa_on) {
             const SpaBase32 S = DB.spa[0];
-            const float wF = w / B.F;
-            const float guess = asinhf(wF * sqrtf(fmaf(kd0, kd0, kz0 * kz0) + 2.0f * Ip)) / w;
-            const float ti = spa32_solve(S, kd0, kz0, Ip, guess);
-            if (ti != 0.0f) {
-                cf Ax, Ay, Fx, Fy;
-                spa32_AF(S, ti, Ax, Ay, &Fx, &Fy);
-                float px, py;
-                spa32_pxy(kd0, Ax, Ay, px, py);
-                SpaQ32 Q{&S, px, py, kz0, Ip};
-                bool oks;
-                // S_tun = -int_{t_s}^{t_r} f dt = i int_0^{t_i} f(t_r + i tau) dtau
-                const cf Qs = spa32_quad_from(Q_ACTION, Q, spa32_rule(Q_ACTION, Q, 0.0f, ti, nullptr), oks);
-                // The exit position's two quadratures come after the rate, for the
-                // candidates it keeps only: consecutive candidates share t_r, and the
-                // warps of a time sample whose field keeps none skip them.  A failed
-                // quadrature drops the candidate, as it did before the rate.
-                if (oks) {
-                    // amplitude sqrt(dkdt) exp(i S_tun) [pre] [sqrt(jac)] = sqrt(dkdt) exp(-Q) [...],
-                    // kept as its log-rate lr = log |amp|^2 - log dkdt and phase arg
-                    float lr = -2.0f * Qs.re, arg = -Qs.im;
-                    if (J.prefix & (ETRAJ_PREFIX_PRE | ETRAJ_PREFIX_PRECC)) {
-                        const cf kx = cmk(px + Ax.re, Ax.im), ky = cmk(py + Ay.re, Ay.im);
-                        const cf num = num32(J, B, kx, ky, kz0);
-                        const float cpre = (J.prefix & ETRAJ_PREFIX_PRE) ? J.fc.c : B.c_cc;
-                        const cf kF = cadd(cmul(kx, Fx), cmul(ky, Fy));
-                        // (k_ts . F(t_s))^((n*+1)/2) as |z|^p cis(p arg z)
-                        const float mag = powf(hypotf(kF.re, kF.im), e_half);
-                        float sn, cs;
-                        sincosf(e_half * atan2f(kF.im, kF.re), &sn, &cs);
-                        const cf den = cmk(mag * cs, mag * sn);
-                        const float dd = fmaf(den.re, den.re, den.im * den.im);
-                        const cf nd = cscale(cmul(num, cconj(den)), cpre / dd);
-                        lr += 2.0f * logf(hypotf(nd.re, nd.im));
-                        arg += atan2f(nd.im, nd.re);
-                    }
-                    if (J.prefix & ETRAJ_PREFIX_JAC) lr += logf(spa32_jac(S, DB.spa[1], DB.spa[2], kd0, kz0, Ip, ti));
-                    lr += log_dkdt;
-                    // FP32's exp down to its normal range, FP64 below
-                    rate = (lr >= -87.0f) ? (double)expf(lr) : exp((double)lr);
-                    keep = (!(rate != rate) && !(rate < J.cutoff)) ? 1 : 0;
-                    if (keep) {
-                        Seg32 sy;
-                        const Seg32 sx = spa32_rule(Q_IM_AXY, Q, 0.0f, ti, &sy);
-                        bool okx, oky;
-                        x0 = spa32_quad_from(Q_IM_AX, Q, sx, okx).re;
-                        y0 = spa32_quad_from(Q_IM_AY, Q, sy, oky).re;
-                        keep = (okx && oky) ? 1 : 0;
-                        cf A0x, A0y;
-                        spa32_AF(S, 0.0f, A0x, A0y, nullptr, nullptr);
-                        kx0 = (double)(px + A0x.re);
-                        ky0 = (double)(py + A0y.re);
-                    }
-                    if (keep && J.phase != ETRAJ_PHASE_CTMC) {
-                        // arg reduced to [-pi, pi]: k 2 pi subtracted with 2 pi split in two
-                        // floats (Cody and Waite's reduction)
-                        const float k = rintf(arg * 0.159154943f);
-                        const float r = fmaf(-k, -1.7484556e-7f, fmaf(-k, 6.28318548f, arg));
-                        ph = (double)r;
-                    }
+            Spa32Rate R;
+            if (spa32_rate(J, DB, S, kd0, kz0, R)) {
+                // FP32's exp down to its normal range, FP64 below
+                rate = (R.lr >= -87.0f) ? (double)expf(R.lr) : exp((double)R.lr);
+                keep = (!(rate != rate) && !(rate < J.cutoff)) ? 1 : 0;
+                if (keep) {
+                    // the exit position's two quadratures, for the candidates the rate
+                    // keeps only (a failed quadrature drops the candidate)
+                    SpaQ32 Q{&S, R.px, R.py, kz0, Ip};
+                    Seg32 sy;
+                    const Seg32 sx = spa32_rule(Q_IM_AXY, Q, 0.0f, R.ti, &sy);
+                    bool okx, oky;
+                    x0 = spa32_quad_from(Q_IM_AX, Q, sx, okx).re;
+                    y0 = spa32_quad_from(Q_IM_AY, Q, sy, oky).re;
+                    keep = (okx && oky) ? 1 : 0;
+                    cf A0x, A0y;
+                    spa32_AF(S, 0.0f, A0x, A0y, nullptr, nullptr);
+                    kx0 = (double)(R.px + A0x.re);
+                    ky0 = (double)(R.py + A0y.re);
+                }
+                if (keep && J.phase != ETRAJ_PHASE_CTMC) {
+                    // arg reduced to [-pi, pi]: k 2 pi subtracted with 2 pi split in two
+                    // floats (Cody and Waite's reduction)
+                    const float k = rintf(R.arg * 0.159154943f);
+                    const float r = fmaf(-k, -1.7484556e-7f, fmaf(-k, 6.28318548f, R.arg));
+                    ph = (double)r;
                 }
             }
         }
@@ -803,7 +825,61 @@ k_sample32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double*
     }
 }
 
+// The FP64 SPA sampler's pre-pass (atoms): each candidate's rate in FP32 at the FP64
+// sampler's own (kd, kz) draws, and flag[g] = 0 where that rate is more than 100
+// times below the cutoff -- a candidate the FP64 rate cannot keep (FP32's rate is
+// within 3e-3 of FP64's where both solve, and the FP32 sampler keeps the FP64
+// sampler's electrons but for a few in 1e6, at the cutoff) -- else 1.  k_sample_spa then skips the
+// candidates marked 0 and computes every other one in FP64 as before, so its
+// survivors and their values do not change.
+__global__ void __launch_bounds__(128)
+k_spa_prefilter(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double* __restrict__ kdv,
+                const double* __restrict__ kzv, const DBatch* __restrict__ batches, uint8_t* __restrict__ flag) {
+    const int64_t total = nb * J.n_cand;
+    const float lr_drop = logf(J.fc.cutoff) - 4.6051702f;  // log(cutoff / 100)
+    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t bl = q / J.n_cand, i = q - bl * J.n_cand, b = b0 + bl;
+        const DBatch& DB = batches[b];
+        double kd0, kz0;
+        if (!J.mc) {
+            kd0 = kdv[i / J.n_kz];
+            kz0 = kzv[i % J.n_kz];
+        } else {
+            uint32_t c[4] = {(uint32_t)i, (uint32_t)((uint64_t)i >> 32), (uint32_t)b, 0x4B445A00u};
+            philox4x32(c, J.seed);
+            const double ua = u53(c[0], c[1]), ub = u53(c[2], c[3]);
+            kd0 = ((ua - 0.5) * 2.0) * J.mc_kd_max;
+            if (J.dim == 3) {
+                kz0 = ((ub - 0.5) * 2.0) * J.mc_kz_max;
+                if (J.mc_kd_max == 0.0) kd0 = 0.0;
+                else if (J.mc_kz_max == 0.0) kz0 = 0.0;
+            } else {
+                kz0 = 0.0;
+            }
+        }
+        uint8_t maybe = 1;
+        if (!(fabs(kd0) < 1e-4) && DB.f.spa_on) {
+            Spa32Rate R;
+            if (spa32_rate(J, DB, DB.spa[0], (float)kd0, (float)kz0, R) && R.lr < lr_drop) maybe = 0;
+        }
+        flag[b * J.n_cand + i] = maybe;
+    }
+}
+
 }  // namespace
+
+int launch_spa_prefilter(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
+                         DBatch* batches, uint8_t* flag, int sm_count, cudaStream_t s) {
+    const int64_t bb = (3 * nb + 127) / 128;
+    k_spa32_bases<<<(int)(bb > 0 ? bb : 1), 128, 0, s>>>(J, b0, nb, batches);
+    const int threads = 128;
+    const int64_t want = (nb * J.n_cand + threads - 1) / threads;
+    const int64_t cap = (int64_t)sm_count * 64;
+    const int blocks = (int)(want < cap ? (want > 0 ? want : 1) : cap);
+    k_spa_prefilter<<<blocks, threads, 0, s>>>(J, b0, nb, kd, kz, batches, flag);
+    return 2;
+}
 
 int launch_sample32_range(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
                           DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,

@@ -59,9 +59,11 @@ def make_job(*, init_cond_method, laser, target, dimension, sample_t_intv, sampl
              traj_t_final, final_p_max, final_p_num, ss_kd_max=0.0, ss_kd_num=0, ss_kz_max=0.0,
              ss_kz_num=0, mc_kt_num=0, mc_kd_max=0.0, mc_kz_max=0.0, traj_phase_method="CTMC",
              traj_rtol=1e-6, sample_monte_carlo=False, sample_cutoff_limit=1e-16,
-             rate_prefix="Full", mol_orbit_ridx=0, precision="fp64", seed=0):
+             rate_prefix="Full", mol_orbit_ridx=0, precision="fp64", seed=0, mc_kt_proposal="uniform"):
     """Checks the keywords as TrajectorySimulationJob (TrajectorySimulation.jl:164-298) and
-    the sampler constructors do, and packs them into an etraj_job."""
+    the sampler constructors do, and packs them into an etraj_job.  mc_kt_proposal
+    ("uniform", the reference's, or "adk_gauss": normal transverse momenta of the
+    ADK width with importance weights) applies to Monte-Carlo ADK and SPANE."""
     method = _sym(init_cond_method)
     if method not in _METHODS:
         raise ValueError("[ElectronSamplers] Undefined initial condition method [%s]." % method)
@@ -105,6 +107,10 @@ def make_job(*, init_cond_method, laser, target, dimension, sample_t_intv, sampl
     j.mc_kt_num, j.mc_kd_max, j.mc_kz_max = int(mc_kt_num), float(mc_kd_max), float(mc_kz_max)
     j.sample_cutoff_limit = float(sample_cutoff_limit)
     j.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+    proposals = {"uniform": abi.PROPOSAL_UNIFORM, "adk_gauss": abi.PROPOSAL_ADK_GAUSS}
+    if _sym(mc_kt_proposal) not in proposals:
+        raise ValueError("`mc_kt_proposal` must be \"uniform\" or \"adk_gauss\".")
+    j.mc_kt_proposal = proposals[_sym(mc_kt_proposal)]
     j.laser = laser.to_c()
     if isinstance(target, MoleculeBase):
         j.target, keep = target.to_c(orbit_ridx=mol_orbit_ridx, wfat=(method == "WFAT"))
@@ -250,6 +256,19 @@ class Engine:
         self._check(self.lib.etraj_set_bulk_tile(self.ctx, dimension, phase, target, 1 if multi else 0,
                                                  threads, blocks_per_sm, refill_min))
 
+    def bulk_step_chunk(self, dimension, phase, target, multi=False):
+        """(steps, tuned): the step budget of the bulk integrator's first round."""
+        v = C.c_int32()
+        st = self.lib.etraj_bulk_step_chunk(self.ctx, dimension, phase, target, 1 if multi else 0, C.byref(v))
+        if st not in (abi.OK, abi.ERR_NOT_FOUND):
+            self._check(st)
+        return v.value, st == abi.OK
+
+    def set_bulk_step_chunk(self, dimension, phase, target, steps, multi=False):
+        """Pin the step budget of the bulk integrator's first round on this engine."""
+        self._check(self.lib.etraj_set_bulk_step_chunk(self.ctx, dimension, phase, target, 1 if multi else 0,
+                                                       steps))
+
     def run_batch(self, jobs, want_spectrum=True, want_amplitude=False, weights=None):
         """Run up to 64 FP32-bulk jobs (same dimension, phase, rtol, target and grid)
         as one batch; returns [(result, spectrum, amplitude)] and, with `weights`,
@@ -387,7 +406,7 @@ def perform_traj_simulation(*, init_cond_method, laser, target, dimension, sampl
                             traj_phase_method="CTMC", traj_rtol=1e-6, output_fmt="jld2",
                             output_compress=True, output_path=None, sample_monte_carlo=False,
                             sample_cutoff_limit=1e-16, rate_prefix="Full", mol_orbit_ridx=0,
-                            show_progress=False, precision="fp64", seed=0, engine=None):
+                            show_progress=False, precision="fp64", seed=0, engine=None, mc_kt_proposal="uniform"):
     """Performs a semiclassical trajectory simulation (TrajectorySimulation.jl:103-161) on the GPU.
 
     Returns a dict with the keys of the reference's output file, and writes
@@ -404,7 +423,8 @@ def perform_traj_simulation(*, init_cond_method, laser, target, dimension, sampl
                    ss_kz_num=ss_kz_num, mc_kt_num=mc_kt_num, mc_kd_max=mc_kd_max,
                    mc_kz_max=mc_kz_max, traj_phase_method=traj_phase_method, traj_rtol=traj_rtol,
                    sample_monte_carlo=sample_monte_carlo, sample_cutoff_limit=sample_cutoff_limit,
-                   rate_prefix=rate_prefix, mol_orbit_ridx=mol_orbit_ridx, precision=precision, seed=seed)
+                   rate_prefix=rate_prefix, mol_orbit_ridx=mol_orbit_ridx, precision=precision, seed=seed,
+                   mc_kt_proposal=mc_kt_proposal)
     fmt = _sym(output_fmt)
     if fmt == "hdf5":
         fmt = "h5"

@@ -163,7 +163,20 @@ typedef struct etraj_job {
     uint64_t seed;               /* Monte-Carlo stream; the reference draws from an unseeded global RNG */
     etraj_laser laser;
     etraj_target target;
+    int32_t mc_kt_proposal;      /* Monte-Carlo ADK / SPANE: ETRAJ_PROPOSAL_* (0, the reference's, by default) */
+    int32_t reserved2;
 } etraj_job;
+
+/* How Monte-Carlo ADK and SPANE candidates draw their transverse momenta.
+ * UNIFORM is the reference's gen_rand_pt (shared_methods.jl:3-12): kd (and kz)
+ * uniform in [-mc_kd_max, mc_kd_max] (and +-mc_kz_max), each candidate weighted
+ * by dkdt = step_t * spans / mc_kt_num.  ADK_GAUSS is not in the reference: kd
+ * (and, in 3D, kz) normal with the ADK width sigma^2 = F(t_r) / (2 kappa) of the
+ * candidate's time sample (Box-Muller from the same two draws), a draw outside
+ * +-mc_kd_max (+-mc_kz_max) dropped, and each candidate weighted by
+ * step_t / (mc_kt_num pdf(kd) [pdf(kz)]) -- an importance-sampling estimate of
+ * the same integral, with the candidates where the rate is. */
+typedef enum { ETRAJ_PROPOSAL_UNIFORM = 0, ETRAJ_PROPOSAL_ADK_GAUSS = 1 } etraj_mc_proposal;
 
 typedef struct etraj_result {
     /* caller-owned outputs; either pointer may be NULL to skip that copy */
@@ -314,6 +327,12 @@ int etraj_bulk_tile(etraj_ctx* ctx, int dimension, int phase, int target, int mu
                     int* blocks_per_sm, int* refill_min);
 int etraj_set_bulk_tile(etraj_ctx* ctx, int dimension, int phase, int target, int multi, int threads,
                         int blocks_per_sm, int refill_min);
+/* The step chunk of a variant: the step budget per electron of the bulk
+ * integrator's first round (round r: chunk 16^r; see etraj_set_straggler_repack).
+ * The autotuner picks it after the shape, from 256, 1024 (the default) and 4096
+ * steps, on the same sample; etraj_set_bulk_step_chunk pins it (16 .. 65536). */
+int etraj_bulk_step_chunk(etraj_ctx* ctx, int dimension, int phase, int target, int multi, int* steps);
+int etraj_set_bulk_step_chunk(etraj_ctx* ctx, int dimension, int phase, int target, int multi, int steps);
 
 /* ---- rounds of the bulk integrator ------------------------------------------------------
  * No counterpart in the reference.  A few electrons of a job can need up to
@@ -321,8 +340,9 @@ int etraj_set_bulk_tile(etraj_ctx* ctx, int dimension, int phase, int target, in
  * keeps its whole thread block -- and that block's share of an SM -- resident
  * for seconds, so concurrent jobs (the serving loop) cannot get onto the GPU.
  * With repacking on (the default) the bulk integrator of a job runs in
- * rounds: once the queue is empty, an electron that has taken 1024 steps in
- * round 0 (then 16384, 262144 in the next rounds) writes its integrator state
+ * rounds: once the queue is empty, an electron that has taken the step chunk
+ * in round 0 (1024 steps by default, tuned; then 16x, 256x that in the next
+ * rounds) writes its integrator state
  * to a device buffer and frees its lane, and the next round resumes the parked
  * electrons in as few blocks as they fill.  Batches (etraj_run_batch) run as
  * one launch.  Each electron's arithmetic does not depend on where it runs, so

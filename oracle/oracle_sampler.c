@@ -213,6 +213,8 @@ int o_sampler_init(const etraj_job* job, o_sampler* S) {
         double kd_span = (job->mc_kd_max > 0.0) ? 2.0 * job->mc_kd_max : 1.0;
         double kz_span = (job->mc_kz_max > 0.0) ? 2.0 * job->mc_kz_max : 1.0;
         S->dkdt = ((t_step * kd_span) * kz_span) / (double)job->mc_kt_num;
+        S->gauss = (job->mc_kt_proposal == ETRAJ_PROPOSAL_ADK_GAUSS) ? 1 : 0;
+        S->dkdt_base = (S->dim == 3 ? t_step : t_step * kz_span) / (double)job->mc_kt_num;
         S->n_cand = job->mc_kt_num;
     }
     return 0;
@@ -328,8 +330,10 @@ dm_cplx o_pre_numerator(const o_sampler* S, const o_batch* B, dm_cplx kx, dm_cpl
 
 /* One ADK / SPANE candidate (ADKSampler.jl:318-347, SPANESampler.jl:320-352).
  * Returns 1 and fills row[] when the electron survives the cutoff. */
-int o_candidate(const o_sampler* S, const o_batch* B, double kd0, double kz0, double* row) {
+int o_candidate(const o_sampler* S, const o_batch* B, double kd0, double kz0, double dkdt, double* row) {
     if (fabs(kd0) < 1e-4) return 0;
+    /* a Gaussian draw outside +-mc_kd_max (+-mc_kz_max) is dropped */
+    if (S->gauss && (fabs(kd0) > S->mc_kd_max || (S->dim == 3 && fabs(kz0) > S->mc_kz_max))) return 0;
     double Ip = S->Ip, F = B->F;
     double kx0 = kd0 * (-B->sphi);
     double ky0 = kd0 * B->cphi;
@@ -357,7 +361,7 @@ int o_candidate(const o_sampler* S, const o_batch* B, double kd0, double kz0, do
     /* ADKAmpExp(F, Ip, kd, kz) = exp(-(kd^2+kz^2+2Ip)^1.5/3F) */
     double Xe = (kd0 * kd0 + kz0 * kz0) + 2.0 * Ip;
     double E = dm_exp(-(Xe * sqrt(Xe)) / (3.0 * Fexp));
-    double r1 = sqrt(S->dkdt) * E;
+    double r1 = sqrt(dkdt) * E;
     dm_cplx amp;
     if (S->prefix & (ETRAJ_PREFIX_PRE | ETRAJ_PREFIX_PRECC)) {
         dm_cplx kx, ky, kz = dm_c(kz0, 0.0);
@@ -383,7 +387,7 @@ int o_candidate(const o_sampler* S, const o_batch* B, double kd0, double kz0, do
         amp = dm_cscale(amp, sqrt(jac));
     }
     double rate = amp.re * amp.re + amp.im * amp.im;
-    double crit = spane ? rate / S->dkdt : rate;
+    double crit = spane ? rate / dkdt : rate;
     if (dm_isnan(rate) || crit < S->cutoff) return 0;
     int k = 0;
     row[k++] = x0;
@@ -490,10 +494,37 @@ int o_candidate_wfat(const o_sampler* S, const o_batch* B, double kd0, double kz
 
 /* (kd0, kz0) of Monte-Carlo candidate i of batch b (shared_methods.jl:4-12,
  * ADKSampler.jl:350-363). */
-void o_mc_point(const o_sampler* S, int64_t b, int64_t i, double* kd0, double* kz0) {
+/* A Monte-Carlo point and its weight dkdt: gen_rand_pt (shared_methods.jl:3-12,
+ * weight S->dkdt), or with the Gaussian proposal (etraj_mc_proposal ADK_GAUSS, not
+ * in the reference) kd (and kz in 3D) normal of variance F / (2 kappa), by
+ * Box-Muller from the same two uniforms, weighted by dkdt_base / pdf. */
+void o_mc_point(const o_sampler* S, int64_t b, int64_t i, double F, double* kd0, double* kz0, double* dkdt) {
     uint32_t c[4] = {(uint32_t)i, (uint32_t)((uint64_t)i >> 32), (uint32_t)b, 0x4B445A00u};
     o_philox4x32(c, S->seed);
     double u1 = o_u53(c[0], c[1]), u2 = o_u53(c[2], c[3]);
+    *dkdt = S->dkdt;
+    if (S->gauss) {
+        const double sig = sqrt(F / (2.0 * S->kappa));
+        const double r = sqrt(-2.0 * dm_log(1.0 - u1));
+        double sn, cs;
+        dm_sincos(6.283185307179586 * u2, &sn, &cs);
+        const double z1 = r * cs, z2 = r * sn;
+        const double norm = sig * 2.5066282746310002; /* sigma sqrt(2 pi) */
+        const double inv2s2 = 1.0 / (2.0 * (sig * sig));
+        double w = S->dkdt_base;
+        *kd0 = 0.0;
+        *kz0 = 0.0;
+        if (S->dim != 3 || S->mc_kd_max != 0.0) {
+            *kd0 = sig * z1;
+            w = w * (norm * dm_exp((*kd0 * *kd0) * inv2s2));
+        }
+        if (S->dim == 3 && S->mc_kz_max != 0.0) {
+            *kz0 = sig * z2;
+            w = w * (norm * dm_exp((*kz0 * *kz0) * inv2s2));
+        }
+        *dkdt = w;
+        return;
+    }
     if (S->dim == 3) {
         *kd0 = ((u1 - 0.5) * 2.0) * S->mc_kd_max;
         *kz0 = ((u2 - 0.5) * 2.0) * S->mc_kz_max;
@@ -518,16 +549,16 @@ int64_t o_sample_batch(const o_sampler* S, int64_t b, double* init, int64_t capa
     const int spa = (S->method == ETRAJ_SAMPLER_SPA);
     if (spa && B.F <= 1e-3) return 0; /* SPASampler.jl:167-169 */
     for (int64_t i = 0; i < S->n_cand; ++i) {
-        double kd0, kz0;
+        double kd0, kz0, dkdt = S->dkdt;
         if (!S->mc) {
             kd0 = S->kd[i / S->n_kz];
             kz0 = S->kz[i % S->n_kz];
         } else {
-            o_mc_point(S, b, i, &kd0, &kz0);
+            o_mc_point(S, b, i, B.F, &kd0, &kz0, &dkdt);
         }
         const int kept = spa ? (g_spa_independent ? o_candidate_spa_ref(S, &B, kd0, kz0, row)
                                                   : o_candidate_spa(S, &B, kd0, kz0, row))
-                             : S->wfat ? o_candidate_wfat(S, &B, kd0, kz0, row) : o_candidate(S, &B, kd0, kz0, row);
+                             : S->wfat ? o_candidate_wfat(S, &B, kd0, kz0, row) : o_candidate(S, &B, kd0, kz0, dkdt, row);
         if (kept) {
             if (count < capacity) memcpy(init + count * S->rows, row, sizeof(double) * (size_t)S->rows);
             ++count;

@@ -16,6 +16,8 @@ typedef struct {
     int64_t n_t, n_kd, n_kz, n_cand;
     double *t, *kd, *kz;
     double mc_kd_max, mc_kz_max, dkdt;
+    int gauss;          /* Monte-Carlo: the Gaussian proposal (etraj_mc_proposal ADK_GAUSS) */
+    double dkdt_base;   /* gauss: step_t / mc_kt_num (times the kz span in 2D) */
     double spa_omega; /* the SPA initial guess' angular frequency (SPASampler.jl:160-166) */
     /* molecular targets (mol.h layouts) */
     int mol, wfat;
@@ -42,14 +44,14 @@ double o_linrange(double a, double b, int64_t n, int64_t i);
 int o_sampler_init(const etraj_job* job, o_sampler* S);
 void o_sampler_free(o_sampler* S);
 void o_batch_prepare(const o_sampler* S, int64_t b, o_batch* B);
-int o_candidate(const o_sampler* S, const o_batch* B, double kd0, double kz0, double* row);
+int o_candidate(const o_sampler* S, const o_batch* B, double kd0, double kz0, double dkdt, double* row);
 int o_candidate_spa(const o_sampler* S, const o_batch* B, double kd0, double kz0, double* row);
 int o_candidate_spa_ref(const o_sampler* S, const o_batch* B, double kd0, double kz0, double* row);
 dm_cplx o_pre_numerator(const o_sampler* S, const o_batch* B, dm_cplx kx, dm_cplx ky, dm_cplx kz);
 dm_cplx o_mol_numerator_ref(const o_sampler* S, const o_batch* B, dm_cplx nkx, dm_cplx nky, dm_cplx nkz);
 double o_wfat_rate_ref(const o_sampler* S, const o_batch* B, double kd, double kz);
 int o_candidate_wfat(const o_sampler* S, const o_batch* B, double kd0, double kz0, double* row);
-void o_mc_point(const o_sampler* S, int64_t b, int64_t i, double* kd0, double* kz0);
+void o_mc_point(const o_sampler* S, int64_t b, int64_t i, double F, double* kd0, double* kz0, double* dkdt);
 int64_t o_sample_batch(const o_sampler* S, int64_t b, double* init, int64_t capacity);
 
 #endif

@@ -227,6 +227,12 @@ int oracle_validate(const etraj_job* job, char* msg, int len) {
         return o_fail(msg, len, "[TrajectorySimulationJob] `sample_t_intv` must be a valid interval.");
     if (!(job->traj_t_final > job->sample_t_intv[1]))
         return o_fail(msg, len, "[TrajectorySimulationJob] `traj_t_final` must be greater than the last time point of `sample_t_intv`.");
+    if (job->mc_kt_proposal != ETRAJ_PROPOSAL_UNIFORM && job->mc_kt_proposal != ETRAJ_PROPOSAL_ADK_GAUSS)
+        return o_fail(msg, len, "unknown mc_kt_proposal.");
+    if (job->mc_kt_proposal == ETRAJ_PROPOSAL_ADK_GAUSS &&
+        (!job->sample_monte_carlo ||
+         (job->init_cond_method != ETRAJ_SAMPLER_ADK && job->init_cond_method != ETRAJ_SAMPLER_SPANE)))
+        return o_fail(msg, len, "mc_kt_proposal ADK_GAUSS applies to Monte-Carlo ADK and SPANE sampling only.");
     if (job->dimension != 2 && job->dimension != 3)
         return o_fail(msg, len, "[TrajectorySimulationJob] `dimension` must be either 2 or 3.");
     if (job->init_cond_method != ETRAJ_SAMPLER_ADK && job->init_cond_method != ETRAJ_SAMPLER_SPANE &&

@@ -204,6 +204,30 @@ def test_rounds_with_parking_keep_every_bit():
     off.close()
 
 
+def test_step_chunk_keeps_every_bit():
+    """The rounds' step chunk (the tuner's third dimension) moves where electrons
+    run, not what they compute: a pinned chunk of 64 steps parks hundreds of
+    electrons and gives the default's bits."""
+    T = 2 * np.pi * 1600.0 / 45.563352525
+    L = et.Cos2Laser(peak_int=1e14, wave_len=1600.0, cyc_num=4, ellip=0.3)
+    job = et.make_job(init_cond_method="ADK", laser=L, target=et.get_atom("Ar"), dimension=2,
+                      sample_t_intv=(-T, T), sample_t_num=200, traj_t_final=3 * T,
+                      final_p_max=(2.0, 2.0), final_p_num=(100, 100), sample_monte_carlo=True, mc_kt_num=400,
+                      mc_kd_max=1.0, traj_phase_method="SCTS", seed=3, precision="fp32_bulk")
+    a = et.Engine(device=0)
+    b = et.Engine(device=0)
+    b.set_bulk_step_chunk(2, abi.PHASE_SCTS, abi.TARGET_SAE, 64)
+    assert b.bulk_step_chunk(2, abi.PHASE_SCTS, abi.TARGET_SAE)[0] == 64
+    r1, s1, a1 = a.run(job, want_amplitude=True)
+    r2, s2, a2 = b.run(job, want_amplitude=True)
+    assert r1.num_effective_traj == r2.num_effective_traj > 0 and r1.num_steps == r2.num_steps
+    assert np.array_equal(s1, s2) and np.array_equal(a1, a2)
+    with pytest.raises(et.EtrajError):
+        b.set_bulk_step_chunk(2, abi.PHASE_SCTS, abi.TARGET_SAE, 8)
+    a.close()
+    b.close()
+
+
 def test_static_assignment_keeps_every_bit():
     """One electron per lane with no work stealing and no rounds (the plain
     kernel's schedule) gives the same bits as the work-stealing schedule, on the

@@ -69,6 +69,8 @@ CASES = [
     dict(method="ADK", dim=2, phase="SCTS", target="H", laser="gauss", nt=200, nkd=101),
     dict(method="SPANE", dim=3, phase="CTMC", target="H", laser="bichrom", mc=True, nt=100, nkd=30, nkz=30),
     dict(method="ADK", dim=2, phase="QTMC", target="Xe", laser="cos4", ellip=1.0, nt=200, nkd=101),
+    dict(proposal="adk_gauss", method="SPANE", dim=2, phase="SCTS", target="Ar", laser="cos2", ellip=1.0,
+         mc=True, nt=300, nkd=200, nkz=1, intensity=1.2e14),
 ]
 
 

@@ -35,7 +35,7 @@ def period(wave_len=800.0):
 
 def job_of(method="ADK", dim=2, phase="CTMC", target="H", laser="cos4", mc=False, nt=24,
            nkd=15, nkz=7, pnum=None, pmax=1.5, prefix="Full", cutoff=1e-16, seed=3, ellip=0.0,
-           intensity=1e14, t_final_periods=3.0, rtol=1e-6):
+           intensity=1e14, t_final_periods=3.0, rtol=1e-6, proposal="uniform"):
     T = period()
     if laser == "cos4":
         L = et.Cos4Laser(peak_int=intensity, wave_len=800.0, cyc_num=2, ellip=ellip)
@@ -53,7 +53,7 @@ def job_of(method="ADK", dim=2, phase="CTMC", target="H", laser="cos4", mc=False
     kw = dict(init_cond_method=method, laser=L, target=tgt, dimension=dim, sample_t_intv=(-T, T),
               sample_t_num=nt, traj_t_final=t_final_periods * T, final_p_max=(pmax,) * dim,
               final_p_num=pnum, traj_phase_method=phase, rate_prefix=prefix,
-              sample_cutoff_limit=cutoff, seed=seed, traj_rtol=rtol)
+              sample_cutoff_limit=cutoff, seed=seed, traj_rtol=rtol, mc_kt_proposal=proposal)
     if mc:
         kw.update(sample_monte_carlo=True, mc_kt_num=nkd * nkz, mc_kd_max=1.0,
                   mc_kz_max=1.0 if dim == 3 else 0.0)
@@ -108,6 +108,11 @@ SAMPLE_CASES = [
     dict(method="SPA", dim=3, mc=True, laser="bichrom", phase="QTMC", nt=12, nkd=8, nkz=8),
     dict(method="SPA", dim=3, target="Xe", laser="gauss", prefix=["Pre", "Jac"], ellip=0.5, nt=12, nkd=9, nkz=5),
     dict(method="SPA", dim=2, prefix="Exp", ellip=1.0, nt=16, nkd=31),
+    # the Gaussian transverse-momentum proposal (importance weights in dkdt)
+    dict(method="ADK", dim=2, mc=True, proposal="adk_gauss", ellip=0.3),
+    dict(method="ADK", dim=3, mc=True, target="Ar", laser="gauss", phase="SCTS", proposal="adk_gauss"),
+    dict(method="SPANE", dim=3, mc=True, laser="bichrom", prefix="Pre", proposal="adk_gauss"),
+    dict(method="SPANE", dim=2, mc=True, target="He", prefix="Exp", proposal="adk_gauss"),
 ]
 
 
@@ -160,6 +165,7 @@ RUN_CASES = [
     dict(method="ADK", dim=2, pnum=(1, 50)),
     dict(method="ADK", dim=2, pmax=0.3),  # many electrons land outside the grid
     dict(method="SPA", dim=2, phase="QTMC", ellip=1.0, nt=16, nkd=31),
+    dict(method="ADK", dim=2, phase="SCTS", mc=True, ellip=0.3, proposal="adk_gauss"),
 ]
 
 
