@@ -57,10 +57,17 @@ k_onesweep_hist(const uint32_t* __restrict__ keys, const unsigned long long* __r
     for (int i = threadIdx.x; i < kMaxPasses * kMaxDigits; i += kThreads) (&h[0][0])[i] = 0u;
     __syncthreads();
     int w[kMaxPasses], sh[kMaxPasses];
-    for (int p = 0; p < npass; ++p) pass_digits(bits, npass, p, &w[p], &sh[p]);
+#pragma unroll
+    for (int p = 0; p < kMaxPasses; ++p) {
+        w[p] = 0;
+        sh[p] = 0;
+        if (p < npass) pass_digits(bits, npass, p, &w[p], &sh[p]);
+    }
     for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < n; i += (int64_t)gridDim.x * kThreads) {
         const uint32_t k = keys[i];
-        for (int p = 0; p < npass; ++p) atomicAdd(&h[p][(k >> sh[p]) & ((1u << w[p]) - 1u)], 1u);
+#pragma unroll
+        for (int p = 0; p < kMaxPasses; ++p)
+            if (p < npass) atomicAdd(&h[p][(k >> sh[p]) & ((1u << w[p]) - 1u)], 1u);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < npass * kMaxDigits; i += kThreads) {
@@ -238,7 +245,8 @@ k_onesweep_pass(const uint32_t* __restrict__ kin, const uint32_t* __restrict__ v
 // segment, and every FP64 add is issued for the whole warp on GB300's narrow
 // FP64 pipe.)  The bounds (first, end) of bin k are two uint32 stored in the
 // 8-byte slot spec_re[k], zeroed beforehand, so an empty bin reads (0, 0) and
-// sums to +0.0, and k_bin_sum reads the slot before it writes the sum there.
+// sums to +0.0, and k_bin_sum reads the slot before it writes the sum there,
+// and the bin of the momentum spectrum (re, or re^2 + im^2 when coherent).
 __global__ void __launch_bounds__(256)
 k_segment_bounds(const uint32_t* __restrict__ keys, const unsigned long long* __restrict__ count,
                  uint32_t grid, uint32_t* __restrict__ bounds) {
@@ -255,7 +263,7 @@ k_segment_bounds(const uint32_t* __restrict__ keys, const unsigned long long* __
 __global__ void __launch_bounds__(256)
 k_bin_sum(const uint32_t* __restrict__ vals, int64_t grid, const double* __restrict__ c_re,
           const double* __restrict__ c_im, int coherent, double* __restrict__ spec_re,
-          double* __restrict__ spec_im) {
+          double* __restrict__ spec_im, double* __restrict__ mspec) {
     for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < grid;
          g += (int64_t)gridDim.x * blockDim.x) {
         const uint2 b = reinterpret_cast<const uint2*>(spec_re)[g];
@@ -268,18 +276,19 @@ k_bin_sum(const uint32_t* __restrict__ vals, int64_t grid, const double* __restr
         }
         spec_re[g] = sr;
         if (coherent) spec_im[g] = si;
+        mspec[g] = coherent ? sr * sr + si * si : sr;
     }
 }
 
 int launch_bin_sums(const uint32_t* keys, const uint32_t* vals, const unsigned long long* count, int64_t max_n,
                     int64_t grid, const double* c_re, const double* c_im, int coherent, double* spec_re,
-                    double* spec_im, cudaStream_t s) {
+                    double* spec_im, double* mspec, cudaStream_t s) {
     int64_t pb = (max_n + 255) / 256;
     if (pb > 152 * 32) pb = 152 * 32;
     int64_t gb = (grid + 255) / 256;
     if (gb > 152 * 32) gb = 152 * 32;
     k_segment_bounds<<<(int)(pb > 0 ? pb : 1), 256, 0, s>>>(keys, count, (uint32_t)grid, (uint32_t*)spec_re);
-    k_bin_sum<<<(int)(gb > 0 ? gb : 1), 256, 0, s>>>(vals, grid, c_re, c_im, coherent, spec_re, spec_im);
+    k_bin_sum<<<(int)(gb > 0 ? gb : 1), 256, 0, s>>>(vals, grid, c_re, c_im, coherent, spec_re, spec_im, mspec);
     return 2;
 }
 
@@ -290,50 +299,55 @@ __global__ void k_finalize_spec(const double* __restrict__ re, const double* __r
         out[g] = coherent ? re[g] * re[g] + im[g] * im[g] : re[g];
 }
 
-// One level of the 256-ary canonical tree over two arrays.  Level 0 reads
-// n = *count elements, level k reads ceil(n / 256^k).  Each node holds 256
-// slots (absent ones +0.0) summed as a binary tree over consecutive pairs:
-// lane j of the node's warp sums slots 8j..8j+7 in three pairwise levels, and
-// five shuffle levels combine lanes (2i, 2i+1), (4i, 4i+2), ...  No chain of
-// dependent FP64 additions is longer than 8, which matters on GB300, whose
-// FP64 unit has a long latency.
-constexpr int kTreeWarps = 8;
-__global__ void __launch_bounds__(32 * kTreeWarps)
-k_tree_level(const double* __restrict__ a_in, const double* __restrict__ b_in,
-             double* __restrict__ a_out, double* __restrict__ b_out,
-             const unsigned long long* __restrict__ count, int level) {
-    int64_t m = (int64_t)*count;
-    for (int k = 0; k < level; ++k) m = (m + 255) / 256;
+// The 256-ary canonical tree over two arrays (ion_prob, ion_prob_uncollected).
+// Level 0 reads n = *count elements, level k reads ceil(n / 256^k).  Each node
+// holds 256 slots (absent ones +0.0) summed as a binary tree over consecutive
+// pairs: lane j of the node's warp sums slots 8j..8j+7 in three pairwise
+// levels, and five shuffle levels combine lanes (2i, 2i+1), (4i, 4i+2), ...
+// No chain of dependent FP64 additions is longer than 8, which matters on
+// GB300, whose FP64 unit has a long latency.
+
+// The node over 256 slots whose lane j holds slots 8j..8j+7 in va/vb: its sums
+// reach lane 0.
+__device__ __forceinline__ void tree_node(double (&va)[8], double (&vb)[8], int lane, double* sa_out,
+                                          double* sb_out) {
+#pragma unroll
+    for (int w = 4; w >= 1; w >>= 1) {
+#pragma unroll
+        for (int j = 0; j < w; ++j) {
+            va[j] = va[2 * j] + va[2 * j + 1];
+            vb[j] = vb[2 * j] + vb[2 * j + 1];
+        }
+    }
+    double sa = va[0], sb = vb[0];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const double ra = __shfl_down_sync(0xffffffffu, sa, o);
+        const double rb = __shfl_down_sync(0xffffffffu, sb, o);
+        if ((lane & (2 * o - 1)) == 0) {
+            sa = sa + ra;
+            sb = sb + rb;
+        }
+    }
+    *sa_out = sa;
+    *sb_out = sb;
+}
+
+// Nodes node0, node0 + stride, ... of a level over m inputs, one per warp.
+__device__ __forceinline__ void tree_nodes(const double* a_in, const double* b_in, double* a_out, double* b_out,
+                                           int64_t m, int64_t node0, int64_t stride, int lane) {
     const int64_t nb = (m + 255) / 256;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int64_t node = (int64_t)blockIdx.x * kTreeWarps + warp; node < nb;
-         node += (int64_t)gridDim.x * kTreeWarps) {
+    for (int64_t node = node0; node < nb; node += stride) {
         const int64_t base = node * 256 + 8 * lane;
         double va[8], vb[8];
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
             const bool in = base + j < m;
-            va[j] = in ? a_in[base + j] : 0.0;
-            vb[j] = in ? b_in[base + j] : 0.0;
+            va[j] = in ? __ldcg(a_in + base + j) : 0.0;
+            vb[j] = in ? __ldcg(b_in + base + j) : 0.0;
         }
-#pragma unroll
-        for (int w = 4; w >= 1; w >>= 1) {
-#pragma unroll
-            for (int j = 0; j < w; ++j) {
-                va[j] = va[2 * j] + va[2 * j + 1];
-                vb[j] = vb[2 * j] + vb[2 * j + 1];
-            }
-        }
-        double sa = va[0], sb = vb[0];
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const double ra = __shfl_down_sync(0xffffffffu, sa, o);
-            const double rb = __shfl_down_sync(0xffffffffu, sb, o);
-            if ((lane & (2 * o - 1)) == 0) {
-                sa = sa + ra;
-                sb = sb + rb;
-            }
-        }
+        double sa, sb;
+        tree_node(va, vb, lane, &sa, &sb);
         if (lane == 0) {
             a_out[node] = sa;
             b_out[node] = sb;
@@ -341,24 +355,91 @@ k_tree_level(const double* __restrict__ a_in, const double* __restrict__ b_in,
     }
 }
 
-__global__ void k_tree_result(const double* __restrict__ a, const double* __restrict__ b,
-                              const unsigned long long* __restrict__ count, double* __restrict__ sums) {
-    const bool empty = (*count == 0ull);
-    sums[0] = empty ? 0.0 : a[0];
-    sums[1] = empty ? 0.0 : b[0];
-}
+constexpr int kTreeWarps = 8;
 
-__global__ void __launch_bounds__(256)
-k_counters(const int32_t* __restrict__ status, const int32_t* __restrict__ steps,
-           const unsigned long long* __restrict__ count, Counters* __restrict__ c) {
+// One read of the per-trajectory outputs, in trajectory order, for all the
+// deposit needs from them besides the sort: the digit counts of every sort pass
+// (as k_onesweep_hist), level 0 of the canonical trees (as k_tree_level) and the
+// counters.  A warp takes a node of 256 trajectories, lane j its slots 8j..8j+7,
+// loaded as 16-byte vectors when the node is whole and the arrays are aligned.
+// The block that finishes last adds the tree's upper levels and writes the sums
+// (sums[0] ion_prob, sums[1] ion_prob_uncollected; 0 for no trajectory).
+__global__ void __launch_bounds__(32 * kTreeWarps)
+k_deposit_prepass(const uint32_t* __restrict__ keys, const int32_t* __restrict__ status,
+                  const int32_t* __restrict__ steps, const double* __restrict__ w_ion,
+                  const double* __restrict__ w_unc, const unsigned long long* __restrict__ count, int bits,
+                  int npass, uint32_t* __restrict__ ghist, double* __restrict__ a_out, double* __restrict__ b_out,
+                  double* __restrict__ sums, unsigned int* __restrict__ done, Counters* __restrict__ c) {
+    __shared__ uint32_t h[kMaxPasses][kMaxDigits];
+    __shared__ unsigned long long part[3][kTreeWarps];
     const int64_t n = (int64_t)*count;
+    int w[kMaxPasses], sh[kMaxPasses];
+#pragma unroll
+    for (int p = 0; p < kMaxPasses; ++p) {
+        w[p] = 0;
+        sh[p] = 0;
+        if (p < npass) pass_digits(bits, npass, p, &w[p], &sh[p]);
+    }
+    for (int i = threadIdx.x; i < kMaxPasses * kMaxDigits; i += blockDim.x) (&h[0][0])[i] = 0u;
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool vec = ((((uintptr_t)keys | (uintptr_t)status | (uintptr_t)steps | (uintptr_t)w_ion |
+                        (uintptr_t)w_unc) & 15u) == 0u);
     unsigned long long f = 0, io = 0, st = 0;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t s = status[i];
-        f += ((s & 0xff) != 0) ? 1ull : 0ull;
-        io += (s & 0x100) ? 1ull : 0ull;
-        st += (unsigned long long)steps[i];
+    const int64_t nb = (n + 255) / 256;
+    for (int64_t node = (int64_t)blockIdx.x * kTreeWarps + warp; node < nb;
+         node += (int64_t)gridDim.x * kTreeWarps) {
+        const int64_t base = node * 256 + 8 * lane;
+        double va[8], vb[8];
+        uint32_t k[8];
+        int32_t sv[8], tv[8];
+        int valid = 8;
+        if (vec && node * 256 + 256 <= n) {
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const uint4 kk = reinterpret_cast<const uint4*>(keys + base)[q];
+                const int4 ss = reinterpret_cast<const int4*>(status + base)[q];
+                const int4 tt = reinterpret_cast<const int4*>(steps + base)[q];
+                k[4 * q] = kk.x; k[4 * q + 1] = kk.y; k[4 * q + 2] = kk.z; k[4 * q + 3] = kk.w;
+                sv[4 * q] = ss.x; sv[4 * q + 1] = ss.y; sv[4 * q + 2] = ss.z; sv[4 * q + 3] = ss.w;
+                tv[4 * q] = tt.x; tv[4 * q + 1] = tt.y; tv[4 * q + 2] = tt.z; tv[4 * q + 3] = tt.w;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const double2 x = reinterpret_cast<const double2*>(w_ion + base)[q];
+                const double2 y = reinterpret_cast<const double2*>(w_unc + base)[q];
+                va[2 * q] = x.x; va[2 * q + 1] = x.y;
+                vb[2 * q] = y.x; vb[2 * q + 1] = y.y;
+            }
+        } else {
+            valid = (int)((n - base) < 0 ? 0 : ((n - base) > 8 ? 8 : (n - base)));
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const bool in = j < valid;
+                k[j] = in ? keys[base + j] : 0u;
+                sv[j] = in ? status[base + j] : 0;
+                tv[j] = in ? steps[base + j] : 0;
+                va[j] = in ? w_ion[base + j] : 0.0;
+                vb[j] = in ? w_unc[base + j] : 0.0;
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            if (j < valid) {
+#pragma unroll
+                for (int p = 0; p < kMaxPasses; ++p)
+                    if (p < npass) atomicAdd(&h[p][(k[j] >> sh[p]) & ((1u << w[p]) - 1u)], 1u);
+                f += ((sv[j] & 0xff) != 0) ? 1ull : 0ull;
+                io += (sv[j] & 0x100) ? 1ull : 0ull;
+                st += (unsigned long long)tv[j];
+            }
+        }
+        double sa, sb;
+        tree_node(va, vb, lane, &sa, &sb);
+        if (lane == 0) {
+            a_out[node] = sa;
+            b_out[node] = sb;
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -366,20 +447,54 @@ k_counters(const int32_t* __restrict__ status, const int32_t* __restrict__ steps
         io += __shfl_down_sync(0xffffffffu, io, o);
         st += __shfl_down_sync(0xffffffffu, st, o);
     }
-    // one atomic per block and counter
-    __shared__ unsigned long long part[3][8];
-    const int w = threadIdx.x >> 5;
-    if ((threadIdx.x & 31) == 0) {
-        part[0][w] = f;
-        part[1][w] = io;
-        part[2][w] = st;
+    if (lane == 0) {
+        part[0][warp] = f;
+        part[1][warp] = io;
+        part[2][warp] = st;
     }
     __syncthreads();
     if (threadIdx.x < 3) {
         unsigned long long v = 0;
-        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) v += part[threadIdx.x][k];
+        for (int q = 0; q < kTreeWarps; ++q) v += part[threadIdx.x][q];
         unsigned long long* dst = (threadIdx.x == 0) ? &c->n_failed : (threadIdx.x == 1) ? &c->n_ionized : &c->n_steps;
         if (v) atomicAdd(dst, v);
+    }
+#pragma unroll
+    for (int p = 0; p < kMaxPasses; ++p)
+        if (p < npass)
+            for (int d = threadIdx.x; d < (1 << w[p]); d += blockDim.x) {
+                const uint32_t v = h[p][d];
+                if (v) atomicAdd(&ghist[p * kMaxDigits + d], v);
+            }
+    if (blockIdx.x == 0 && threadIdx.x == 0) c->n_eff = (unsigned long long)n;
+    // the last block to finish sums the levels above 0 (the pattern of a fence and a
+    // counter of finished blocks: no block waits for another)
+    __shared__ bool s_last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) s_last = (atomicAdd(done, 1u) == gridDim.x - 1u);
+    __syncthreads();
+    if (!s_last) return;
+    __threadfence();
+    int64_t m = nb;
+    const double* ta = a_out;
+    const double* tb = b_out;
+    double* oa = a_out + nb;
+    double* ob = b_out + nb;
+    while (m > 1) {
+        const int64_t nb1 = (m + 255) / 256;
+        tree_nodes(ta, tb, oa, ob, m, warp, kTreeWarps, lane);
+        __syncthreads();
+        ta = oa;
+        tb = ob;
+        oa += nb1;
+        ob += nb1;
+        m = nb1;
+    }
+    if (threadIdx.x == 0) {
+        sums[0] = (m == 1) ? __ldcg(ta) : 0.0;
+        sums[1] = (m == 1) ? __ldcg(tb) : 0.0;
+        *done = 0u;  // ready for the next launch
     }
 }
 
@@ -390,6 +505,8 @@ __global__ void k_copy_count(const unsigned long long* __restrict__ count, Count
 int64_t tiles_for(int64_t n) { return (n + kTile - 1) / kTile; }
 // digit counts and offsets of every pass, one tile counter per pass (+ padding)
 constexpr int kOnesweepAuxWords = 2 * kMaxPasses * kMaxDigits + 64;
+// the pre-pass's counter of finished blocks, in the padding after the tile counters
+constexpr int kPrepassDoneWord = 2 * kMaxPasses * kMaxDigits + 32;
 
 int64_t tree_size(int64_t n) {
     int64_t s = 0, m = n;
@@ -406,10 +523,10 @@ int key_bits(int64_t grid) {
     return b;
 }
 
-// Blocks of k_onesweep_pass that fit on the device at once (its grid: the
-// look-back waits only for tiles taken earlier, by blocks of the same
-// co-resident, cooperative grid).
-int onesweep_blocks() {
+// Blocks of a kernel that fit on the device at once, per device and kernel
+// (Tag tells the kernels' caches apart).
+template <int Tag>
+int resident_blocks(const void* fn, int threads) {
     static int cached[64] = {};
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
@@ -418,7 +535,7 @@ int onesweep_blocks() {
     }
     if (!cached[dev]) {
         int per_sm = 0, sms = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_onesweep_pass, kThreads, 0) != cudaSuccess ||
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0) != cudaSuccess ||
             cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || per_sm < 1 ||
             sms < 1) {
             cudaGetLastError();
@@ -429,27 +546,42 @@ int onesweep_blocks() {
     return cached[dev];
 }
 
+// The grid of k_onesweep_pass: the look-back waits only for tiles taken
+// earlier, by blocks of the same co-resident, cooperative grid.
+int onesweep_blocks() { return resident_blocks<0>((const void*)k_onesweep_pass, kThreads); }
+
 // Stable LSD radix sort of (key, index) pairs on the low `bits` key bits, in as
 // few passes of at most kMaxDigitBits as cover them (20 bits: 7 + 7 + 6; 25:
 // 9 + 8 + 8).  The order is the same for any split: by key, then by index.
 // The sorted pairs are left in the buffers *kout, *vout point to.  `post` holds
 // kMaxDigits words per tile, `aux` the digit counts, offsets and tile counters
-// (kOnesweepAuxWords), `err` is raised by a look-back that gives up.
-int radix_sort(const uint32_t* keys, const unsigned long long* count, int64_t max_n, int bits,
+// (kOnesweepAuxWords), `err` is raised by a look-back that gives up.  With
+// hist_ready the caller has cleared both (radix_clear) and counted the digits
+// into aux itself (k_deposit_prepass).
+int sort_passes(int bits) { return (bits + kMaxDigitBits - 1) / kMaxDigitBits; }
+
+void radix_clear(int64_t max_n, unsigned long long* post, uint32_t* aux, cudaStream_t s) {
+    cudaMemsetAsync(aux, 0, sizeof(uint32_t) * kOnesweepAuxWords, s);
+    cudaMemsetAsync(post, 0, sizeof(unsigned long long) * (size_t)tiles_for(max_n) * kMaxDigits, s);
+}
+
+int radix_sort(const uint32_t* keys, const unsigned long long* count, int64_t max_n, int bits, bool hist_ready,
                uint32_t* const kbuf[2], uint32_t* const vbuf[2], unsigned long long* post, uint32_t* aux,
                unsigned long long* err, const uint32_t** kout, const uint32_t** vout, cudaStream_t s) {
     const int64_t nb = tiles_for(max_n);
-    const int npass = (bits + kMaxDigitBits - 1) / kMaxDigitBits;
+    const int npass = sort_passes(bits);
     uint32_t* ghist = aux;
     uint32_t* base = aux + kMaxPasses * kMaxDigits;
     unsigned int* tile_ctr = aux + 2 * kMaxPasses * kMaxDigits;
-    cudaMemsetAsync(aux, 0, sizeof(uint32_t) * kOnesweepAuxWords, s);
-    cudaMemsetAsync(post, 0, sizeof(unsigned long long) * (size_t)nb * kMaxDigits, s);
-    int hblocks = onesweep_blocks();
-    if ((int64_t)hblocks > nb) hblocks = (int)nb;
-    k_onesweep_hist<<<hblocks, kThreads, 0, s>>>(keys, count, bits, npass, ghist);
+    int launches = 1;
+    if (!hist_ready) {
+        radix_clear(max_n, post, aux, s);
+        int hblocks = onesweep_blocks();
+        if ((int64_t)hblocks > nb) hblocks = (int)nb;
+        k_onesweep_hist<<<hblocks, kThreads, 0, s>>>(keys, count, bits, npass, ghist);
+        ++launches;
+    }
     k_onesweep_scan<<<1, kMaxDigits, 0, s>>>(ghist, npass, base);
-    int launches = 2;
     const uint32_t* kin = keys;
     const uint32_t* vin = nullptr;
     int which = 0;
@@ -512,47 +644,33 @@ int launch_deposit(const DJob& J, const TrajOut& out, const unsigned long long* 
     if (coherent) cudaMemsetAsync(spec_im, 0, (size_t)grid * sizeof(double), s);
     cudaMemsetAsync(counters, 0, sizeof(Counters), s);
     if (max_n > 0) {
+        // one read of the per-trajectory outputs: digit counts, the trees, counters
+        const int bits = key_bits(grid);
+        radix_clear(max_n, d.post, d.aux, s);
+        const int64_t nodes = (max_n + 255) / 256;
+        int pblocks = resident_blocks<1>((const void*)k_deposit_prepass, 32 * kTreeWarps);
+        if ((int64_t)pblocks * kTreeWarps > nodes) pblocks = (int)((nodes + kTreeWarps - 1) / kTreeWarps);
+        unsigned int* done = d.aux + kPrepassDoneWord;
+        k_deposit_prepass<<<pblocks, 32 * kTreeWarps, 0, s>>>(out.key, out.status, out.steps, out.w_ion, out.w_unc,
+                                                              count, bits, sort_passes(bits), d.aux, d.tree_a,
+                                                              d.tree_b, sums, done, counters);
+        ++launches;
         // stable LSD radix sort of (key, survivor index); keys are in [0, grid]
         uint32_t* kbuf[2] = {d.keys_a, d.keys_b};
         uint32_t* vbuf[2] = {d.vals_a, d.vals_b};
         const uint32_t *kin = nullptr, *vin = nullptr;
-        launches += radix_sort(out.key, count, max_n, key_bits(grid), kbuf, vbuf, d.post, d.aux,
+        launches += radix_sort(out.key, count, max_n, bits, true, kbuf, vbuf, d.post, d.aux,
                                &counters->sort_err, &kin, &vin, s);
         launches += launch_bin_sums(kin, vin, count, max_n, grid, out.c_re, out.c_im, coherent, spec_re,
-                                    spec_im, s);
-        // canonical 256-ary trees for ion_prob and ion_prob_uncollected
-        const double* a = out.w_ion;
-        const double* b = out.w_unc;
-        double* ta = d.tree_a;
-        double* tb = d.tree_b;
-        int64_t m = max_n;
-        int level = 0;
-        do {
-            int64_t nbl = (m + 255) / 256;
-            int64_t want = (nbl + kTreeWarps - 1) / kTreeWarps;
-            int tb_blocks = (int)(want < 152 * 16 ? want : 152 * 16);
-            k_tree_level<<<tb_blocks, 32 * kTreeWarps, 0, s>>>(a, b, ta, tb, count, level);
-            ++launches;
-            a = ta;
-            b = tb;
-            ta += nbl;
-            tb += nbl;
-            m = nbl;
-            ++level;
-        } while (m > 1);
-        k_tree_result<<<1, 1, 0, s>>>(a, b, count, sums);
-        int cblocks = (int)((max_n + 255) / 256);
-        if (cblocks > 152 * 2) cblocks = 152 * 2;
-        k_counters<<<cblocks, 256, 0, s>>>(out.status, out.steps, count, counters);
-        launches += 2;
+                                    spec_im, momentum_spec, s);
     } else {
         cudaMemsetAsync(sums, 0, 2 * sizeof(double), s);
+        k_copy_count<<<1, 1, 0, s>>>(count, counters);
+        int fblocks = (int)((grid + 255) / 256);
+        if (fblocks > 152 * 16) fblocks = 152 * 16;
+        k_finalize_spec<<<fblocks, 256, 0, s>>>(spec_re, spec_im, grid, coherent, momentum_spec);
+        launches += 2;
     }
-    k_copy_count<<<1, 1, 0, s>>>(count, counters);
-    int fblocks = (int)((grid + 255) / 256);
-    if (fblocks > 152 * 16) fblocks = 152 * 16;
-    k_finalize_spec<<<fblocks, 256, 0, s>>>(spec_re, spec_im, grid, coherent, momentum_spec);
-    launches += 2;
     return launches;
 }
 
@@ -853,11 +971,12 @@ extern "C" int etraj_deposit_noalloc(int64_t n, const uint32_t* key, const doubl
         int cblocks = (int)((n + 255) / 256);
         if (cblocks > sms * 8) cblocks = sms * 8;
         k_clamp_keys<<<cblocks, 256, 0, s>>>(key, n, (uint32_t)grid, kclamp);
-        radix_sort(kclamp, count, n, key_bits(grid), kbuf, vbuf, post, aux, err, &kin, &vin, s);
-        launch_bin_sums(kin, vin, count, n, grid, c_re, c_im, coherent, spec_re, spec_im, s);
+        radix_sort(kclamp, count, n, key_bits(grid), false, kbuf, vbuf, post, aux, err, &kin, &vin, s);
+        launch_bin_sums(kin, vin, count, n, grid, c_re, c_im, coherent, spec_re, spec_im, momentum_spec, s);
+    } else {
+        int fblocks = (int)((grid + 255) / 256);
+        if (fblocks > sms * 16) fblocks = sms * 16;
+        k_finalize_spec<<<fblocks, 256, 0, s>>>(spec_re, spec_im, grid, coherent, momentum_spec);
     }
-    int fblocks = (int)((grid + 255) / 256);
-    if (fblocks > sms * 16) fblocks = sms * 16;
-    k_finalize_spec<<<fblocks, 256, 0, s>>>(spec_re, spec_im, grid, coherent, momentum_spec);
     return (cudaGetLastError() == cudaSuccess) ? ETRAJ_OK : ETRAJ_ERR_CUDA;
 }
