@@ -159,19 +159,9 @@ struct Counters {
 int launch_batch_prepare(const DJob& J, const double* t, DBatch* batches, cudaStream_t s);
 // Samples the candidates of time samples [b0, b0+nb) (flag and SoA indexed by
 // b * n_cand + i).
-// Scratch of the FP64 sampler's pre-pass (the list of candidates it may keep): the
-// survivors' compaction buffers, free until that compaction runs.
-struct SampleScratch {
-    int64_t* list;
-    uint32_t* block_sums;
-    int64_t block_cap;
-    unsigned long long* count;
-};
 int launch_sample_range(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
                         DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
-                        cudaStream_t s, const SampleScratch* scr);
-int launch_rate_prefilter(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
-                          const DBatch* batches, uint8_t* flag, int sm_count, cudaStream_t s);
+                        cudaStream_t s);
 // The FP64 SPA sampler's FP32 pre-pass (atoms): fills batches[b].spa and sets
 // flag = 0 for the candidates whose FP32 rate is more than 100 times below the cutoff.
 int launch_spa_prefilter(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,

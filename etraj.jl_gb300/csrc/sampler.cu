@@ -302,13 +302,11 @@ __device__ __forceinline__ void mc_gauss_point(const DJob& J, double F, double u
 __global__ void __launch_bounds__(256)
 k_sample(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double* __restrict__ kdv,
          const double* __restrict__ kzv, const DBatch* __restrict__ batches, InitSoA soa,
-         uint8_t* __restrict__ flag, const int64_t* __restrict__ list, const unsigned long long* __restrict__ lcount) {
-    // every candidate of the range, or (list) the *lcount candidates it names
-    const int64_t total = list ? (int64_t)*lcount : nb * J.n_cand;
+         uint8_t* __restrict__ flag) {
+    const int64_t total = nb * J.n_cand;
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
          q += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t c = list ? list[q] : q;
-        const int64_t bl = c / J.n_cand, i = c - bl * J.n_cand, b = b0 + bl;
+        const int64_t bl = q / J.n_cand, i = q - bl * J.n_cand, b = b0 + bl;
         const DBatch& B = batches[b];
         double kd0, kz0, dkdt = J.dkdt;
         if (!J.mc) {
@@ -624,8 +622,8 @@ int launch_batch_prepare(const DJob& J, const double* t, DBatch* batches, cudaSt
 }
 
 int launch_sample_range(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
-                        DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count, cudaStream_t s,
-                        const SampleScratch* scr) {
+                        DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
+                        cudaStream_t s) {
     if (J.method == ETRAJ_SAMPLER_SPA) {
         // atoms: an FP32 pre-pass marks the candidates far below the cutoff, which
         // the FP64 kernel then skips (molecules: every candidate in FP64)
@@ -642,21 +640,8 @@ int launch_sample_range(const DJob& J, int64_t b0, int64_t nb, const double* kd,
     int64_t want = (nb * J.n_cand + threads - 1) / threads;
     int64_t cap = (int64_t)sm_count * 32;
     int blocks = (int)(want < cap ? (want > 0 ? want : 1) : cap);
-    // atoms, ADK/SPANE, uniform draws: an FP32 pre-pass marks the candidates far below
-    // the cutoff, a compaction lists the others, and the FP64 kernel runs over the
-    // list, so its warps hold candidates that may be kept instead of idle lanes
-    const bool pre = scr && !J.mol.on && !J.gauss && J.cutoff >= kSample32MinCutoff &&
-                     (J.method == ETRAJ_SAMPLER_ADK || J.method == ETRAJ_SAMPLER_SPANE) &&
-                     compact_blocks(nb * J.n_cand) + 1 <= scr->block_cap;
-    if (!pre) {
-        k_sample<<<blocks, threads, 0, s>>>(J, b0, nb, kd, kz, batches, soa, flag, nullptr, nullptr);
-        return 1;
-    }
-    uint8_t* fr = flag + b0 * J.n_cand;
-    int launches = launch_rate_prefilter(J, b0, nb, kd, kz, batches, flag, sm_count, s);
-    launches += launch_compact(fr, nb * J.n_cand, scr->list, scr->block_sums, scr->block_cap, scr->count, s);
-    k_sample<<<blocks, threads, 0, s>>>(J, b0, nb, kd, kz, batches, soa, flag, scr->list, scr->count);
-    return launches + 1;
+    k_sample<<<blocks, threads, 0, s>>>(J, b0, nb, kd, kz, batches, soa, flag);
+    return 1;
 }
 
 int64_t compact_blocks(int64_t n) { return (n + kCompactChunk - 1) / kCompactChunk; }

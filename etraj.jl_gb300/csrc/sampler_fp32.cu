@@ -691,121 +691,15 @@ __device__ __forceinline__ float u24_unit(uint32_t x) {
 // One candidate per thread.  A thread's (time sample, candidate) pair advances
 // by the grid's stride without dividing, so the 64-bit divisions that split a
 // flat candidate index run once per thread instead of once per candidate.
-// One ADK, SPANE or WFAT candidate in FP32 at the momentum draw (kd0, kz0) of time
-// sample b (ADKSampler.jl:233-335, SPANESampler.jl, WFATSampler.jl:173-240): exit
-// point, initial momentum, rate and, when kept and asked for, the phase.  Returns
-// the reference's cutoff rule; C.crit is what the cutoff compares (the rate, or
-// rate / dkdt for SPANE), NaN where no rate is evaluated (kd0 ~ 0, SPANE's
-// weak-field skip).
-struct Cand32 {
-    float x0, y0, kx0, ky0, rate, ph, crit;
-};
-__device__ __forceinline__ uint8_t cand32(const DJob& J, const FBatch& B, int64_t b, float kd0, float kz0,
-                                          bool want_phase, Cand32& C) {
-    const float Ip = J.fc.Ip, kap2 = J.fc.kap2, sqdkdt = J.fc.sqdkdt;
-    const float inv_dkdt = J.fc.inv_dkdt, cutoff = J.fc.cutoff, e_pre = J.fc.e_pre;
-    const float c_pre = J.fc.c;
-    const float spane_lim = J.mc ? 0.04f : 0.111111111f;  // 1/25, 1/9
-    const bool spane = (J.method == ETRAJ_SAMPLER_SPANE);
-    uint8_t keep = 0;
-    float x0 = 0.0f, y0 = 0.0f, kx0 = 0.0f, ky0 = 0.0f, rate = 0.0f, ph = 0.0f;
-    float crit = __int_as_float(0x7fc00000);
-    if (J.method == ETRAJ_SAMPLER_WFAT) {
-        // WFATSampler.jl:173-240: ADK's exit point, the WFAT rate, CTMC rows
-        if (!(fmaf(kd0, kd0, kz0 * kz0) < 1e-8f)) {
-            const float F = B.F;
-            kx0 = kd0 * (-B.sphi);
-            ky0 = kd0 * B.cphi;
-            const float r0 = fmaf(0.5f, fmaf(kd0, kd0, kz0 * kz0), Ip) / F;
-            x0 = r0 * B.cphi;
-            y0 = r0 * B.sphi;
-            rate = wfat_rate32(J, J.mol.tabf + b * (int64_t)J.mol.stride, F, kd0, kz0);
-            keep = (!(rate != rate) && !(rate < cutoff)) ? 1 : 0;
-        }
-    } else if (!(fabsf(kd0) < 1e-4f)) {
-        const float F = B.F;
-        kx0 = kd0 * (-B.sphi);
-        ky0 = kd0 * B.cphi;
-        const float k2 = fmaf(kd0, kd0, kz0 * kz0);
-        const float Xk = k2 + 2.0f * Ip;
-        float ti, X2, Fexp;
-        bool skip = false;
-        if (!spane) {
-            const float r0 = fmaf(0.5f, k2, Ip) / F;
-            x0 = r0 * B.cphi;
-            y0 = r0 * B.sphi;
-            ti = sqrtf(kap2 + k2) / F;
-            X2 = Xk * (F * F);
-            Fexp = F;
-        } else {
-            const float F2eff = fmaf(F, F, -fmaf(kx0, B.dFx, ky0 * B.dFy));
-            const float r0 = ((0.5f * F) * Xk) / F2eff;
-            x0 = r0 * B.cphi;
-            y0 = r0 * B.sphi;
-            skip = (F2eff <= (F * F) * spane_lim);
-            ti = sqrtf((kap2 + k2) / F2eff);
-            X2 = Xk * F2eff;
-            Fexp = sqrtf(F2eff);
-        }
-        if (!skip) {
-            const float E = expf(-(Xk * sqrtf(Xk)) / (3.0f * Fexp));
-            const float r1 = sqdkdt * E;
-            cf amp;
-            if (J.prefix & (ETRAJ_PREFIX_PRE | ETRAJ_PREFIX_PRECC)) {
-                cf kx, ky;
-                if (!spane) {
-                    kx = cmk(kx0, -(ti * B.Fx));
-                    ky = cmk(ky0, -(ti * B.Fy));
-                } else {
-                    const float h = 0.5f * ti * ti;
-                    kx = cmk(fmaf(h, B.dFx, kx0), -(ti * B.Fx));
-                    ky = cmk(fmaf(h, B.dFy, ky0), -(ti * B.Fy));
-                }
-                // rotate conj(k_ts) into the field frame (ADKSampler.jl:247-249)
-                const cf nkx = cmk(kz0, 0.0f);
-                const cf nky = cadd(cscale(cconj(kx), B.ny0), cscale(cconj(ky), B.ny1));
-                const cf nkz = cadd(cscale(cconj(kx), B.nz0), cscale(cconj(ky), B.nz1));
-                cf num = cmk(0.0f, 0.0f);
-                if (J.mol.on) {
-                    num = mol_num32(J, J.mol.tabf + b * (int64_t)J.mol.stride, nkx, nky, nkz);
-                } else {
-                    for (int mp = -J.l; mp <= J.l; ++mp) {
-                        const int ii = mp + J.l;
-                        const cf Y = cmul(cmk(J.fPlm[2 * ii], J.fPlm[2 * ii + 1]), sph_sum(J.l, mp, nkx, nky, nkz));
-                        num = cadd(num, cmul(cmk(B.CD[2 * ii], B.CD[2 * ii + 1]), Y));
-                    }
-                }
-                const float cpre = (J.prefix & ETRAJ_PREFIX_PRE) ? c_pre : B.c_cc;
-                const float den = (e_pre == 0.5f) ? sqrtf(X2) : exp2f(e_pre * log2f(X2));
-                amp = cscale(num, (cpre / den) * r1);
-            } else {
-                amp = cmk(r1, 0.0f);
-            }
-            if (J.prefix & ETRAJ_PREFIX_JAC) {
-                const float jac = spane ? fabsf(fmaf(sqrtf(k2) / (F * F), B.W, F)) : F;
-                amp = cscale(amp, sqrtf(jac));
-            }
-            rate = fmaf(amp.re, amp.re, amp.im * amp.im);
-            const float crit = spane ? rate * inv_dkdt : rate;
-            keep = (!(rate != rate) && !(crit < cutoff)) ? 1 : 0;
-            if (keep && want_phase) ph = atan2f(amp.im, amp.re);
-        }
-    }
-    C.x0 = x0;
-    C.y0 = y0;
-    C.kx0 = kx0;
-    C.ky0 = ky0;
-    C.rate = rate;
-    C.ph = ph;
-    C.crit = crit;
-    return keep;
-}
-
 __global__ void __launch_bounds__(256)
 k_sample32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double* __restrict__ kdv,
            const double* __restrict__ kzv, const DBatch* __restrict__ batches, InitSoA soa,
            uint8_t* __restrict__ flag) {
-    const float kd_max = J.fc.kd_max, kz_max = J.fc.kz_max;
+    const float Ip = J.fc.Ip, kap2 = J.fc.kap2, sqdkdt = J.fc.sqdkdt;
+    const float inv_dkdt = J.fc.inv_dkdt, cutoff = J.fc.cutoff, e_pre = J.fc.e_pre;
+    const float c_pre = J.fc.c, kd_max = J.fc.kd_max, kz_max = J.fc.kz_max;
+    const float spane_lim = J.mc ? 0.04f : 0.111111111f;  // 1/25, 1/9
+    const bool spane = (J.method == ETRAJ_SAMPLER_SPANE);
     const int64_t n = J.n_cand, stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t step_b = stride / n, step_i = stride - step_b * n;
     const int64_t q0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -833,9 +727,89 @@ k_sample32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double*
                 kz0 = 0.0f;
             }
         }
-        Cand32 C;
-        const uint8_t keep = cand32(J, B, b, kd0, kz0, J.phase != ETRAJ_PHASE_CTMC, C);
-        const float x0 = C.x0, y0 = C.y0, kx0 = C.kx0, ky0 = C.ky0, rate = C.rate, ph = C.ph;
+        uint8_t keep = 0;
+        float x0 = 0.0f, y0 = 0.0f, kx0 = 0.0f, ky0 = 0.0f, rate = 0.0f, ph = 0.0f;
+        if (J.method == ETRAJ_SAMPLER_WFAT) {
+            // WFATSampler.jl:173-240: ADK's exit point, the WFAT rate, CTMC rows
+            if (!(fmaf(kd0, kd0, kz0 * kz0) < 1e-8f)) {
+                const float F = B.F;
+                kx0 = kd0 * (-B.sphi);
+                ky0 = kd0 * B.cphi;
+                const float r0 = fmaf(0.5f, fmaf(kd0, kd0, kz0 * kz0), Ip) / F;
+                x0 = r0 * B.cphi;
+                y0 = r0 * B.sphi;
+                rate = wfat_rate32(J, J.mol.tabf + b * (int64_t)J.mol.stride, F, kd0, kz0);
+                keep = (!(rate != rate) && !(rate < cutoff)) ? 1 : 0;
+            }
+        } else if (!(fabsf(kd0) < 1e-4f)) {
+            const float F = B.F;
+            kx0 = kd0 * (-B.sphi);
+            ky0 = kd0 * B.cphi;
+            const float k2 = fmaf(kd0, kd0, kz0 * kz0);
+            const float Xk = k2 + 2.0f * Ip;
+            float ti, X2, Fexp;
+            bool skip = false;
+            if (!spane) {
+                const float r0 = fmaf(0.5f, k2, Ip) / F;
+                x0 = r0 * B.cphi;
+                y0 = r0 * B.sphi;
+                ti = sqrtf(kap2 + k2) / F;
+                X2 = Xk * (F * F);
+                Fexp = F;
+            } else {
+                const float F2eff = fmaf(F, F, -fmaf(kx0, B.dFx, ky0 * B.dFy));
+                const float r0 = ((0.5f * F) * Xk) / F2eff;
+                x0 = r0 * B.cphi;
+                y0 = r0 * B.sphi;
+                skip = (F2eff <= (F * F) * spane_lim);
+                ti = sqrtf((kap2 + k2) / F2eff);
+                X2 = Xk * F2eff;
+                Fexp = sqrtf(F2eff);
+            }
+            if (!skip) {
+                const float E = expf(-(Xk * sqrtf(Xk)) / (3.0f * Fexp));
+                const float r1 = sqdkdt * E;
+                cf amp;
+                if (J.prefix & (ETRAJ_PREFIX_PRE | ETRAJ_PREFIX_PRECC)) {
+                    cf kx, ky;
+                    if (!spane) {
+                        kx = cmk(kx0, -(ti * B.Fx));
+                        ky = cmk(ky0, -(ti * B.Fy));
+                    } else {
+                        const float h = 0.5f * ti * ti;
+                        kx = cmk(fmaf(h, B.dFx, kx0), -(ti * B.Fx));
+                        ky = cmk(fmaf(h, B.dFy, ky0), -(ti * B.Fy));
+                    }
+                    // rotate conj(k_ts) into the field frame (ADKSampler.jl:247-249)
+                    const cf nkx = cmk(kz0, 0.0f);
+                    const cf nky = cadd(cscale(cconj(kx), B.ny0), cscale(cconj(ky), B.ny1));
+                    const cf nkz = cadd(cscale(cconj(kx), B.nz0), cscale(cconj(ky), B.nz1));
+                    cf num = cmk(0.0f, 0.0f);
+                    if (J.mol.on) {
+                        num = mol_num32(J, J.mol.tabf + b * (int64_t)J.mol.stride, nkx, nky, nkz);
+                    } else {
+                        for (int mp = -J.l; mp <= J.l; ++mp) {
+                            const int ii = mp + J.l;
+                            const cf Y = cmul(cmk(J.fPlm[2 * ii], J.fPlm[2 * ii + 1]), sph_sum(J.l, mp, nkx, nky, nkz));
+                            num = cadd(num, cmul(cmk(B.CD[2 * ii], B.CD[2 * ii + 1]), Y));
+                        }
+                    }
+                    const float cpre = (J.prefix & ETRAJ_PREFIX_PRE) ? c_pre : B.c_cc;
+                    const float den = (e_pre == 0.5f) ? sqrtf(X2) : exp2f(e_pre * log2f(X2));
+                    amp = cscale(num, (cpre / den) * r1);
+                } else {
+                    amp = cmk(r1, 0.0f);
+                }
+                if (J.prefix & ETRAJ_PREFIX_JAC) {
+                    const float jac = spane ? fabsf(fmaf(sqrtf(k2) / (F * F), B.W, F)) : F;
+                    amp = cscale(amp, sqrtf(jac));
+                }
+                rate = fmaf(amp.re, amp.re, amp.im * amp.im);
+                const float crit = spane ? rate * inv_dkdt : rate;
+                keep = (!(rate != rate) && !(crit < cutoff)) ? 1 : 0;
+                if (keep && J.phase != ETRAJ_PHASE_CTMC) ph = atan2f(amp.im, amp.re);
+            }
+        }
         const int64_t g = b * J.n_cand + i;
         flag[g] = keep;
         if (keep) {
@@ -893,54 +867,7 @@ k_spa_prefilter(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const do
     }
 }
 
-// The FP64 ADK/SPANE sampler's pre-pass (atoms, uniform draws): each candidate's
-// cutoff value in FP32 (cand32) at the FP64 sampler's own (kd, kz) draws, and
-// flag[g] = 0 where it is more than 100 times below the cutoff, else 1.  FP32's
-// rate is within ~1e-5 of FP64's on this path, so a candidate marked 0 is one the
-// FP64 rule drops; the FP64 kernel then runs over the candidates marked 1 only,
-// and its survivors and their values do not change.
-__global__ void __launch_bounds__(256)
-k_rate_prefilter(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double* __restrict__ kdv,
-                 const double* __restrict__ kzv, const DBatch* __restrict__ batches, uint8_t* __restrict__ flag) {
-    const int64_t total = nb * J.n_cand;
-    const float lim = J.fc.cutoff * 0.01f;
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
-         q += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t bl = q / J.n_cand, i = q - bl * J.n_cand, b = b0 + bl;
-        double kd0, kz0;
-        if (!J.mc) {
-            kd0 = kdv[i / J.n_kz];
-            kz0 = kzv[i % J.n_kz];
-        } else {
-            uint32_t c[4] = {(uint32_t)i, (uint32_t)((uint64_t)i >> 32), (uint32_t)b, 0x4B445A00u};
-            philox4x32(c, J.seed);
-            const double ua = u53(c[0], c[1]), ub = u53(c[2], c[3]);
-            kd0 = ((ua - 0.5) * 2.0) * J.mc_kd_max;
-            if (J.dim == 3) {
-                kz0 = ((ub - 0.5) * 2.0) * J.mc_kz_max;
-                if (J.mc_kd_max == 0.0) kd0 = 0.0;
-                else if (J.mc_kz_max == 0.0) kz0 = 0.0;
-            } else {
-                kz0 = 0.0;
-            }
-        }
-        Cand32 C;
-        cand32(J, batches[b].f, b, (float)kd0, (float)kz0, false, C);
-        flag[b * J.n_cand + i] = (C.crit == C.crit && C.crit < lim) ? 0 : 1;
-    }
-}
-
 }  // namespace
-
-int launch_rate_prefilter(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
-                          const DBatch* batches, uint8_t* flag, int sm_count, cudaStream_t s) {
-    const int threads = 256;
-    const int64_t want = (nb * J.n_cand + threads - 1) / threads;
-    const int64_t cap = (int64_t)sm_count * 32;
-    const int blocks = (int)(want < cap ? (want > 0 ? want : 1) : cap);
-    k_rate_prefilter<<<blocks, threads, 0, s>>>(J, b0, nb, kd, kz, batches, flag);
-    return 1;
-}
 
 int launch_spa_prefilter(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
                          DBatch* batches, uint8_t* flag, int sm_count, cudaStream_t s) {
