@@ -101,9 +101,11 @@ k_onesweep_scan(const uint32_t* __restrict__ ghist, int npass, uint32_t* __restr
 // Posts of the look-back: a 64-bit word per (tile, digit), the count in the low 32
 // bits and above them 2p+1 ("this tile's count") or 2p+2 ("the count of this and
 // every earlier tile") for pass p, so one region, cleared once per sort, serves
-// every pass.  A wait gives up after kLookbackSpins polls (the tiles it waits for
-// belong to blocks of the same cooperative grid that took their tiles earlier,
-// so it never should) and raises *err.
+// every pass.  A block takes its tile from a counter, so every tile it waits for
+// was taken earlier by a block that is running, and that block posts its own
+// count before it waits on anything: the look-back needs no co-resident grid (a
+// plain launch, which other streams' kernels can share the GPU with).  A wait
+// gives up after kLookbackSpins polls (so it never should) and raises *err.
 constexpr int kLookbackSpins = 1 << 22;
 constexpr int kWindow = 16;  // posts a look-back step loads at once
 
@@ -546,8 +548,7 @@ int resident_blocks(const void* fn, int threads) {
     return cached[dev];
 }
 
-// The grid of k_onesweep_pass: the look-back waits only for tiles taken
-// earlier, by blocks of the same co-resident, cooperative grid.
+// The grid of k_onesweep_pass: as many blocks as fit on the device at once.
 int onesweep_blocks() { return resident_blocks<0>((const void*)k_onesweep_pass, kThreads); }
 
 // Stable LSD radix sort of (key, index) pairs on the low `bits` key bits, in as
@@ -593,9 +594,7 @@ int radix_sort(const uint32_t* keys, const unsigned long long* count, int64_t ma
         uint32_t* vo = vbuf[which];
         const uint32_t* bp = base + p * kMaxDigits;
         unsigned int* tc = tile_ctr + p;
-        void* args[] = {(void*)&kin, (void*)&vin, (void*)&ko, (void*)&vo, (void*)&count, (void*)&p,
-                        (void*)&shift, (void*)&w, (void*)&bp, (void*)&post, (void*)&tc, (void*)&err};
-        cudaLaunchCooperativeKernel((const void*)k_onesweep_pass, dim3(grid), dim3(kThreads), args, 0, s);
+        k_onesweep_pass<<<grid, kThreads, 0, s>>>(kin, vin, ko, vo, count, p, shift, w, bp, post, tc, err);
         ++launches;
         kin = ko;
         vin = vo;
