@@ -251,7 +251,7 @@ DFS_HD void clk_adv(int n, df f, df d, int& no, df& fo) {
 // exp(-b r) of the SAE potential; a lane with b r > 50 takes exactly 0, and on the
 // device a warp whose active lanes all do skips the evaluation: no lane's result
 // depends on the electrons that share its warp.
-DFS_HD df sae_exp(df b, df r, const float* exptab) {
+DFO df sae_exp(df b, df r, const float* exptab) {
     const df br = df_mul(b, r);
     const bool far = br.hi > kSaeSkip;
 #if defined(__CUDA_ARCH__)
