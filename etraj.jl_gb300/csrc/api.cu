@@ -741,15 +741,17 @@ void prepare_bulk(const DJob& J, double tmin, BulkParams& B) {
 }
 
 // Double-float integrator parameters (integrate_setup.h) and its launch shapes:
-// persistent grids of 128-thread blocks, as many as are resident, and no more
-// than the job keeps busy (~4 electrons per lane).
+// persistent grids, as many blocks as are resident, and no more than the job
+// keeps busy (~4 electrons per lane).
 void prepare_df(const DJob& J, double tmin, int64_t max_n, int sm_count, DFParams& D) {
     prepare_df_params(J, tmin, max_n, D);
-    D.threads = 128;
-    const int64_t lanes_per_block = (int64_t)D.threads * 4;
-    const int64_t want = (max_n + lanes_per_block - 1) / lanes_per_block;
+    D.threads = df_threads(false);
+    D.threads_main = df_threads(true);
     for (int main = 0; main < 2; ++main) {
-        const int64_t cap = (int64_t)sm_count * df_blocks_per_sm(D.dim, D.phase, D.tgt, main != 0, D.threads);
+        const int th = main ? D.threads_main : D.threads;
+        const int64_t lanes_per_block = (int64_t)th * 4;
+        const int64_t want = (max_n + lanes_per_block - 1) / lanes_per_block;
+        const int64_t cap = (int64_t)sm_count * df_blocks_per_sm(D.dim, D.phase, D.tgt, main != 0, th);
         (main ? D.blocks_main : D.blocks) = (int)(want < 1 ? 1 : (want < cap ? want : cap));
     }
 }

@@ -275,7 +275,7 @@ struct DFParams {
     float r2_far;         // SAE: r^2 beyond which every exp(-b_i r) of the potential is 0
     int max_iters;
     int threads, blocks;    // launch shape of the start-up pass (persistent grid)
-    int blocks_main;        // blocks of the main pass (threads each)
+    int threads_main, blocks_main;  // and of the main pass
     int64_t max_n;
     float* carry;           // kDfCarryWords x max_n words: electrons passed to the main pass
 };
@@ -299,6 +299,8 @@ int launch_integrate_df(const DFParams& P, InitSoA soa, const double* t, const i
                         cudaStream_t s);
 // Resident blocks per SM of a double-float integrator pass (main: the main pass).
 int df_blocks_per_sm(int dim, int phase, int tgt, bool main, int threads);
+// threads per block of the double-float integrator's passes (their launch bounds)
+int df_threads(bool main);
 
 // Deterministic deposit: stable radix sort of (key, survivor) and segmented sums.
 struct DepositScratch {

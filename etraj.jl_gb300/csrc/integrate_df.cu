@@ -52,14 +52,17 @@ __device__ const float g_df_rcpc[2 * kLogTabN] = {ETRAJ_DF_RCPC_TABLE};
 
 namespace {
 
-constexpr int kDfThreads = 128;
-// Resident 128-thread blocks per SM the passes' register budgets are set for (168
-// and 128 registers a thread; a few hundred bytes spill).  On the argon headline
-// job (4.0e6 electrons) the integrator took 93.8, 93.5, 96.9 and 98.8 ms with the
-// budgets (3, 4), (2, 4), (4, 4) and (3, 5), with identical results; without
-// launch bounds (up to 251 registers) it took 139 ms.
+// Threads per block and resident blocks per SM of the two passes: register budgets
+// of 168 (start-up) and 128 (main) a thread, a few hundred bytes spilled.  With
+// 128-thread blocks the argon headline job (4.0e6 electrons) took 93.8, 93.5, 96.9
+// and 98.8 ms with (3, 4), (2, 4), (4, 4) and (3, 5) blocks, with identical
+// results; without launch bounds (up to 251 registers) it took 139 ms.  With the
+// warps of a block in step (below), main-pass blocks of 256 threads were 4 %
+// faster than 128 and 3 % faster than 512 (2e6-candidate job: 13.5, 14.1, 13.9 ms).
+constexpr int kDfThreadsStart = 128;
 constexpr int kDfMinBlocksStart = 3;
-constexpr int kDfMinBlocksMain = 4;
+constexpr int kDfThreadsMain = 256;
+constexpr int kDfMinBlocksMain = 2;
 
 template <int DIM, int PHASE>
 constexpr int slot_floats() {
@@ -74,7 +77,7 @@ enum LaneMode { kFree = 0, kBase = 1, kInit1 = 2, kWait = 3, kStep = 4 };
 // MAIN = true: the main pass over the carried electrons, every stage direct.
 // work[0] and work[2] are the passes' queues, work[1] counts carried electrons.
 template <int DIM, int PHASE, int TGT, bool MAIN>
-__global__ void __launch_bounds__(kDfThreads, MAIN ? kDfMinBlocksMain : kDfMinBlocksStart)
+__global__ void __launch_bounds__(MAIN ? kDfThreadsMain : kDfThreadsStart, MAIN ? kDfMinBlocksMain : kDfMinBlocksStart)
 k_integrate_df(const __grid_constant__ DFParams P, InitSoA soa, const double* __restrict__ tsamp,
                const int64_t* __restrict__ idx, const unsigned long long* __restrict__ count,
                unsigned long long* __restrict__ work, TrajOut out) {
@@ -115,7 +118,11 @@ k_integrate_df(const __grid_constant__ DFParams P, InitSoA soa, const double* __
         mode = kFree;
     };
 
+    // The block's warps go through the evaluations in step (a barrier at each): the
+    // loop's code is far larger than the instruction cache, and warps at the same
+    // place share the lines they fetch.
     for (int st = 1;; st = (st == 6) ? 1 : st + 1) {
+        if (st != 1) __syncthreads();
         if (st == 1) {
             // ---- attempt boundary: hand over, start the next attempts, refill ------------
             if (mode == kWait) mode = kStep;
@@ -167,7 +174,7 @@ k_integrate_df(const __grid_constant__ DFParams P, InitSoA soa, const double* __
                     }
                 }
             }
-            if (__ballot_sync(FULL, mode != kFree) == 0u) break;
+            if (!__syncthreads_or(mode != kFree)) break;  // the block leaves together
         }
         // ---- the inputs of this turn's evaluation ------------------------------------------
         if (mode == kStep) dfs::stage_in<MAIN>(L, ks, st);
@@ -216,18 +223,40 @@ __global__ void k_field_table_df(const __grid_constant__ DJob J, double T0, doub
     dfs::table_piece(J.laser, T0, h, k, nodes, tab + kDfTableF4 * (size_t)k);
 }
 
+// Both passes may take the stage slots of their whole block in dynamic shared
+// memory (up to kDfThreads x slot_floats floats, above the default 48 KB).
+template <int DIM, int PHASE, int TGT>
+void allow_smem() {
+    static bool done[64] = {};  // per device
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        dev = 0;
+    }
+    if (done[dev]) return;
+    const int most = (int)((size_t)slot_floats<DIM, PHASE>() * sizeof(float) *
+                           (size_t)(kDfThreadsMain > kDfThreadsStart ? kDfThreadsMain : kDfThreadsStart));
+    cudaFuncSetAttribute(k_integrate_df<DIM, PHASE, TGT, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+    cudaFuncSetAttribute(k_integrate_df<DIM, PHASE, TGT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+    done[dev] = true;
+}
+
 template <int DIM, int PHASE, int TGT>
 int launch_df_t(const DFParams& P, InitSoA soa, const double* t, const int64_t* idx, const unsigned long long* count,
                 unsigned long long* work, TrajOut out, cudaStream_t s) {
     const size_t smem = (size_t)slot_floats<DIM, PHASE>() * sizeof(float) * (size_t)P.threads;
+    const size_t smem_main = (size_t)slot_floats<DIM, PHASE>() * sizeof(float) * (size_t)P.threads_main;
+    allow_smem<DIM, PHASE, TGT>();
     cudaMemsetAsync(work, 0, 3 * sizeof(unsigned long long), s);
     k_integrate_df<DIM, PHASE, TGT, false><<<P.blocks, P.threads, smem, s>>>(P, soa, t, idx, count, work, out);
-    k_integrate_df<DIM, PHASE, TGT, true><<<P.blocks_main, P.threads, smem, s>>>(P, soa, t, idx, count, work, out);
+    k_integrate_df<DIM, PHASE, TGT, true><<<P.blocks_main, P.threads_main, smem_main, s>>>(P, soa, t, idx, count,
+                                                                                         work, out);
     return 2;
 }
 
 template <int DIM, int PHASE, int TGT>
 int blocks_t(bool main, int threads) {
+    allow_smem<DIM, PHASE, TGT>();
     const size_t smem = (size_t)slot_floats<DIM, PHASE>() * sizeof(float) * (size_t)threads;
     int nb = 0;
     const cudaError_t e =
@@ -267,6 +296,8 @@ int launch_field_table_df(const DJob& J, double T0, double h, int n_int, const D
                                                  : FN<3, ETRAJ_PHASE_QTMC, ETRAJ_TARGET_SAE> ARGS;             \
     return tgt == ETRAJ_TARGET_HYDROGEN_LIKE ? FN<3, ETRAJ_PHASE_SCTS, ETRAJ_TARGET_HYDROGEN_LIKE> ARGS         \
                                              : FN<3, ETRAJ_PHASE_SCTS, ETRAJ_TARGET_SAE> ARGS;
+
+int df_threads(bool main) { return main ? kDfThreadsMain : kDfThreadsStart; }
 
 int launch_integrate_df(const DFParams& P, InitSoA soa, const double* t, const int64_t* idx,
                         const unsigned long long* count, unsigned long long* work, TrajOut out, cudaStream_t s) {
