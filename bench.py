@@ -120,9 +120,9 @@ INTEGRATOR_DRAM_BYTES_PER_ELECTRON = 30.48
 # the passes (116 B per electron) stays in L2; at full size it adds about that much
 # per electron again.  FMA-pipe issue (sm__inst_executed_pipe_fma, warp
 # instructions against 4 per SM and cycle) was 35.3 % (start-up) and 41.5 % (main).
-DF_FP32_INST_PER_STEP = 6680
+DF_FP32_INST_PER_STEP = 6717
 DF_DRAM_BYTES_PER_ELECTRON = 189.0
-DF_FMA_PIPE_ISSUE_NCU = {"start_up": 0.353, "main": 0.415}
+DF_FMA_PIPE_ISSUE_NCU = {"start_up": 0.348, "main": 0.505}
 
 
 def rank_env():
