@@ -52,15 +52,17 @@ __device__ const float g_df_rcpc[2 * kLogTabN] = {ETRAJ_DF_RCPC_TABLE};
 
 namespace {
 
-// Threads per block and resident blocks per SM of the two passes: register budgets
-// of 168 (start-up) and 128 (main) a thread, a few hundred bytes spilled.  With
-// 128-thread blocks the argon headline job (4.0e6 electrons) took 93.8, 93.5, 96.9
-// and 98.8 ms with (3, 4), (2, 4), (4, 4) and (3, 5) blocks, with identical
-// results; without launch bounds (up to 251 registers) it took 139 ms.  With the
-// warps of a block in step (below), main-pass blocks of 256 threads were 4 %
-// faster than 128 and 3 % faster than 512 (2e6-candidate job: 13.5, 14.1, 13.9 ms).
-constexpr int kDfThreadsStart = 128;
-constexpr int kDfMinBlocksStart = 3;
+// Threads per block and resident blocks per SM of the two passes: a register
+// budget of 128 a thread, a few hundred bytes spilled.  With 128-thread blocks
+// whose warps ran freely, the argon headline job (4.0e6 electrons) took 93.8,
+// 93.5, 96.9 and 98.8 ms with (start-up, main) blocks per SM of (3, 4), (2, 4),
+// (4, 4) and (3, 5), with identical results; without launch bounds (up to 251
+// registers) it took 139 ms.  With the warps of a block in step (below), blocks
+// of 256 threads were faster than 128 or 512 on a 2e6-candidate job: main pass
+// 13.5 ms against 14.1 and 13.9; start-up pass in 2 x 256 threads (128
+// registers) against 3 x 128 (168 registers), 13.2 against 13.5 ms for both.
+constexpr int kDfThreadsStart = 256;
+constexpr int kDfMinBlocksStart = 2;
 constexpr int kDfThreadsMain = 256;
 constexpr int kDfMinBlocksMain = 2;
 
