@@ -361,7 +361,7 @@ constexpr int kTreeWarps = 8;
 
 // One read of the per-trajectory outputs, in trajectory order, for all the
 // deposit needs from them besides the sort: the digit counts of every sort pass
-// (as k_onesweep_hist), level 0 of the canonical trees (as k_tree_level) and the
+// (as k_onesweep_hist), level 0 of the canonical trees (tree_nodes) and the
 // counters.  A warp takes a node of 256 trajectories, lane j its slots 8j..8j+7,
 // loaded as 16-byte vectors when the node is whole and the arrays are aligned.
 // The block that finishes last adds the tree's upper levels and writes the sums
@@ -699,7 +699,7 @@ __global__ void k_inst_segments(const int64_t* __restrict__ idx, const unsigned 
     seg[i] = lo;
 }
 
-// The canonical ion_prob tree (k_tree_level's node rule) over one instance's
+// The canonical ion_prob tree (tree_node's rule) over one instance's
 // segment per block, levels ping-ponging between two scratch regions.
 __global__ void __launch_bounds__(256)
 k_inst_tree(const double* __restrict__ wa, const double* __restrict__ wb, const int64_t* __restrict__ seg,
