@@ -547,7 +547,7 @@ def trajectory_stats(eng, job, job64):
             "step_counts_differing_from_fp64": int(np.sum(s32 != s64)) if s32.shape == s64.shape else None}
 
 
-def serving_requests(n=512, rate=20.0, seed=2024):
+def serving_requests(n=512, rate=20.0, seed=2024, precision="fp32_bulk"):
     """The serving workload: n requests with Poisson arrivals at `rate` per second,
     each a random mix of target {H, Ar}, laser {Cos4 LP, Cos2 CP, counter-rotating
     CP bichromatic (lambda, lambda/2)}, wavelength U(400, 1600) nm, intensity
@@ -580,17 +580,18 @@ def serving_requests(n=512, rate=20.0, seed=2024):
                           final_p_max=(2.0, 2.0), final_p_num=(grid, grid), sample_monte_carlo=True,
                           mc_kt_num=1000, mc_kd_max=1.0,
                           traj_phase_method=("CTMC", "QTMC", "SCTS")[int(rng.integers(0, 3))],
-                          seed=i, precision="fp32_bulk")
+                          seed=i, precision=precision)
         reqs.append(job)
     return arrivals, reqs
 
 
-def serving_report(n=512, rate=20.0, slots=8, fp64_seconds=20.0):
-    """Replays the request stream in real time against an etraj server (bulk
-    path) and reports arrival-to-result latency and aggregate throughput; then
-    serves the stream's first requests one at a time on the FP64 path, for
-    about `fp64_seconds` (a request's time is set by its slowest trajectory)."""
-    arrivals, reqs = serving_requests(n, rate)
+def serving_report(n=512, rate=20.0, slots=8, fp64_seconds=20.0, precision="fp32_bulk"):
+    """Replays the request stream in real time against an etraj server (at
+    `precision`) and reports arrival-to-result latency and aggregate throughput;
+    then, unless fp64_seconds is 0, serves the stream's first requests one at a
+    time on the FP64 path, for about `fp64_seconds` (a request's time is set by
+    its slowest trajectory)."""
+    arrivals, reqs = serving_requests(n, rate, precision=precision)
     srv = et.Server(device=0, slots=slots)
     # warm-up: one small job per slot
     for t in [srv.submit(reqs[k]) for k in range(slots)]:
@@ -619,29 +620,31 @@ def serving_report(n=512, rate=20.0, slots=8, fp64_seconds=20.0):
             time.sleep(0.0005)
     span = time.perf_counter() - t0 - arrivals[0]
     srv.close()
-    eng = et.Engine(device=0)
-    fp64_ms, fp64_eff = [], []
-    for job in reqs:
-        j = job.copy()
-        j.precision = abi.PRECISION_FP64
-        t1 = time.perf_counter()
-        r, _, _ = eng.run(j, want_spectrum=True)
-        fp64_ms.append(1e3 * (time.perf_counter() - t1))
-        fp64_eff.append(r.num_effective_traj)
-        if sum(fp64_ms) > 1e3 * fp64_seconds:
-            break
-    eng.close()
     lat_ms = 1e3 * np.array(lat)
-    fp64_rate = sum(fp64_eff) / (sum(fp64_ms) / 1e3)
-    return {"requests": n, "arrival_rate_per_s": rate, "slots": slots,
-            "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99)),
-                           "max": float(lat_ms.max())},
-            "trajectories_per_s": float(sum(effs) / span), "effective_trajectories": int(sum(effs)),
-            "span_s": float(span), "max_running": max_running, "max_queued": max_queued,
-            "fp64_one_at_a_time": {"requests": len(fp64_ms), "trajectories_per_s": fp64_rate,
-                                   "mean_service_ms": float(np.mean(fp64_ms)),
-                                   "offered_load_vs_capacity": float(rate * np.mean(fp64_ms) / 1e3)},
-            "workload": serving_requests.__doc__.split("\n\n")[0].replace("\n    ", " ")}
+    out = {"precision": precision, "requests": n, "arrival_rate_per_s": rate, "slots": slots,
+           "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99)),
+                          "max": float(lat_ms.max())},
+           "trajectories_per_s": float(sum(effs) / span), "effective_trajectories": int(sum(effs)),
+           "span_s": float(span), "max_running": max_running, "max_queued": max_queued,
+           "workload": serving_requests.__doc__.split("\n\n")[0].replace("\n    ", " ")}
+    if fp64_seconds > 0:
+        eng = et.Engine(device=0)
+        fp64_ms, fp64_eff = [], []
+        for job in reqs:
+            j = job.copy()
+            j.precision = abi.PRECISION_FP64
+            t1 = time.perf_counter()
+            r, _, _ = eng.run(j, want_spectrum=True)
+            fp64_ms.append(1e3 * (time.perf_counter() - t1))
+            fp64_eff.append(r.num_effective_traj)
+            if sum(fp64_ms) > 1e3 * fp64_seconds:
+                break
+        eng.close()
+        out["fp64_one_at_a_time"] = {"requests": len(fp64_ms),
+                                     "trajectories_per_s": sum(fp64_eff) / (sum(fp64_ms) / 1e3),
+                                     "mean_service_ms": float(np.mean(fp64_ms)),
+                                     "offered_load_vs_capacity": float(rate * np.mean(fp64_ms) / 1e3)}
+    return out
 
 
 def multi_instance_jobs(n=64, seed=7):
