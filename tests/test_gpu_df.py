@@ -120,3 +120,21 @@ def test_df_rejects_spans_beyond_its_clock(eng):
     with pytest.raises(et.EtrajError) as e:
         eng.run(job)
     assert e.value.status == abi.ERR_UNSUPPORTED
+
+
+def test_df_small_and_empty_jobs(eng):
+    """The passes' warps go through the stages in step and a block leaves when all
+    of its lanes are free: jobs of a few electrons (most warps of a block without
+    work), of just over one block, and of none, against the FP64 path."""
+    empty = job_of(method="ADK", dim=2, cutoff=1e300)
+    empty.precision = abi.PRECISION_FP32_DF
+    res, spec, _ = eng.run(empty)
+    assert res.num_effective_traj == 0 and res.ion_prob == 0.0 and not spec.any()
+    for kw in (dict(method="ADK", dim=2, nt=4, nkd=9),                # 4 electrons
+               dict(method="ADK", dim=3, phase="QTMC", nt=6, nkd=9, nkz=5),  # a few tens
+               dict(method="SPANE", dim=2, phase="SCTS", target="Ar", laser="cos2", ellip=1.0,
+                    mc=True, nt=12, nkd=300, nkz=1, intensity=1.2e14)):  # 1329: two blocks of 1024 lanes' work
+        job = job_of(**kw)
+        r64, _, _ = eng.run(job)
+        assert 0 < r64.num_effective_traj < 2048, r64.num_effective_traj
+        compare_df_fp64(eng, job)
