@@ -32,12 +32,6 @@ using namespace etraj;
 
 #define ETRAJ_VERSION_STRING "etraj-gb300 1.0 (sm_103a)"
 
-namespace etraj {
-int launch_sample_range(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
-                        DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
-                        cudaStream_t s);
-}
-
 namespace {
 
 constexpr bool kHaveFp32Bulk = true;
@@ -647,12 +641,19 @@ int alloc_outputs(etraj_ctx* ctx, const DJob& J, int64_t max_n, bool with_state,
 // WFAT, atoms and molecules, while every kept rate stays in FP32's normal
 // range; SPA for atoms), the FP64 path and molecular SPA in FP64.
 int launch_sampler(int precision, const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
-                   DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count, cudaStream_t s) {
-    // (a Gaussian-proposal job samples in FP64 on every path)
+                   DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count, cudaStream_t s,
+                   const SampleScratch* scr) {
+    // (a Gaussian-proposal job samples in FP64 on every path; the listed FP64 SPA
+    // sampler serves double-float jobs only)
     const bool fp32 = precision == ETRAJ_PRECISION_FP32_BULK && !J.gauss &&
                       (J.method == ETRAJ_SAMPLER_SPA ? !J.mol.on : J.cutoff >= kSample32MinCutoff);
     return fp32 ? launch_sample32_range(J, b0, nb, kd, kz, batches, soa, flag, sm_count, s)
-                : launch_sample_range(J, b0, nb, kd, kz, batches, soa, flag, sm_count, s);
+                : launch_sample_range(J, b0, nb, kd, kz, batches, soa, flag, sm_count, s,
+                                      precision == ETRAJ_PRECISION_FP32_DF ? scr : nullptr);
+}
+
+SampleScratch sample_scratch(const Pipeline& P, int64_t n) {
+    return SampleScratch{P.idx, P.block_sums, compact_blocks(n) + 1, P.count};
 }
 
 // Copies a job's host inputs (time and momentum samples, molecular tables) to the device.
@@ -1063,7 +1064,9 @@ int enqueue_kernels(etraj_ctx* ctx, const etraj_job* job, const HostJob& H, cons
     int launches = 0;
     rec(ctx, ctx->stage_ev[0], s);
     launches += launch_batch_prepare(J, P.t, P.batches, s);
-    launches += launch_sampler(job->precision, J, 0, J.n_t, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s);
+    const SampleScratch scr = sample_scratch(P, J.n_total);
+    launches += launch_sampler(job->precision, J, 0, J.n_t, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s,
+                               &scr);
     rec(ctx, ctx->stage_ev[1], s);
     launches += launch_compact(P.flag, J.n_total, P.idx, P.block_sums, compact_blocks(J.n_total) + 1, P.count, s);
     rec(ctx, ctx->stage_ev[2], s);
@@ -1410,7 +1413,7 @@ int run_batch(etraj_ctx* ctx, const etraj_job* jobs, int n, etraj_result* res, c
             so.x += c; so.y += c; so.kx += c; so.ky += c; so.kz += c; so.rate += c; so.batch += c;
             if (so.phase) so.phase += c;
             launches += launch_sampler(ETRAJ_PRECISION_FP32_BULK, J, 0, J.n_t, P.kd + koff[i], P.kz + zoff[i], bat, so,
-                                       P.flag + c, ctx->sm_count, s);
+                                       P.flag + c, ctx->sm_count, s, nullptr);
         }
         rec(ctx, ctx->stage_ev[1], s);
         launches += launch_compact(P.flag, N, P.idx, P.block_sums, compact_blocks(N) + 1, P.count, s);
@@ -1580,7 +1583,8 @@ int sample_range(etraj_ctx* ctx, const etraj_job* job, int64_t b0, int64_t nb, d
     cudaStream_t s = ctx->stream;
     upload_inputs(H, P, s);
     launch_batch_prepare(H.J, P.t, P.batches, s);
-    launch_sampler(job->precision, H.J, b0, nb, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s);
+    const SampleScratch scr = sample_scratch(P, H.J.n_total);
+    launch_sampler(job->precision, H.J, b0, nb, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s, &scr);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_err(ctx, e, "sample launch");
     return gather_rows(ctx, H, P, b0 * H.J.n_cand, nb * H.J.n_cand, init, capacity, count);

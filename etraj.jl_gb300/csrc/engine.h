@@ -159,13 +159,22 @@ struct Counters {
 int launch_batch_prepare(const DJob& J, const double* t, DBatch* batches, cudaStream_t s);
 // Samples the candidates of time samples [b0, b0+nb) (flag and SoA indexed by
 // b * n_cand + i).
+// The FP64 SPA sampler's list for double-float jobs (the candidates its FP32
+// pre-pass may keep), in the survivors' compaction buffers, which are free until
+// that compaction runs.
+struct SampleScratch {
+    int64_t* list;
+    uint32_t* block_sums;
+    int64_t block_cap;
+    unsigned long long* count;
+};
 int launch_sample_range(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
                         DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
-                        cudaStream_t s);
+                        cudaStream_t s, const SampleScratch* scr);
 // The FP64 SPA sampler's FP32 pre-pass (atoms): fills batches[b].spa and sets
 // flag = 0 for the candidates whose FP32 rate is more than 100 times below the cutoff.
 int launch_spa_prefilter(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
-                         DBatch* batches, uint8_t* flag, int sm_count, cudaStream_t s);
+                         DBatch* batches, float log_margin, uint8_t* flag, int sm_count, cudaStream_t s);
 // FP32 variant of the same kernel for the bulk path (sampler_fp32.cu); used
 // when the rate cutoff keeps every kept rate in FP32's normal range.
 // Its SPA variant first fills batches[b].spa of the batches it samples.

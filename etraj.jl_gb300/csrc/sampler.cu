@@ -514,13 +514,16 @@ k_compact_scatter(const uint8_t* __restrict__ flag, int64_t n, const uint32_t* _
 __global__ void __launch_bounds__(128)
 k_sample_spa(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double* __restrict__ kdv,
              const double* __restrict__ kzv, const DBatch* __restrict__ batches, InitSoA soa,
-             uint8_t* __restrict__ flag, int prefiltered) {
-    const int64_t total = nb * J.n_cand;
+             uint8_t* __restrict__ flag, int prefiltered, const int64_t* __restrict__ list,
+             const unsigned long long* __restrict__ lcount) {
+    // every candidate of the range, or (list) the *lcount candidates it names
+    const int64_t total = list ? (int64_t)*lcount : nb * J.n_cand;
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
          q += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t bl = q / J.n_cand, i = q - bl * J.n_cand, b = b0 + bl;
-        // a candidate the FP32 pre-pass found far below the cutoff (flag 0) keeps flag 0
-        if (prefiltered && flag[b * J.n_cand + i] == 0) continue;
+        const int64_t c = list ? list[q] : q;
+        const int64_t bl = c / J.n_cand, i = c - bl * J.n_cand, b = b0 + bl;
+        // a candidate the FP32 pre-pass dropped (flag 0) keeps flag 0
+        if (!list && prefiltered && flag[b * J.n_cand + i] == 0) continue;
         const DBatch& B = batches[b];
         double kd0, kz0;
         if (!J.mc) {
@@ -623,17 +626,26 @@ int launch_batch_prepare(const DJob& J, const double* t, DBatch* batches, cudaSt
 
 int launch_sample_range(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
                         DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
-                        cudaStream_t s) {
+                        cudaStream_t s, const SampleScratch* scr) {
     if (J.method == ETRAJ_SAMPLER_SPA) {
-        // atoms: an FP32 pre-pass marks the candidates far below the cutoff, which
-        // the FP64 kernel then skips (molecules: every candidate in FP64)
+        // atoms: an FP32 pre-pass marks the candidates below the cutoff (FP64 jobs:
+        // far below), which the FP64 kernel then skips; for double-float jobs (scr)
+        // a compaction lists the others and the FP64 kernel runs over the list,
+        // so its warps hold only candidates it may keep (molecules: every
+        // candidate in FP64)
         const int pre = J.mol.on ? 0 : 1;
-        int launches = pre ? launch_spa_prefilter(J, b0, nb, kd, kz, batches, flag, sm_count, s) : 0;
+        const bool listed = pre && scr && compact_blocks(nb * J.n_cand) + 1 <= scr->block_cap;
+        const float log_margin = listed ? -0.22314355f : -4.6051702f;  // log(0.8), log(1/100)
+        int launches = pre ? launch_spa_prefilter(J, b0, nb, kd, kz, batches, log_margin, flag, sm_count, s) : 0;
+        if (listed)
+            launches += launch_compact(flag + b0 * J.n_cand, nb * J.n_cand, scr->list, scr->block_sums,
+                                       scr->block_cap, scr->count, s);
         const int threads = 128;
         const int64_t want = (nb * J.n_cand + threads - 1) / threads;
         const int64_t cap = (int64_t)sm_count * 64;
         const int blocks = (int)(want < cap ? (want > 0 ? want : 1) : cap);
-        k_sample_spa<<<blocks, threads, 0, s>>>(J, b0, nb, kd, kz, batches, soa, flag, pre);
+        k_sample_spa<<<blocks, threads, 0, s>>>(J, b0, nb, kd, kz, batches, soa, flag, pre,
+                                                 listed ? scr->list : nullptr, listed ? scr->count : nullptr);
         return launches + 1;
     }
     int threads = 256;

@@ -826,17 +826,21 @@ k_sample32(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double*
 }
 
 // The FP64 SPA sampler's pre-pass (atoms): each candidate's rate in FP32 at the FP64
-// sampler's own (kd, kz) draws, and flag[g] = 0 where that rate is more than 100
-// times below the cutoff -- a candidate the FP64 rate cannot keep (FP32's rate is
-// within 3e-3 of FP64's where both solve, and the FP32 sampler keeps the FP64
-// sampler's electrons but for a few in 1e6, at the cutoff) -- else 1.  k_sample_spa then skips the
-// candidates marked 0 and computes every other one in FP64 as before, so its
-// survivors and their values do not change.
+// sampler's own (kd, kz) draws, and flag[g] = 0 where its FP32 solve succeeds and
+// that rate is below exp(log_margin) x the cutoff, else 1.  The FP64 path uses a
+// margin of 1/100: a candidate so far below is one the FP64 rate cannot keep
+// (FP32's rate is within 3e-3 of FP64's where both solve, and the FP32 sampler
+// keeps the FP64 sampler's electrons but for a few in 1e6, at the cutoff), so its
+// survivors and their values do not change.  Double-float jobs use 0.8: a
+// candidate dropped then that FP64 would keep weighs about the cutoff (1e-16 of a
+// rate on the headline jobs).  k_sample_spa then computes every candidate marked
+// 1 in FP64 as before.
 __global__ void __launch_bounds__(128)
 k_spa_prefilter(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const double* __restrict__ kdv,
-                const double* __restrict__ kzv, const DBatch* __restrict__ batches, uint8_t* __restrict__ flag) {
+                const double* __restrict__ kzv, const DBatch* __restrict__ batches, float log_margin,
+                uint8_t* __restrict__ flag) {
     const int64_t total = nb * J.n_cand;
-    const float lr_drop = logf(J.fc.cutoff) - 4.6051702f;  // log(cutoff / 100)
+    const float lr_drop = logf(J.fc.cutoff) + log_margin;
     for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < total;
          q += (int64_t)gridDim.x * blockDim.x) {
         const int64_t bl = q / J.n_cand, i = q - bl * J.n_cand, b = b0 + bl;
@@ -870,14 +874,14 @@ k_spa_prefilter(const __grid_constant__ DJob J, int64_t b0, int64_t nb, const do
 }  // namespace
 
 int launch_spa_prefilter(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
-                         DBatch* batches, uint8_t* flag, int sm_count, cudaStream_t s) {
+                         DBatch* batches, float log_margin, uint8_t* flag, int sm_count, cudaStream_t s) {
     const int64_t bb = (3 * nb + 127) / 128;
     k_spa32_bases<<<(int)(bb > 0 ? bb : 1), 128, 0, s>>>(J, b0, nb, batches);
     const int threads = 128;
     const int64_t want = (nb * J.n_cand + threads - 1) / threads;
     const int64_t cap = (int64_t)sm_count * 64;
     const int blocks = (int)(want < cap ? (want > 0 ? want : 1) : cap);
-    k_spa_prefilter<<<blocks, threads, 0, s>>>(J, b0, nb, kd, kz, batches, flag);
+    k_spa_prefilter<<<blocks, threads, 0, s>>>(J, b0, nb, kd, kz, batches, log_margin, flag);
     return 2;
 }
 

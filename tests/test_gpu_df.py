@@ -71,6 +71,9 @@ CASES = [
     dict(method="ADK", dim=2, phase="QTMC", target="Xe", laser="cos4", ellip=1.0, nt=200, nkd=101),
     dict(proposal="adk_gauss", method="SPANE", dim=2, phase="SCTS", target="Ar", laser="cos2", ellip=1.0,
          mc=True, nt=300, nkd=200, nkz=1, intensity=1.2e14),
+    # SPA: the FP64 sampler over the candidates its FP32 pre-pass keeps at 0.8 x the cutoff
+    dict(method="SPA", dim=2, phase="SCTS", target="Ar", laser="cos2", ellip=1.0, nt=64, nkd=61),
+    dict(method="SPA", dim=3, phase="QTMC", target="H", laser="bichrom", mc=True, nt=40, nkd=20, nkz=20),
 ]
 
 
