@@ -643,17 +643,20 @@ int alloc_outputs(etraj_ctx* ctx, const DJob& J, int64_t max_n, bool with_state,
 int launch_sampler(int precision, const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
                    DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count, cudaStream_t s,
                    const SampleScratch* scr) {
-    // (a Gaussian-proposal job samples in FP64 on every path; the listed FP64 SPA
-    // sampler serves double-float jobs only)
+    // (a Gaussian-proposal job samples in FP64 on every path)
     const bool fp32 = precision == ETRAJ_PRECISION_FP32_BULK && !J.gauss &&
                       (J.method == ETRAJ_SAMPLER_SPA ? !J.mol.on : J.cutoff >= kSample32MinCutoff);
     return fp32 ? launch_sample32_range(J, b0, nb, kd, kz, batches, soa, flag, sm_count, s)
-                : launch_sample_range(J, b0, nb, kd, kz, batches, soa, flag, sm_count, s,
-                                      precision == ETRAJ_PRECISION_FP32_DF ? scr : nullptr);
+                : launch_sample_range(J, b0, nb, kd, kz, batches, soa, flag, sm_count, s, scr);
 }
 
-SampleScratch sample_scratch(const Pipeline& P, int64_t n) {
-    return SampleScratch{P.idx, P.block_sums, compact_blocks(n) + 1, P.count};
+// The FP64 SPA sampler's list and margin: double-float jobs drop candidates whose
+// FP32 rate is below 0.8 x the cutoff (the same electrons survive: FP32's SPA rate
+// is within 3e-3 of FP64's where both solve); FP64 jobs only those 100 times
+// below, which keeps the oracle's sampler exactly.
+SampleScratch sample_scratch(const Pipeline& P, int64_t n, int precision) {
+    const float log_margin = (precision == ETRAJ_PRECISION_FP32_DF) ? -0.22314355f : -4.6051702f;
+    return SampleScratch{P.idx, P.block_sums, compact_blocks(n) + 1, P.count, log_margin};
 }
 
 // Copies a job's host inputs (time and momentum samples, molecular tables) to the device.
@@ -1064,7 +1067,7 @@ int enqueue_kernels(etraj_ctx* ctx, const etraj_job* job, const HostJob& H, cons
     int launches = 0;
     rec(ctx, ctx->stage_ev[0], s);
     launches += launch_batch_prepare(J, P.t, P.batches, s);
-    const SampleScratch scr = sample_scratch(P, J.n_total);
+    const SampleScratch scr = sample_scratch(P, J.n_total, job->precision);
     launches += launch_sampler(job->precision, J, 0, J.n_t, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s,
                                &scr);
     rec(ctx, ctx->stage_ev[1], s);
@@ -1583,7 +1586,7 @@ int sample_range(etraj_ctx* ctx, const etraj_job* job, int64_t b0, int64_t nb, d
     cudaStream_t s = ctx->stream;
     upload_inputs(H, P, s);
     launch_batch_prepare(H.J, P.t, P.batches, s);
-    const SampleScratch scr = sample_scratch(P, H.J.n_total);
+    const SampleScratch scr = sample_scratch(P, H.J.n_total, job->precision);
     launch_sampler(job->precision, H.J, b0, nb, P.kd, P.kz, P.batches, P.soa, P.flag, ctx->sm_count, s, &scr);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_err(ctx, e, "sample launch");

@@ -159,14 +159,16 @@ struct Counters {
 int launch_batch_prepare(const DJob& J, const double* t, DBatch* batches, cudaStream_t s);
 // Samples the candidates of time samples [b0, b0+nb) (flag and SoA indexed by
 // b * n_cand + i).
-// The FP64 SPA sampler's list for double-float jobs (the candidates its FP32
-// pre-pass may keep), in the survivors' compaction buffers, which are free until
-// that compaction runs.
+// The FP64 SPA sampler's list (the candidates its FP32 pre-pass may keep), in the
+// survivors' compaction buffers, which are free until that compaction runs, and
+// the pre-pass's margin: it drops candidates whose FP32 rate is below
+// exp(log_margin) x the cutoff.
 struct SampleScratch {
     int64_t* list;
     uint32_t* block_sums;
     int64_t block_cap;
     unsigned long long* count;
+    float log_margin;
 };
 int launch_sample_range(const DJob& J, int64_t b0, int64_t nb, const double* kd, const double* kz,
                         DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,

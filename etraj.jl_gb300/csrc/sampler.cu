@@ -628,14 +628,14 @@ int launch_sample_range(const DJob& J, int64_t b0, int64_t nb, const double* kd,
                         DBatch* batches, InitSoA soa, uint8_t* flag, int sm_count,
                         cudaStream_t s, const SampleScratch* scr) {
     if (J.method == ETRAJ_SAMPLER_SPA) {
-        // atoms: an FP32 pre-pass marks the candidates below the cutoff (FP64 jobs:
-        // far below), which the FP64 kernel then skips; for double-float jobs (scr)
-        // a compaction lists the others and the FP64 kernel runs over the list,
-        // so its warps hold only candidates it may keep (molecules: every
+        // atoms: an FP32 pre-pass marks the candidates below the cutoff (by the
+        // margin scr gives, else 100 times below), and a compaction lists the
+        // others (with scr), so the FP64 kernel's warps hold only candidates it may
+        // keep; without a list it skips the marked ones in place (molecules: every
         // candidate in FP64)
         const int pre = J.mol.on ? 0 : 1;
         const bool listed = pre && scr && compact_blocks(nb * J.n_cand) + 1 <= scr->block_cap;
-        const float log_margin = listed ? -0.22314355f : -4.6051702f;  // log(0.8), log(1/100)
+        const float log_margin = scr ? scr->log_margin : -4.6051702f;  // log(1/100)
         int launches = pre ? launch_spa_prefilter(J, b0, nb, kd, kz, batches, log_margin, flag, sm_count, s) : 0;
         if (listed)
             launches += launch_compact(flag + b0 * J.n_cand, nb * J.n_cand, scr->list, scr->block_sums,
