@@ -24,6 +24,11 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=o
           "-I" + HERE, "-I" + os.path.join(ROOT, "include"), "--expt-relaxed-constexpr"]
 UNITS = {
     "api.cu": ["--fmad=false"],
+    "job.cu": ["--fmad=false"],
+    "pipeline.cu": ["--fmad=false"],
+    "tune.cu": ["--fmad=false"],
+    "batch.cu": ["--fmad=false"],
+    "server.cu": ["--fmad=false"],
     "sampler.cu": ["--fmad=false"],
     "integrate_fp64.cu": ["--fmad=false"],
     "deposit.cu": ["--fmad=false"],
